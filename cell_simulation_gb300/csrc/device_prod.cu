@@ -1,0 +1,871 @@
+// device_prod.cu — production (Philox) RDME step: one fused, persistent
+// launch per frame over a (replicate, tile) work queue.
+//
+// Each work item is a column of TY x TZ voxels in the (y, z) plane spanning
+// x in [x0, x1) of one replicate.  The CTA rolls along x with rings of
+// shared-memory planes ((TY+2) x (TZ+2) windows with a one-voxel halo for
+// slots, two voxels for region codes):
+//   load     plane i+1 from HBM (16-byte vector loads for K = 16), and decide
+//            its x-moves while the content is in registers;
+//   X sweep  plane i from raw planes i-1, i, i+1 (the only cross-plane
+//            dependency), then decide y-moves of the result;
+//   Y sweep  in-plane, then decide z-moves;
+//   Z sweep  in-plane, then reactions (SSA within tau) and the store of the
+//            interior to the destination lattice.
+// Every lattice byte is read once and written once per frame (plus the halo
+// re-reads of neighbouring tiles, which mostly hit L2); species-count deltas
+// are reduced per CTA in shared memory and added to the per-replicate counts
+// with one atomic per species per work item.
+//
+// Frame bookkeeping lives on the device so a captured two-frame CUDA graph
+// can be replayed: the launch reads its frame number from stepbuf[parity]
+// and writes frame+1 to stepbuf[parity^1]; work counters alternate the same
+// way, each launch resetting the one the next launch will use.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "cuda_check.h"
+#include "internal.h"
+#include "prod_common.cuh"
+
+namespace cellsim {
+
+struct ProdParams {
+    ProdTables T;
+    const RepDesc* reps;
+    const WorkItem* items;
+    uint32_t n_items;
+    uint32_t parity;
+    uint32_t* counters;  // [2]
+    uint32_t* stepbuf;   // [2]
+    const uint8_t* src;
+    uint8_t* dst;
+    const uint8_t* region_code;
+    const uint8_t* reservoir;  // may be null
+    unsigned long long* counts;  // [n_rep][S1]
+    uint32_t* diag;
+};
+
+template <int K, int TY, int TZ>
+struct Tile {
+    static constexpr int WY = TY + 2, WZ = TZ + 2, WIN = WY * WZ;
+    static constexpr int RWY = TY + 4, RWZ = TZ + 4, RWIN = RWY * RWZ;
+    static constexpr size_t vox_bytes = (size_t)(4 + 2) * WIN * K;    // raw[4], xp, yp
+    static constexpr size_t dec_bytes = (size_t)(4 + 2) * WIN * 4;    // decx[4], decy, decz
+    static constexpr size_t reg_bytes = ((size_t)4 * RWIN + 15) / 16 * 16;
+    static size_t smem(uint32_t S1) { return vox_bytes + dec_bytes + reg_bytes + (size_t)(S1 + PD_N) * 4; }
+};
+
+template <int K>
+__device__ __forceinline__ Vox<K> ld_vox(const uint8_t* p) {
+    Vox<K> c;
+    if (K == 16) {
+        uint4 t = __ldg(reinterpret_cast<const uint4*>(p));
+        c.w[0] = (uint64_t)t.x | ((uint64_t)t.y << 32);
+        c.w[K / 8 - 1] = (uint64_t)t.z | ((uint64_t)t.w << 32);
+    } else {
+        uint2 t = __ldg(reinterpret_cast<const uint2*>(p));
+        c.w[0] = (uint64_t)t.x | ((uint64_t)t.y << 32);
+    }
+    return c;
+}
+
+template <int K>
+__device__ __forceinline__ void st_vox(uint8_t* p, const Vox<K>& c) {
+    if (K == 16) {
+        uint4 t;
+        t.x = (uint32_t)c.w[0]; t.y = (uint32_t)(c.w[0] >> 32);
+        t.z = (uint32_t)c.w[K / 8 - 1]; t.w = (uint32_t)(c.w[K / 8 - 1] >> 32);
+        *reinterpret_cast<uint4*>(p) = t;
+    } else {
+        uint2 t;
+        t.x = (uint32_t)c.w[0]; t.y = (uint32_t)(c.w[0] >> 32);
+        *reinterpret_cast<uint2*>(p) = t;
+    }
+}
+
+template <int K, int TY, int TZ, int NT>
+__global__ void __launch_bounds__(NT) prod_step_kernel(ProdParams P) {
+    using C = Tile<K, TY, TZ>;
+    constexpr int WZ = C::WZ, WIN = C::WIN, RWZ = C::RWZ, RWIN = C::RWIN;
+    extern __shared__ __align__(16) uint8_t smem[];
+    Vox<K>* raw = reinterpret_cast<Vox<K>*>(smem);  // [4][WIN]
+    Vox<K>* xp = raw + 4 * WIN;
+    Vox<K>* yp = xp + WIN;
+    uint32_t* decx = reinterpret_cast<uint32_t*>(smem + C::vox_bytes);  // [4][WIN]
+    uint32_t* decy = decx + 4 * WIN;
+    uint32_t* decz = decy + WIN;
+    uint8_t* reg = smem + C::vox_bytes + C::dec_bytes;  // [4][RWIN]
+    int32_t* s_delta = reinterpret_cast<int32_t*>(smem + C::vox_bytes + C::dec_bytes + C::reg_bytes);
+    uint32_t* s_diag = reinterpret_cast<uint32_t*>(s_delta + P.T.S1);
+    __shared__ uint32_t s_item;
+
+    const int tid = threadIdx.x;
+    const uint32_t frame = P.stepbuf[P.parity];
+    if (blockIdx.x == 0 && tid == 0) {
+        P.counters[P.parity ^ 1u] = 0u;
+        P.stepbuf[P.parity ^ 1u] = frame + 1u;
+    }
+    for (int i = tid; i < PD_N; i += NT) s_diag[i] = 0u;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = atomicAdd(P.counters + P.parity, 1u);
+        __syncthreads();
+        const uint32_t it = s_item;
+        if (it >= P.n_items) break;
+        const WorkItem wi = P.items[it];
+        const RepDesc rd = P.reps[wi.rep];
+        const int X = (int)rd.X, Y = (int)rd.Y, Z = (int)rd.Z;
+        const int y0 = (int)wi.y0, z0 = (int)wi.z0, x0 = (int)wi.x0, x1 = (int)wi.x1;
+        const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
+        const uint8_t* src = P.src + rd.base * K;
+        uint8_t* dst = P.dst + rd.base * K;
+        const uint8_t* rcode = P.region_code + rd.base;
+        const uint8_t* resv = P.reservoir ? P.reservoir + rd.base : nullptr;
+        const uint32_t YZ = (uint32_t)Y * (uint32_t)Z;
+        for (uint32_t s = tid; s < P.T.S1; s += NT) s_delta[s] = 0;
+
+        auto reg_plane = [&](int p) -> uint8_t* { return reg + ((p + 8) & 3) * RWIN; };
+        auto load_reg = [&](int p) {
+            uint8_t* rp = reg_plane(p);
+            for (int e = tid; e < RWIN; e += NT) {
+                int ry = e / RWZ, rz = e - ry * RWZ;
+                int y = y0 - 2 + ry, z = z0 - 2 + rz;
+                uint8_t code = 0;
+                if (p >= 0 && p < X && y >= 0 && y < Y && z >= 0 && z < Z)
+                    code = rcode[((uint64_t)p * Y + y) * Z + z];
+                rp[e] = code;
+            }
+        };
+        // load raw plane p and decide its x-moves
+        auto load_raw = [&](int p) {
+            Vox<K>* cp = raw + ((p + 4) & 3) * WIN;
+            uint32_t* dp = decx + ((p + 4) & 3) * WIN;
+            const uint8_t* rs_p = reg_plane(p);
+            const uint8_t* rlo_p = reg_plane(p - 1);
+            const uint8_t* rhi_p = reg_plane(p + 1);
+            for (int e = tid; e < WIN; e += NT) {
+                int wy = e / WZ, wz = e - wy * WZ;
+                int y = y0 - 1 + wy, z = z0 - 1 + wz;
+                Vox<K> c = vox_zero<K>();
+                uint32_t d = 0;
+                if (p >= 0 && p < X && y >= 0 && y < Y && z >= 0 && z < Z) {
+                    uint32_t v = ((uint32_t)p * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
+                    c = ld_vox<K>(src + (uint64_t)v * K);
+                    if (!vox_empty<K>(c)) {
+                        int ri = (wy + 1) * RWZ + wz + 1;
+                        d = decide_moves<K>(c, v, frame, 0u, rs_p[ri], rlo_p[ri], rhi_p[ri], k0, k1, P.T);
+                    }
+                }
+                cp[e] = c;
+                dp[e] = d;
+            }
+        };
+
+        // prologue: regions x0-2..x0+1, raw x0-1 and x0 with their x-decisions
+        for (int p = x0 - 2; p <= x0 + 1; p++) load_reg(p);
+        __syncthreads();
+        load_raw(x0 - 1);
+        load_raw(x0);
+        __syncthreads();
+        for (int i = x0; i < x1; i++) {
+            load_reg(i + 2);
+            __syncthreads();
+            load_raw(i + 1);
+            __syncthreads();
+            // ---- X sweep of plane i, then y-decisions of the result
+            {
+                const Vox<K>* rlo = raw + ((i + 3) & 3) * WIN;
+                const Vox<K>* rme = raw + ((i + 4) & 3) * WIN;
+                const Vox<K>* rhi = raw + ((i + 5) & 3) * WIN;
+                const uint32_t* dlo = decx + ((i + 3) & 3) * WIN;
+                const uint32_t* dme = decx + ((i + 4) & 3) * WIN;
+                const uint32_t* dhi = decx + ((i + 5) & 3) * WIN;
+                const uint8_t* rg = reg_plane(i);
+                for (int e = tid; e < WIN; e += NT) {
+                    int wy = e / WZ, wz = e - wy * WZ;
+                    int y = y0 - 1 + wy, z = z0 - 1 + wz;
+                    uint32_t v = ((uint32_t)i * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
+                    uint32_t a = dme[e], b = dlo[e], c2 = dhi[e];
+                    Vox<K> own = rme[e];
+                    Vox<K> r = own;
+                    if ((a | (b >> 16) | (c2 & 0xFFFFu)) != 0u)
+                        r = combine<K>(own, a, rlo[e], b, rhi[e], c2, v, v - YZ, v + YZ, frame, 0u);
+                    xp[e] = r;
+                    uint32_t d = 0;
+                    if (!vox_empty<K>(r)) {
+                        int ri = (wy + 1) * RWZ + wz + 1;
+                        d = decide_moves<K>(r, v, frame, 1u, rg[ri], rg[ri - RWZ], rg[ri + RWZ], k0, k1, P.T);
+                    }
+                    decy[e] = d;
+                }
+            }
+            __syncthreads();
+            // ---- Y sweep (interior rows), then z-decisions
+            {
+                const uint8_t* rg = reg_plane(i);
+                for (int e = tid + WZ; e < WIN - WZ; e += NT) {
+                    int wy = e / WZ, wz = e - wy * WZ;
+                    int y = y0 - 1 + wy, z = z0 - 1 + wz;
+                    uint32_t v = ((uint32_t)i * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
+                    uint32_t a = decy[e], b = decy[e - WZ], c2 = decy[e + WZ];
+                    Vox<K> own = xp[e];
+                    Vox<K> r = own;
+                    if ((a | (b >> 16) | (c2 & 0xFFFFu)) != 0u)
+                        r = combine<K>(own, a, xp[e - WZ], b, xp[e + WZ], c2, v, v - (uint32_t)Z, v + (uint32_t)Z, frame, 1u);
+                    yp[e] = r;
+                    uint32_t d = 0;
+                    if (!vox_empty<K>(r)) {
+                        int ri = (wy + 1) * RWZ + wz + 1;
+                        d = decide_moves<K>(r, v, frame, 2u, rg[ri], rg[ri - 1], rg[ri + 1], k0, k1, P.T);
+                    }
+                    decz[e] = d;
+                }
+            }
+            __syncthreads();
+            // ---- Z sweep of the interior, reactions, store
+            {
+                float mult = rd.rate_mult;
+                for (int t = tid; t < TY * TZ; t += NT) {
+                    int ty = t / TZ, tz = t - ty * TZ;
+                    int y = y0 + ty, z = z0 + tz;
+                    if (y >= Y || z >= Z) continue;
+                    int e = (ty + 1) * WZ + tz + 1;
+                    uint32_t v = ((uint32_t)i * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
+                    uint32_t a = decz[e], b = decz[e - 1], c2 = decz[e + 1];
+                    Vox<K> own = yp[e];
+                    Vox<K> r = own;
+                    if ((a | (b >> 16) | (c2 & 0xFFFFu)) != 0u)
+                        r = combine<K>(own, a, yp[e - 1], b, yp[e + 1], c2, v, v - 1u, v + 1u, frame, 2u);
+                    uint32_t rv = resv ? (uint32_t)resv[v] : 0u;
+                    if (rv != 0u || P.T.n_zero_order != 0u || !vox_empty<K>(r))
+                        react_voxel<K>(r, rv, v, frame, k0, k1, mult, P.T, s_delta, s_diag);
+                    st_vox<K>(dst + (uint64_t)v * K, r);
+                }
+            }
+            __syncthreads();
+        }
+        // flush this work item's count deltas
+        for (uint32_t s = tid; s < P.T.S1; s += NT) {
+            int32_t d = s_delta[s];
+            if (d) atomicAdd(P.counts + (size_t)rd.counts_index * P.T.S1 + s, (unsigned long long)(long long)d);
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < PD_N; i += NT)
+        if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
+}
+
+// ------------------------------------------------------------------ configs
+
+typedef void (*ProdKernelFn)(ProdParams);
+
+struct KernelCfg {
+    int K, TY, TZ, NT;
+    ProdKernelFn fn;
+    size_t (*smem)(uint32_t);
+};
+
+template <int K, int TY, int TZ, int NT>
+static KernelCfg make_cfg() {
+    return KernelCfg{K, TY, TZ, NT, prod_step_kernel<K, TY, TZ, NT>, &Tile<K, TY, TZ>::smem};
+}
+
+static const std::vector<KernelCfg>& all_cfgs() {
+    static const std::vector<KernelCfg> v = {
+        make_cfg<16, 8, 32, 256>(), make_cfg<16, 4, 64, 256>(), make_cfg<16, 16, 32, 256>(), make_cfg<16, 8, 64, 256>(),
+        make_cfg<8, 8, 32, 256>(),  make_cfg<8, 4, 64, 256>(),  make_cfg<8, 16, 32, 256>(),  make_cfg<8, 8, 64, 256>(),
+    };
+    return v;
+}
+
+// ------------------------------------------------------------------ host side
+
+struct DeviceProd {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t K = 16, S1 = 1, R = 0, NC = 1, n_rep = 0;
+    uint64_t total_voxels = 0;
+    int num_sms = 1;
+    std::vector<RepDesc> h_reps;
+    DevBuf<RepDesc> reps;
+    DevBuf<uint8_t> slots[2];
+    DevBuf<uint8_t> region_code, reservoir;
+    DevBuf<uint32_t> thr;
+    DevBuf<uint8_t> rx_reactants, rx_ch_sp, one_list;
+    DevBuf<int8_t> rx_ch_d;
+    DevBuf<float> rx_rate;
+    DevBuf<uint16_t> one_off;
+    DevBuf<unsigned long long> counts;
+    DevBuf<uint32_t> diag, counters, stepbuf;
+    DevBuf<WorkItem> items;      // batched order
+    DevBuf<WorkItem> items_rep;  // grouped per replicate (plain launches)
+    std::vector<uint32_t> rep_item_off;
+    uint32_t n_items = 0;
+    int cur = 0;
+    ProdTables T{};
+    int cfg_index = -1;
+    uint32_t seg_len = 0;
+    uint64_t cur_seed = 0;
+    bool seed_set = false;
+    cudaGraphExec_t graph = nullptr;
+    int graph_cfg = -1;
+    ~DeviceProd() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+static uint32_t threshold_of(double D, double tau, double lambda) {
+    double p = D * tau / (lambda * lambda);
+    if (!(p > 0.0)) return 0u;
+    if (p >= 1.0) return 0xFFFFFFFFu;
+    double t = std::floor(p * 4294967296.0);
+    return t >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t;
+}
+
+// Builds the shared reaction/diffusion tables of the production path.
+static void build_tables(DeviceProd* d, const Model& m) {
+    d->K = m.K;
+    d->S1 = m.n_species + 1;
+    d->R = m.n_reactions;
+    d->NC = m.nr + 1;
+    if (m.K != 8 && m.K != 16) throw Error(CS_ERR_LIMIT, "the production path supports max_particles_site 8 or 16");
+    if (m.nr > 254) throw Error(CS_ERR_LIMIT, "at most 254 regions on the production path");
+    std::vector<uint32_t> thr((size_t)d->NC * d->NC * d->S1, 0u);
+    for (uint32_t a = 1; a < d->NC; a++)
+        for (uint32_t b = 1; b < d->NC; b++)
+            for (uint32_t q = 0; q < d->S1; q++) {
+                double D = m.diffusion[((size_t)(a - 1) * m.nr + (b - 1)) * m.np + q];
+                double p = D * (double)m.tau / ((double)m.lambda * (double)m.lambda);
+                if (p > 0.5) throw Error(CS_ERR_INVALID_ARG, "D*tau/lambda^2 exceeds 1/2 for some species and region pair: the per-axis sweep needs tau <= lambda^2/(2 D)");
+                thr[((size_t)a * d->NC + b) * d->S1 + q] = threshold_of(D, m.tau, m.lambda);
+            }
+    std::vector<uint8_t> rre(3 * std::max<uint32_t>(d->R, 1), 0), csp(8 * std::max<uint32_t>(d->R, 1), 0);
+    std::vector<int8_t> cdl(8 * std::max<uint32_t>(d->R, 1), 0);
+    std::vector<float> rate(std::max<uint32_t>(d->R, 1), 0.0f);
+    for (uint32_t r = 0; r < d->R; r++) {
+        for (int j = 0; j < 3; j++) rre[3 * r + j] = (uint8_t)m.reactants[(size_t)(r + 1) * 3 + j];
+        rate[r] = m.rates[r + 1];
+        if (!(rate[r] >= 0.0f)) throw Error(CS_ERR_INVALID_ARG, "reaction rates must be non-negative on the production path");
+        int n = 0;
+        for (uint32_t s = 1; s < d->S1; s++) {
+            int32_t v = m.stoich[(size_t)(r + 1) * d->S1 + s];
+            if (!v) continue;
+            if (n >= 8 || v < -127 || v > 127) throw Error(CS_ERR_LIMIT, "a reaction may change at most 8 species by at most 127");
+            csp[8 * r + n] = (uint8_t)s;
+            cdl[8 * r + n] = (int8_t)v;
+            n++;
+        }
+    }
+    // reactions possible with exactly one particle q (q = 0: empty voxel)
+    std::vector<uint16_t> off(d->S1 + 1, 0);
+    std::vector<uint8_t> lst;
+    for (uint32_t q = 0; q < d->S1; q++) {
+        off[q] = (uint16_t)lst.size();
+        for (uint32_t r = 0; r < d->R; r++) {
+            uint32_t nv = 0, nq = 0;
+            for (int j = 0; j < 3; j++) {
+                uint32_t s = rre[3 * r + j];
+                if (s) { nv++; nq += (s == q); }
+            }
+            if (nv == 0 || (q != 0 && nv == 1 && nq == 1)) lst.push_back((uint8_t)r);
+        }
+    }
+    off[d->S1] = (uint16_t)lst.size();
+    uint32_t n_zero = off[1] - off[0];
+    if (lst.empty()) lst.push_back(0);
+    d->thr.alloc(thr.size());
+    d->rx_reactants.alloc(rre.size());
+    d->rx_ch_sp.alloc(csp.size());
+    d->rx_ch_d.alloc(cdl.size());
+    d->rx_rate.alloc(rate.size());
+    d->one_off.alloc(off.size());
+    d->one_list.alloc(lst.size());
+    CS_CUDA(cudaMemcpy(d->thr.p, thr.data(), thr.size() * 4, cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->rx_reactants.p, rre.data(), rre.size(), cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->rx_ch_sp.p, csp.data(), csp.size(), cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->rx_ch_d.p, cdl.data(), cdl.size(), cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->rx_rate.p, rate.data(), rate.size() * 4, cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->one_off.p, off.data(), off.size() * 2, cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->one_list.p, lst.data(), lst.size(), cudaMemcpyHostToDevice));
+    ProdTables& T = d->T;
+    T.S1 = d->S1;
+    T.R = d->R;
+    T.NC = d->NC;
+    T.K = d->K;
+    T.tau = m.tau;
+    T.tau_d = (double)m.tau;
+    T.precision = CS_PREC_MIXED;
+    T.max_events = 64;
+    T.n_zero_order = n_zero;
+    T.thr = d->thr.p;
+    T.rx_reactants = d->rx_reactants.p;
+    T.rx_rate = d->rx_rate.p;
+    T.rx_ch_sp = d->rx_ch_sp.p;
+    T.rx_ch_d = d->rx_ch_d.p;
+    T.one_off = d->one_off.p;
+    T.one_list = d->one_list.p;
+}
+
+static int pick_default_cfg(uint32_t K) {
+    const auto& c = all_cfgs();
+    for (size_t i = 0; i < c.size(); i++)
+        if (c[i].K == (int)K && c[i].TY == 8 && c[i].TZ == 32) return (int)i;
+    return -1;
+}
+
+// Work items for the current tile config: (replicate, y0, z0, x-segment).
+static void build_items(DeviceProd* d) {
+    const KernelCfg& cfg = all_cfgs()[d->cfg_index];
+    std::vector<WorkItem> all, per_rep;
+    d->rep_item_off.assign(d->n_rep + 1, 0);
+    // target: enough items to keep every SM busy with a few in flight
+    uint64_t cols_total = 0;
+    for (auto& r : d->h_reps) cols_total += (uint64_t)((r.Y + cfg.TY - 1) / cfg.TY) * ((r.Z + cfg.TZ - 1) / cfg.TZ);
+    uint64_t want = (uint64_t)d->num_sms * 8;
+    for (uint32_t ri = 0; ri < d->n_rep; ri++) {
+        const RepDesc& r = d->h_reps[ri];
+        d->rep_item_off[ri] = (uint32_t)per_rep.size();
+        uint32_t nseg = 1;
+        if (d->seg_len) nseg = (r.X + d->seg_len - 1) / d->seg_len;
+        else if (cols_total < want) nseg = (uint32_t)std::min<uint64_t>((want + cols_total - 1) / cols_total, std::max<uint32_t>(r.X / 16, 1));
+        uint32_t seg = (r.X + nseg - 1) / nseg;
+        for (uint32_t x0 = 0; x0 < r.X; x0 += seg)
+            for (uint32_t y0 = 0; y0 < r.Y; y0 += cfg.TY)
+                for (uint32_t z0 = 0; z0 < r.Z; z0 += cfg.TZ) {
+                    WorkItem w{};
+                    w.rep = ri; w.y0 = y0; w.z0 = z0; w.x0 = x0; w.x1 = std::min(r.X, x0 + seg);
+                    per_rep.push_back(w);
+                }
+    }
+    d->rep_item_off[d->n_rep] = (uint32_t)per_rep.size();
+    all = per_rep;
+    // batched order: largest work first (longest processing time first)
+    std::stable_sort(all.begin(), all.end(), [&](const WorkItem& a, const WorkItem& b) {
+        uint64_t wa = (uint64_t)(a.x1 - a.x0), wb = (uint64_t)(b.x1 - b.x0);
+        return wa > wb;
+    });
+    d->n_items = (uint32_t)all.size();
+    d->items.alloc(all.size());
+    d->items_rep.alloc(per_rep.size());
+    CS_CUDA(cudaMemcpy(d->items.p, all.data(), all.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->items_rep.p, per_rep.data(), per_rep.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+}
+
+static void set_cfg(DeviceProd* d, int idx) {
+    const KernelCfg& cfg = all_cfgs()[idx];
+    size_t sm = cfg.smem(d->S1);
+    CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    d->cfg_index = idx;
+    build_items(d);
+    if (d->graph) {
+        cudaGraphExecDestroy(d->graph);
+        d->graph = nullptr;
+    }
+}
+
+static int grid_for(DeviceProd* d, uint32_t n_items) {
+    const KernelCfg& cfg = all_cfgs()[d->cfg_index];
+    int per_sm = 0;
+    CS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg.fn, cfg.NT, cfg.smem(d->S1)));
+    if (per_sm < 1) throw Error(CS_ERR_CUDA, "production kernel does not fit on an SM");
+    return (int)std::min<uint64_t>((uint64_t)per_sm * d->num_sms, n_items);
+}
+
+// One frame over all replicates (batched) or over replicate `rep` alone.
+static void launch_frame(DeviceProd* d, int parity, int rep) {
+    const KernelCfg& cfg = all_cfgs()[d->cfg_index];
+    ProdParams P{};
+    P.T = d->T;
+    P.reps = d->reps.p;
+    P.parity = (uint32_t)parity;
+    P.stepbuf = d->stepbuf.p;
+    P.src = d->slots[parity].p;
+    P.dst = d->slots[parity ^ 1].p;
+    P.region_code = d->region_code.p;
+    P.reservoir = d->reservoir.n ? d->reservoir.p : nullptr;
+    P.counts = d->counts.p;
+    P.diag = d->diag.p;
+    if (rep < 0) {
+        P.items = d->items.p;
+        P.n_items = d->n_items;
+        P.counters = d->counters.p;
+    } else {
+        P.items = d->items_rep.p + d->rep_item_off[rep];
+        P.n_items = d->rep_item_off[rep + 1] - d->rep_item_off[rep];
+        P.counters = d->counters.p + 2 * (1 + rep);
+    }
+    int grid = grid_for(d, P.n_items);
+    cfg.fn<<<grid, cfg.NT, cfg.smem(d->S1), d->stream>>>(P);
+    CS_LAUNCH_CHECK();
+}
+
+static DeviceProd* prod_alloc(const Model& m, int device, const std::vector<RepDesc>& reps, uint64_t total_voxels) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        throw Error(CS_ERR_CUDA, "no CUDA device available (libcellsim has no CPU fallback)");
+    if (device < 0 || device >= ndev) throw Error(CS_ERR_INVALID_ARG, "device index out of range");
+    DeviceGuard g(device);
+    std::unique_ptr<DeviceProd> d(new DeviceProd());
+    d->device = device;
+    CS_CUDA(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+    CS_CUDA(cudaDeviceGetAttribute(&d->num_sms, cudaDevAttrMultiProcessorCount, device));
+    build_tables(d.get(), m);
+    d->h_reps = reps;
+    d->n_rep = (uint32_t)reps.size();
+    d->total_voxels = total_voxels;
+    d->reps.alloc(reps.size());
+    CS_CUDA(cudaMemcpy(d->reps.p, reps.data(), reps.size() * sizeof(RepDesc), cudaMemcpyHostToDevice));
+    for (int b = 0; b < 2; b++) d->slots[b].alloc(total_voxels * d->K);
+    d->region_code.alloc(total_voxels);
+    d->counts.alloc((size_t)d->n_rep * d->S1);
+    d->diag.alloc(PD_N);
+    d->counters.alloc(2 * (1 + d->n_rep));
+    d->stepbuf.alloc(2);
+    CS_CUDA(cudaMemset(d->diag.p, 0, PD_N * 4));
+    CS_CUDA(cudaMemset(d->counters.p, 0, d->counters.bytes()));
+    CS_CUDA(cudaMemset(d->stepbuf.p, 0, 8));
+    CS_CUDA(cudaMemset(d->counts.p, 0, d->counts.bytes()));
+    int ci = pick_default_cfg(d->K);
+    if (ci < 0) throw Error(CS_ERR_LIMIT, "no kernel configuration for this K");
+    set_cfg(d.get(), ci);
+    return d.release();
+}
+
+DeviceProd* prod_create(const Model& m, int device) {
+    m.check_tables();
+    RepDesc r{};
+    r.base = 0;
+    r.X = m.res[0]; r.Y = m.res[1]; r.Z = m.res[2];
+    r.seed_lo = 0; r.seed_hi = 0;
+    r.rate_mult = 1.0f;
+    r.counts_index = 0;
+    std::unique_ptr<DeviceProd> d(prod_alloc(m, device, {r}, m.V));
+    DeviceGuard g(device);
+    std::vector<uint8_t> rc(m.V);
+    bool any_res = false;
+    for (uint64_t v = 0; v < m.V; v++) {
+        rc[v] = (uint8_t)(m.regions[v] + 1);
+        any_res |= m.reservoir[v] != 0;
+    }
+    CS_CUDA(cudaMemcpy(d->region_code.p, rc.data(), m.V, cudaMemcpyHostToDevice));
+    if (any_res) {
+        std::vector<uint8_t> r8(m.V);
+        for (uint64_t v = 0; v < m.V; v++) r8[v] = (uint8_t)m.reservoir[v];
+        d->reservoir.alloc(m.V);
+        CS_CUDA(cudaMemcpy(d->reservoir.p, r8.data(), m.V, cudaMemcpyHostToDevice));
+    }
+    prod_set_lattice(d.get(), m, m.slots.data());
+    return d.release();
+}
+
+void prod_destroy(DeviceProd* d) {
+    if (!d) return;
+    cudaSetDevice(d->device);
+    if (d->stream) cudaStreamSynchronize(d->stream);
+    delete d;
+}
+
+// Uploads a reference-layout lattice (u32 slots) for replicate 0, compacting
+// each voxel's slots, and resets the species counts to slots + reservoirs.
+void prod_set_lattice(DeviceProd* d, const Model& m, const uint32_t* slots) {
+    DeviceGuard g(d->device);
+    uint64_t V = m.V;
+    std::vector<uint8_t> s8(V * d->K, 0);
+    std::vector<long long> cnt(d->S1, 0);
+    for (uint64_t v = 0; v < V; v++) {
+        uint32_t j = 0;
+        for (uint32_t k = 0; k < m.K; k++) {
+            uint32_t q = slots[v * m.K + k];
+            if (q > 255u) throw Error(CS_ERR_LIMIT, "slot value above 255");
+            if (q) { s8[v * d->K + j++] = (uint8_t)q; cnt[q]++; }
+        }
+        if (m.reservoir[v]) cnt[m.reservoir[v]]++;
+    }
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    d->cur = 0;
+    CS_CUDA(cudaMemcpy(d->slots[0].p, s8.data(), s8.size(), cudaMemcpyHostToDevice));
+    std::vector<unsigned long long> c(d->S1);
+    for (uint32_t s = 0; s < d->S1; s++) c[s] = (unsigned long long)cnt[s];
+    CS_CUDA(cudaMemcpy(d->counts.p, c.data(), c.size() * 8, cudaMemcpyHostToDevice));
+}
+
+void prod_get_lattice(DeviceProd* d, const Model& m, uint32_t* slots, uint32_t* occ, int32_t* conc) {
+    DeviceGuard g(d->device);
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    uint64_t V = m.V;
+    std::vector<uint8_t> s8(V * d->K);
+    CS_CUDA(cudaMemcpy(s8.data(), d->slots[d->cur].p, s8.size(), cudaMemcpyDeviceToHost));
+    for (uint64_t v = 0; v < V; v++) {
+        uint32_t n = 0;
+        if (conc)
+            for (uint32_t s = 0; s < d->S1; s++) conc[v * d->S1 + s] = 0;
+        for (uint32_t k = 0; k < d->K; k++) {
+            uint32_t q = s8[v * d->K + k];
+            if (slots && k < m.K) slots[v * m.K + k] = q;
+            if (q) {
+                n++;
+                if (conc) conc[v * d->S1 + q] += 1;
+            }
+        }
+        if (occ) occ[v] = n;
+        if (conc && m.reservoir[v]) conc[v * d->S1 + m.reservoir[v]] = 1;
+    }
+}
+
+void prod_seed(DeviceProd* d, uint64_t seed) {
+    if (d->seed_set && seed == d->cur_seed) return;
+    for (auto& r : d->h_reps) {
+        r.seed_lo = (uint32_t)seed;
+        r.seed_hi = (uint32_t)(seed >> 32);
+    }
+    CS_CUDA(cudaMemcpyAsync(d->reps.p, d->h_reps.data(), d->h_reps.size() * sizeof(RepDesc), cudaMemcpyHostToDevice,
+                            d->stream));
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    d->cur_seed = seed;
+    d->seed_set = true;
+}
+
+// Runs n frames; batched = one launch per frame over all replicates (a
+// captured two-frame graph replays pairs), otherwise one launch per replicate.
+static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched);
+
+static void run_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched) {
+    if (n == 0) return;
+    uint32_t f32 = (uint32_t)frame0;
+    CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, &f32, 4, cudaMemcpyHostToDevice, d->stream));
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    run_frames_nosync(d, n, batched);
+}
+
+// Enqueues n frames; the frame number must already be in stepbuf[cur].
+static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched) {
+    uint32_t k = 0;
+    if (batched) {
+        if (d->cur == 1 && k < n) {
+            launch_frame(d, 1, -1);
+            d->cur = 0;
+            k++;
+        }
+        if (n - k >= 2) {
+            if (!d->graph || d->graph_cfg != d->cfg_index) {
+                if (d->graph) { cudaGraphExecDestroy(d->graph); d->graph = nullptr; }
+                cudaGraph_t g;
+                CS_CUDA(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
+                launch_frame(d, 0, -1);
+                launch_frame(d, 1, -1);
+                CS_CUDA(cudaStreamEndCapture(d->stream, &g));
+                CS_CUDA(cudaGraphInstantiate(&d->graph, g, 0));
+                cudaGraphDestroy(g);
+                d->graph_cfg = d->cfg_index;
+            }
+            while (n - k >= 2) {
+                CS_CUDA(cudaGraphLaunch(d->graph, d->stream));
+                k += 2;
+            }
+        }
+        if (k < n) {
+            launch_frame(d, 0, -1);
+            d->cur = 1;
+            k++;
+        }
+    } else {
+        for (; k < n; k++) {
+            for (uint32_t r = 0; r < d->n_rep; r++) launch_frame(d, d->cur, (int)r);
+            d->cur ^= 1;
+        }
+    }
+}
+
+void prod_step(DeviceProd* d, uint32_t n_steps, uint64_t seed, int precision, uint64_t frame0, uint32_t write_freq,
+               const std::vector<uint32_t>& logging, std::vector<cs_stat_sample>& samples) {
+    DeviceGuard g(d->device);
+    if (n_steps == 0) return;
+    prod_seed(d, seed);
+    if (d->T.precision != precision) {
+        d->T.precision = precision;
+        if (d->graph) { cudaGraphExecDestroy(d->graph); d->graph = nullptr; }
+    }
+    std::vector<uint64_t> sample_frames;
+    if (write_freq)
+        for (uint64_t f = frame0; f < frame0 + n_steps; f++)
+            if (f > 0 && f % write_freq == 0) sample_frames.push_back(f);
+    uint64_t f = frame0, end = frame0 + n_steps;
+    std::vector<unsigned long long> snap;
+    std::vector<std::vector<unsigned long long>> taken;
+    for (uint64_t sf : sample_frames) {
+        run_frames(d, (uint32_t)(sf - f), f, true);
+        f = sf;
+        std::vector<unsigned long long> h(d->S1);
+        CS_CUDA(cudaMemcpyAsync(h.data(), d->counts.p, d->S1 * 8, cudaMemcpyDeviceToHost, d->stream));
+        CS_CUDA(cudaStreamSynchronize(d->stream));
+        for (uint32_t sp : logging) samples.push_back(cs_stat_sample{sp, (int32_t)(long long)h[sp], (uint32_t)sf});
+    }
+    run_frames(d, (uint32_t)(end - f), f, true);
+}
+
+void prod_get_counts(DeviceProd* d, int64_t* counts) {
+    DeviceGuard g(d->device);
+    std::vector<unsigned long long> h((size_t)d->n_rep * d->S1);
+    CS_CUDA(cudaMemcpyAsync(h.data(), d->counts.p, h.size() * 8, cudaMemcpyDeviceToHost, d->stream));
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    for (size_t i = 0; i < h.size(); i++) counts[i] = (int64_t)h[i];
+}
+
+void prod_get_diag(DeviceProd* d, uint32_t* diag, uint32_t n) {
+    DeviceGuard g(d->device);
+    uint32_t h[PD_N];
+    CS_CUDA(cudaMemcpyAsync(h, d->diag.p, sizeof(h), cudaMemcpyDeviceToHost, d->stream));
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    for (uint32_t i = 0; i < n; i++) diag[i] = i < PD_N ? h[i] : 0u;
+}
+
+void prod_sync(DeviceProd* d) {
+    DeviceGuard g(d->device);
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+}
+
+}  // namespace cellsim
+
+namespace cellsim {
+
+// ------------------------------------------------------------------ ensemble
+
+// Replicates of one model on lattices of their own resolution, filled with
+// region 0 of the model and with counts[s] particles of species s placed
+// uniformly at random (append-at-occupancy rule of src/lattice.rs:280-290,
+// up to 100 draws per particle as in src/lattice.rs:66-95).
+DeviceProd* prod_ensemble_create(const Model& m, uint32_t n, const uint32_t* res, const uint64_t* seeds, const float* mult,
+                                 const uint32_t* init_counts, int device) {
+    if (n == 0) throw Error(CS_ERR_INVALID_ARG, "an ensemble needs at least one replicate");
+    std::vector<RepDesc> reps(n);
+    uint64_t base = 0;
+    for (uint32_t r = 0; r < n; r++) {
+        RepDesc& d = reps[r];
+        std::memset(&d, 0, sizeof(d));
+        d.X = res[3 * r]; d.Y = res[3 * r + 1]; d.Z = res[3 * r + 2];
+        if (!d.X || !d.Y || !d.Z) throw Error(CS_ERR_INVALID_ARG, "replicate resolution must be positive");
+        uint64_t V = (uint64_t)d.X * d.Y * d.Z;
+        if (V * m.K >= (1ull << 32)) throw Error(CS_ERR_LIMIT, "replicate too large (V*K must be below 2^32)");
+        d.base = base;
+        d.seed_lo = (uint32_t)seeds[r];
+        d.seed_hi = (uint32_t)(seeds[r] >> 32);
+        d.rate_mult = mult ? mult[r] : 1.0f;
+        d.counts_index = r;
+        base += V;
+    }
+    std::unique_ptr<DeviceProd> d(prod_alloc(m, device, reps, base));
+    DeviceGuard g(device);
+    d->seed_set = true;  // per-replicate seeds, never overwritten by prod_seed
+    d->cur_seed = ~0ull;
+    CS_CUDA(cudaMemset(d->region_code.p, 1, base));  // region 0 -> code 1
+    std::vector<unsigned long long> cnt((size_t)n * d->S1, 0ull);
+    for (uint32_t r = 0; r < n; r++) {
+        const RepDesc& rd = reps[r];
+        uint64_t V = (uint64_t)rd.X * rd.Y * rd.Z;
+        std::vector<uint8_t> s8(V * d->K, 0), occ(V, 0);
+        HostRng rng;
+        rng.seed(seeds[r] ^ 0xA5A5A5A5DEADBEEFull);
+        for (uint32_t s = 1; s < d->S1; s++) {
+            for (uint32_t i = 0; i < init_counts[s]; i++) {
+                int tries = 0;
+                for (; tries < 100; tries++) {
+                    uint64_t v = rng.below(V);
+                    if (occ[v] < d->K) {
+                        s8[v * d->K + occ[v]++] = (uint8_t)s;
+                        break;
+                    }
+                }
+                if (tries == 100) throw Error(CS_ERR_CAPACITY, "could not place a particle in replicate " + std::to_string(r));
+            }
+            cnt[(size_t)r * d->S1 + s] = init_counts[s];
+        }
+        CS_CUDA(cudaMemcpy(d->slots[0].p + rd.base * d->K, s8.data(), s8.size(), cudaMemcpyHostToDevice));
+    }
+    CS_CUDA(cudaMemcpy(d->counts.p, cnt.data(), cnt.size() * 8, cudaMemcpyHostToDevice));
+    d->cur = 0;
+    return d.release();
+}
+
+void prod_ensemble_step(DeviceProd* d, uint32_t n_steps, bool batched, uint64_t frame0) {
+    DeviceGuard g(d->device);
+    run_frames(d, n_steps, frame0, batched);
+}
+
+void prod_set_precision(DeviceProd* d, int precision) {
+    if (d->T.precision != precision) {
+        d->T.precision = precision;
+        if (d->graph) { cudaGraphExecDestroy(d->graph); d->graph = nullptr; }
+    }
+}
+
+uint64_t prod_total_voxels(const DeviceProd* d) { return d->total_voxels; }
+uint32_t prod_n_items(const DeviceProd* d) { return d->n_items; }
+uint32_t prod_n_replicates(const DeviceProd* d) { return d->n_rep; }
+uint32_t prod_s1(const DeviceProd* d) { return d->S1; }
+
+// Downloads the packed slots of every replicate (K bytes per voxel).
+void prod_get_slots_raw(DeviceProd* d, uint8_t* out) {
+    DeviceGuard g(d->device);
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    CS_CUDA(cudaMemcpy(out, d->slots[d->cur].p, d->total_voxels * d->K, cudaMemcpyDeviceToHost));
+}
+
+// Tile configuration: index into the compiled (K, TY, TZ) variants and the
+// x-segment length (0 = automatic).
+void prod_set_tiling(DeviceProd* d, int cfg_index, uint32_t seg_len) {
+    DeviceGuard g(d->device);
+    const auto& c = all_cfgs();
+    if (cfg_index < 0 || cfg_index >= (int)c.size() || c[cfg_index].K != (int)d->K)
+        throw Error(CS_ERR_INVALID_ARG, "tile configuration does not exist for this K");
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    d->seg_len = seg_len;
+    set_cfg(d, cfg_index);
+}
+
+int prod_tiling_count() { return (int)all_cfgs().size(); }
+void prod_tiling_desc(int i, int* K, int* TY, int* TZ, int* NT) {
+    const auto& c = all_cfgs();
+    if (i < 0 || i >= (int)c.size()) throw Error(CS_ERR_INVALID_ARG, "tile configuration index out of range");
+    *K = c[i].K; *TY = c[i].TY; *TZ = c[i].TZ; *NT = c[i].NT;
+}
+int prod_tiling_current(const DeviceProd* d) { return d->cfg_index; }
+cudaStream_t prod_stream(const DeviceProd* d) { return d->stream; }
+
+}  // namespace cellsim
+
+namespace cellsim {
+// Runs n frames between two CUDA events recorded on the handle's stream and
+// returns the elapsed device time in milliseconds (blocks until done).
+float prod_time_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched) {
+    DeviceGuard g(d->device);
+    cudaEvent_t a, b;
+    CS_CUDA(cudaEventCreate(&a));
+    CS_CUDA(cudaEventCreate(&b));
+    float ms = 0.0f;
+    try {
+        // the frame-number upload inside run_frames synchronises; record after it
+        uint32_t f32 = (uint32_t)frame0;
+        CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, &f32, 4, cudaMemcpyHostToDevice, d->stream));
+        CS_CUDA(cudaStreamSynchronize(d->stream));
+        CS_CUDA(cudaEventRecord(a, d->stream));
+        run_frames_nosync(d, n, batched);
+        CS_CUDA(cudaEventRecord(b, d->stream));
+        CS_CUDA(cudaEventSynchronize(b));
+        CS_CUDA(cudaEventElapsedTime(&ms, a, b));
+    } catch (...) {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        throw;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms;
+}
+}  // namespace cellsim

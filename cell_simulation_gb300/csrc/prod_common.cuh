@@ -1,0 +1,364 @@
+// prod_common.cuh — per-voxel operations of the production (Philox) step,
+// shared by the fused tile kernel.  The algorithm (restated on the CPU in
+// oracle/prod_semantics.c) is:
+//
+//  Diffusion, three sweeps per frame (x, then y, then z).  In the sweep
+//  along axis a every particle of voxel v (slot s of its compacted content)
+//  draws u = Philox(v, frame, sweep<<24 | s/4)[s%4] and moves to v-a when
+//  u < T[r(v)][r(v-a)][q], to v+a when T[.][r(v-a)][q] <= u < that + T[r(v)][r(v+a)][q],
+//  where T = floor(D*tau/lambda^2 * 2^32) for the region codes (id+1; code 0
+//  = outside the lattice, all thresholds 0) -- the move probabilities of
+//  rdme.wgsl:132-136.  Capacity: the free room K - n(w) of a receiving voxel
+//  w is split between its lower neighbour (ceil or floor half, alternating
+//  with the parity of w + frame + sweep) and its upper neighbour; the first
+//  movers in slot order up to that share are accepted, the rest stay.  The
+//  new content of w is its staying particles (slot order), then accepted
+//  arrivals from the lower neighbour, then from the upper neighbour.  A
+//  voxel's new content therefore depends only on itself and its two
+//  neighbours along the axis, never on arrival order, so the result is
+//  independent of tiling and thread scheduling.
+//
+//  Reactions: an exact SSA (Gillespie direct method) inside each voxel over
+//  one tau, with FP32 propensities and FP32 exponential waiting times, an
+//  FP64 clock, and FP64 cumulative selection when max/min non-zero
+//  propensity exceeds 1e6 (or always, or never, by precision mode).  A
+//  reaction that would exceed K particles is rejected.  If anything fired,
+//  the voxel's slots are rewritten species-major (cme.wgsl:90-97).
+#pragma once
+#include <cstdint>
+
+#include "devmath.cuh"
+
+namespace cellsim {
+
+enum { PD_EVENTS = 0, PD_REJECT_CAP = 1, PD_EVENT_CAP = 2, PD_FP64_SEL = 3, PD_N = 8 };
+
+struct RepDesc {
+    uint64_t base;  // first voxel of this replicate in the packed arrays
+    uint32_t X, Y, Z;
+    uint32_t seed_lo, seed_hi;
+    float rate_mult;
+    uint32_t counts_index;  // replicate index into the counts array
+    uint32_t pad[7];
+};
+
+struct WorkItem {
+    uint32_t rep, y0, z0, x0, x1, pad[3];
+};
+
+struct ProdTables {
+    uint32_t S1, R, NC, K;
+    float tau;
+    int32_t precision;  // cs_precision
+    uint32_t max_events;
+    uint32_t n_zero_order;  // reactions without reactants (fire in empty voxels)
+    double tau_d;
+    const uint32_t* thr;          // [NC][NC][S1]
+    const uint8_t* rx_reactants;  // [R][3]
+    const float* rx_rate;         // [R]
+    const uint8_t* rx_ch_sp;      // [R][8]
+    const int8_t* rx_ch_d;        // [R][8]
+    const uint16_t* one_off;      // [S1+1] offsets into one_list
+    const uint8_t* one_list;      // reactions possible in a voxel holding exactly one particle q (or none, q = 0)
+};
+
+// K slot bytes held in 64-bit words, byte s = slot s.
+template <int K>
+struct alignas(K) Vox {
+    uint64_t w[K / 8];
+};
+
+template <int K>
+__device__ __forceinline__ Vox<K> vox_zero() {
+    Vox<K> c;
+#pragma unroll
+    for (int i = 0; i < K / 8; i++) c.w[i] = 0;
+    return c;
+}
+
+__device__ __forceinline__ uint32_t nz64(uint64_t x) {
+    x |= x >> 4;
+    x |= x >> 2;
+    x |= x >> 1;
+    return (uint32_t)__popcll(x & 0x0101010101010101ull);
+}
+
+template <int K>
+__device__ __forceinline__ uint32_t vox_n(const Vox<K>& c) {
+    uint32_t n = 0;
+#pragma unroll
+    for (int i = 0; i < K / 8; i++) n += nz64(c.w[i]);
+    return n;
+}
+
+template <int K>
+__device__ __forceinline__ bool vox_empty(const Vox<K>& c) {
+    uint64_t o = 0;
+#pragma unroll
+    for (int i = 0; i < K / 8; i++) o |= c.w[i];
+    return o == 0;
+}
+
+template <int K>
+__device__ __forceinline__ uint32_t vox_get(const Vox<K>& c, uint32_t i) {
+    if (K == 8) return (uint32_t)(c.w[0] >> (8 * i)) & 0xFFu;
+    uint64_t w = (i < 8) ? c.w[0] : c.w[K / 8 - 1];
+    return (uint32_t)(w >> (8 * (i & 7))) & 0xFFu;
+}
+
+template <int K>
+__device__ __forceinline__ void vox_or(Vox<K>& c, uint32_t i, uint32_t q) {
+    if (K == 8 || i < 8) c.w[0] |= (uint64_t)q << (8 * (i & 7));
+    else c.w[K / 8 - 1] |= (uint64_t)q << (8 * (i & 7));
+}
+
+template <int K>
+__device__ __forceinline__ void vox_set(Vox<K>& c, uint32_t i, uint32_t q) {
+    uint64_t m = ~(0xFFull << (8 * (i & 7)));
+    if (K == 8 || i < 8) c.w[0] = (c.w[0] & m) | ((uint64_t)q << (8 * (i & 7)));
+    else c.w[K / 8 - 1] = (c.w[K / 8 - 1] & m) | ((uint64_t)q << (8 * (i & 7)));
+}
+
+template <int K>
+__device__ __forceinline__ uint32_t vox_count(const Vox<K>& c, uint32_t q) {
+    uint32_t rep = q * 0x01010101u, n = 0;
+#pragma unroll
+    for (int i = 0; i < K / 8; i++)
+        n += __popc(__vcmpeq4((uint32_t)c.w[i], rep)) + __popc(__vcmpeq4((uint32_t)(c.w[i] >> 32), rep));
+    return n >> 3;
+}
+
+// Keep the c lowest set bits of m.
+__device__ __forceinline__ uint32_t lowest_bits(uint32_t m, uint32_t c) {
+    while ((uint32_t)__popc(m) > c) m &= ~(0x80000000u >> __clz(m));
+    return m;
+}
+
+// Move decisions of one voxel for one sweep: bit s = slot s moves to the
+// lower neighbour, bit 16+s = to the upper neighbour.
+template <int K>
+__device__ __forceinline__ uint32_t decide_moves(const Vox<K>& c, uint32_t v, uint32_t frame, uint32_t sweep, uint32_t rs,
+                                                 uint32_t rlo, uint32_t rhi, uint32_t k0, uint32_t k1, const ProdTables& T) {
+    uint32_t n = vox_n<K>(c);
+    if (n == 0) return 0u;
+    const uint32_t* tlo = T.thr + ((size_t)rs * T.NC + rlo) * T.S1;
+    const uint32_t* thi = T.thr + ((size_t)rs * T.NC + rhi) * T.S1;
+    uint32_t mask = 0, group = 0xFFFFFFFFu;
+    U4 ph{0, 0, 0, 0};
+    for (uint32_t s = 0; s < n; s++) {
+        uint32_t q = vox_get<K>(c, s);
+        uint32_t tm = __ldg(tlo + q), tp = __ldg(thi + q);
+        if ((tm | tp) == 0u) continue;
+        if ((s >> 2) != group) {
+            group = s >> 2;
+            ph = d_philox(v, frame, (sweep << 24) | group, 0u, k0, k1);
+        }
+        uint32_t u = (s & 3u) == 0u ? ph.x : (s & 3u) == 1u ? ph.y : (s & 3u) == 2u ? ph.z : ph.w;
+        if (u < tm) mask |= 1u << s;
+        else if ((uint64_t)u < (uint64_t)tm + tp) mask |= 1u << (16 + s);
+    }
+    return mask;
+}
+
+// New content of a voxel after one sweep.
+template <int K>
+__device__ __forceinline__ Vox<K> combine(const Vox<K>& own, uint32_t down, const Vox<K>& lo, uint32_t dlo, const Vox<K>& hi,
+                                          uint32_t dhi, uint32_t v_self, uint32_t v_lo, uint32_t v_hi, uint32_t frame,
+                                          uint32_t sweep) {
+    uint32_t in_lo = dlo >> 16, in_hi = dhi & 0xFFFFu;
+    if ((down | in_lo | in_hi) == 0u) return own;
+    uint32_t n_self = vox_n<K>(own);
+    uint32_t room = K - n_self;
+    uint32_t share_lo = (room + ((v_self + frame + sweep) & 1u)) >> 1, share_hi = room - share_lo;
+    uint32_t acc_lo = lowest_bits(in_lo, share_lo), acc_hi = lowest_bits(in_hi, share_hi);
+    uint32_t out_m = down & 0xFFFFu, out_p = down >> 16;
+    if (out_m) {
+        uint32_t room_l = K - vox_n<K>(lo);
+        uint32_t sh = room_l - ((room_l + ((v_lo + frame + sweep) & 1u)) >> 1);
+        out_m = lowest_bits(out_m, sh);
+    }
+    if (out_p) {
+        uint32_t room_h = K - vox_n<K>(hi);
+        uint32_t sl = (room_h + ((v_hi + frame + sweep) & 1u)) >> 1;
+        out_p = lowest_bits(out_p, sl);
+    }
+    uint32_t keep = ((1u << n_self) - 1u) & ~(out_m | out_p);
+    Vox<K> r = vox_zero<K>();
+    uint32_t j = 0;
+    while (keep) {
+        uint32_t s = __ffs(keep) - 1;
+        keep &= keep - 1;
+        vox_or<K>(r, j++, vox_get<K>(own, s));
+    }
+    while (acc_lo) {
+        uint32_t s = __ffs(acc_lo) - 1;
+        acc_lo &= acc_lo - 1;
+        vox_or<K>(r, j++, vox_get<K>(lo, s));
+    }
+    while (acc_hi) {
+        uint32_t s = __ffs(acc_hi) - 1;
+        acc_hi &= acc_hi - 1;
+        vox_or<K>(r, j++, vox_get<K>(hi, s));
+    }
+    return r;
+}
+
+// Propensity of reaction r (0-based) for the voxel content c.
+template <int K>
+__device__ __forceinline__ float propensity(const ProdTables& T, uint32_t r, const Vox<K>& c, uint32_t resv, float mult) {
+    const uint8_t* re = T.rx_reactants + 3 * r;
+    uint32_t s0 = __ldg(re), s1 = __ldg(re + 1), s2 = __ldg(re + 2);
+    uint32_t ff = 1;
+    uint32_t sp[3] = {s0, s1, s2};
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        uint32_t s = sp[j];
+        if (s == 0) continue;
+        uint32_t m = 0;
+#pragma unroll
+        for (int i = 0; i < j; i++) m += sp[i] == s;
+        uint32_t cnt = (s == resv) ? 1u : vox_count<K>(c, s);
+        if (cnt <= m) return 0.0f;
+        ff *= cnt - m;
+    }
+    return __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), (float)ff);
+}
+
+// SSA within tau for one voxel.  Returns true when any reaction fired (the
+// content is then rewritten species-major).  s_delta[S1] and s_diag[PD_N]
+// are block-shared accumulators.
+template <int K>
+__device__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0, uint32_t k1, float mult,
+                            const ProdTables& T, int32_t* s_delta, uint32_t* s_diag) {
+    if (T.R == 0) return false;
+    uint32_t n = vox_n<K>(c);
+    bool fast_ok = (resv == 0u);
+    if (fast_ok && n == 0u) {
+        uint32_t q0 = 0;
+        if (__ldg(T.one_off + q0 + 1) == __ldg(T.one_off + q0)) return false;  // no zero-order reaction
+    }
+    double td = 0.0;
+    float tf = 0.0f;
+    bool fired = false;
+    uint32_t ev = 0;
+    for (; ev < T.max_events; ev++) {
+        bool fast = fast_ok && n <= 1u;
+        uint32_t q = (n == 1u) ? vox_get<K>(c, 0) : 0u;
+        uint32_t lb = 0, le = T.R;
+        if (fast) { lb = __ldg(T.one_off + q); le = __ldg(T.one_off + q + 1); }
+        float a0 = 0.0f, amax = 0.0f, amin = __int_as_float(0x7f800000);
+        for (uint32_t k = lb; k < le; k++) {
+            uint32_t r = fast ? (uint32_t)__ldg(T.one_list + k) : k;
+            float a = fast ? __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), 1.0f) : propensity<K>(T, r, c, resv, mult);
+            a0 = __fadd_rn(a0, a);
+            if (a > 0.0f) { amax = fmaxf(amax, a); amin = fminf(amin, a); }
+        }
+        if (!(a0 > 0.0f)) break;
+        U4 ph = d_philox(v, frame, (3u << 24) | (ev >> 1), 0u, k0, k1);
+        uint32_t w1 = (ev & 1u) ? ph.z : ph.x, w2 = (ev & 1u) ? ph.w : ph.y;
+        float u1 = __fmul_rn((float)((w1 >> 8) + 1u), 0x1p-24f);
+        float dt = __fdiv_rn(-d_logf(u1), a0);
+        if (T.precision == 1) {
+            tf = __fadd_rn(tf, dt);
+            if (tf > T.tau) break;
+        } else {
+            td = __dadd_rn(td, (double)dt);
+            if (td > T.tau_d) break;
+        }
+        float u2 = __fmul_rn((float)(w2 >> 8), 0x1p-24f);
+        bool use64 = (T.precision == 2) || (T.precision == 0 && amax > __fmul_rn(1e6f, amin));
+        int sel = -1;
+        int last_pos = -1;
+        if (!use64) {
+            float target = __fmul_rn(u2, a0), run = 0.0f;
+            for (uint32_t k = lb; k < le; k++) {
+                uint32_t r = fast ? (uint32_t)__ldg(T.one_list + k) : k;
+                float a = fast ? __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), 1.0f) : propensity<K>(T, r, c, resv, mult);
+                if (a > 0.0f) last_pos = (int)r;
+                run = __fadd_rn(run, a);
+                if (target < run) { sel = (int)r; break; }
+            }
+        } else {
+            atomicAdd(s_diag + PD_FP64_SEL, 1u);
+            double a0d = 0.0;
+            for (uint32_t k = lb; k < le; k++) {
+                uint32_t r = fast ? (uint32_t)__ldg(T.one_list + k) : k;
+                float a = fast ? __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), 1.0f) : propensity<K>(T, r, c, resv, mult);
+                a0d = __dadd_rn(a0d, (double)a);
+            }
+            double target = __dmul_rn((double)u2, a0d), run = 0.0;
+            for (uint32_t k = lb; k < le; k++) {
+                uint32_t r = fast ? (uint32_t)__ldg(T.one_list + k) : k;
+                float a = fast ? __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), 1.0f) : propensity<K>(T, r, c, resv, mult);
+                if (a > 0.0f) last_pos = (int)r;
+                run = __dadd_rn(run, (double)a);
+                if (target < run) { sel = (int)r; break; }
+            }
+        }
+        if (sel < 0) sel = last_pos;
+        if (sel < 0) break;
+        // apply the change list, skipping the voxel's reservoir species
+        const uint8_t* csp = T.rx_ch_sp + 8 * sel;
+        const int8_t* cd = T.rx_ch_d + 8 * sel;
+        int total = (int)n;
+        bool ok = true;
+        for (int j = 0; j < 8; j++) {
+            uint32_t s = __ldg(csp + j);
+            if (s == 0) break;
+            if (s == resv) continue;
+            int d = __ldg(cd + j);
+            int have = (int)vox_count<K>(c, s);
+            if (have + d < 0) ok = false;
+            total += d;
+        }
+        if (!ok || total > (int)K) {
+            atomicAdd(s_diag + PD_REJECT_CAP, 1u);
+            continue;
+        }
+        // removals first, so that the content never exceeds K slots in between
+        for (int pass = 0; pass < 2; pass++) {
+            for (int j = 0; j < 8; j++) {
+                uint32_t s = __ldg(csp + j);
+                if (s == 0) break;
+                if (s == resv) continue;
+                int d = __ldg(cd + j);
+                if (pass == 0) {
+                    for (; d < 0; d++) {  // remove one occurrence: move the last particle into its slot
+                        uint32_t idx = 0;
+                        for (uint32_t i = 0; i < n; i++)
+                            if (vox_get<K>(c, i) == s) idx = i;
+                        vox_set<K>(c, idx, vox_get<K>(c, n - 1));
+                        vox_set<K>(c, n - 1, 0u);
+                        n--;
+                    }
+                } else {
+                    for (; d > 0; d--) vox_set<K>(c, n++, s);
+                    atomicAdd(s_delta + s, __ldg(cd + j));
+                }
+            }
+        }
+        atomicAdd(s_diag + PD_EVENTS, 1u);
+        fired = true;
+    }
+    if (ev == T.max_events) atomicAdd(s_diag + PD_EVENT_CAP, 1u);
+    if (fired) {
+        // species-major rewrite, ascending species id
+        Vox<K> out = vox_zero<K>();
+        uint32_t j = 0, prev = 0;
+        for (;;) {
+            uint32_t best = 256;
+            for (uint32_t i = 0; i < n; i++) {
+                uint32_t b = vox_get<K>(c, i);
+                if (b > prev && b < best) best = b;
+            }
+            if (best == 256) break;
+            uint32_t cnt = vox_count<K>(c, best);
+            for (uint32_t k = 0; k < cnt; k++) vox_or<K>(out, j++, best);
+            prev = best;
+        }
+        c = out;
+    }
+    return fired;
+}
+
+}  // namespace cellsim

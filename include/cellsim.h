@@ -1,0 +1,257 @@
+/*
+ * cellsim.h — C ABI of libcellsim, the GB300 (sm_103a) implementation of the
+ * RDME timestep of javirk/cell_simulation: lattice diffusion, per-voxel
+ * reactions, slot compaction and species counts.
+ *
+ * This header is the drop-in boundary for the reference's wgpu compute path.
+ * Every entry point names the reference interface it replaces (paths are
+ * relative to the reference project).  Conventions:
+ *   - every call returns cs_status (0 = CS_OK); cs_last_error() returns a
+ *     thread-local message for the last failing call on this thread;
+ *   - no exception, panic or abort crosses the ABI;
+ *   - all arrays are caller-allocated host memory in the reference layout
+ *     (logical C order, voxel index v = (x*Y + y)*Z + z, slot s at v*K + s);
+ *     device memory is owned by the library;
+ *   - a cs_sim handle owns one CUDA stream on one device and is not
+ *     thread-safe (the reference's Simulation is used through &mut self);
+ *   - there is no CPU fallback: device calls fail with CS_ERR_CUDA when no
+ *     usable GPU is present.
+ */
+#ifndef CELLSIM_H
+#define CELLSIM_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CELLSIM_ABI_VERSION 1
+
+typedef int32_t cs_status;
+enum {
+    CS_OK = 0,
+    CS_ERR_INVALID_ARG = 1,  /* null pointer, bad size, bad enum            */
+    CS_ERR_NOT_FOUND = 2,    /* unknown region or species name              */
+    CS_ERR_LIMIT = 3,        /* K, species, regions or reactions too large  */
+    CS_ERR_STATE = 4,        /* call out of order (e.g. step before prepare)*/
+    CS_ERR_PARSE = 5,        /* malformed JSON model                        */
+    CS_ERR_IO = 6,           /* file could not be read                      */
+    CS_ERR_CUDA = 7,         /* CUDA runtime error or no device             */
+    CS_ERR_CAPACITY = 8,     /* host placement could not fit a particle     */
+    CS_ERR_DEVICE_STATUS = 9 /* a kernel reported a failure status          */
+};
+
+typedef struct cs_sim cs_sim;
+typedef struct cs_ensemble cs_ensemble;
+
+/* LatticeParams::new(dimensions, resolution, tau, lambda),
+ * src/lattice_params.rs:97-118; max_particles_site is the reference's
+ * compile-time MAX_PARTICLES_SITE (src/lib.rs:15), a run-time value here
+ * (1..16; the production path takes 8 or 16). */
+typedef struct {
+    float dims[3];
+    uint32_t res[3];
+    float tau;
+    float lambda;
+    uint32_t max_particles_site;
+} cs_lattice_params;
+
+/* RegionType, src/region.rs:10-20. */
+typedef enum {
+    CS_REGION_CUBE = 0,
+    CS_REGION_SPHERE = 1,
+    CS_REGION_SEMISPHERE = 2,
+    CS_REGION_CYLINDER = 3,
+    CS_REGION_SPHERICAL_SHELL = 4,
+    CS_REGION_CYLINDRICAL_SHELL = 5,
+    CS_REGION_CAPSID = 6
+} cs_region_type;
+
+/* Payload of a RegionType variant; fields a variant does not use are ignored. */
+typedef struct {
+    int32_t type;               /* cs_region_type                                   */
+    const char* name;           /* Cube, Sphere, SemiSphere, Cylinder               */
+    const char* shell_name;     /* SphericalShell, CylindricalShell, Capsid         */
+    const char* interior_name;  /* SphericalShell, CylindricalShell, Capsid         */
+    float p0[3], pf[3];         /* Cube, Cylinder, CylindricalShell                 */
+    float center[3];            /* Sphere, SemiSphere, SphericalShell, Capsid       */
+    float direction[3];         /* SemiSphere `direction`, Capsid `dir`             */
+    float radius;               /* Sphere, SemiSphere, Cylinder                     */
+    float internal_radius;      /* shells, Capsid                                   */
+    float external_radius;      /* shells, Capsid                                   */
+    float total_length;         /* Capsid                                           */
+} cs_region_desc;
+
+typedef enum {
+    CS_RNG_REFERENCE = 0, /* the reference's PCG/xorshift stream keyed by itime; bit-exact */
+    CS_RNG_PHILOX = 1     /* production path: Philox4x32-10, x/y/z sweeps, SSA within tau */
+} cs_rng_mode;
+
+typedef enum {
+    CS_PREC_MIXED = 0, /* FP32 propensities/waiting times, FP64 clock, FP64 selection past 6 decades */
+    CS_PREC_FP32 = 1,  /* everything FP32 (precision comparisons)                                  */
+    CS_PREC_FP64 = 2   /* FP32 propensities, FP64 clock and FP64 selection always                  */
+} cs_precision;
+
+typedef struct {
+    uint32_t res[3];
+    uint32_t max_particles_site;
+    uint32_t n_regions;
+    uint32_t n_species;    /* S, excluding the void species 0 */
+    uint32_t n_reactions;  /* R, excluding the dummy row 0    */
+    uint32_t n_logging;
+    uint64_t n_voxels;
+    uint64_t frame;        /* frames stepped since prepare     */
+    float tau;
+    float lambda;
+    float dims[3];
+    int32_t rng_mode;      /* -1 before cs_prepare_for_gpu     */
+    int32_t device;
+} cs_info;
+
+/* SolverStatisticSample<i32>, src/statistics.rs:4-9 (name -> species index). */
+typedef struct {
+    uint32_t species;
+    int32_t value;
+    uint32_t iteration_count;
+} cs_stat_sample;
+
+/* ---------------- lifecycle ---------------- */
+const char* cs_version(void);
+const char* cs_last_error(void);
+/* Simulation::new, src/simulation.rs:51-97 */
+cs_status cs_create(const cs_lattice_params* params, cs_sim** out);
+/* Simulation::from_file, src/simulation.rs:210-232 (model part; no texture) */
+cs_status cs_from_json_file(const char* path, uint64_t placement_seed, cs_sim** out);
+cs_status cs_from_json_string(const char* json, uint64_t placement_seed, cs_sim** out);
+void cs_destroy(cs_sim* sim);
+/* Seeds the host placement RNG that replaces rand::thread_rng
+ * (src/lattice.rs:65) so that models are reproducible. */
+cs_status cs_seed_placement(cs_sim* sim, uint64_t seed);
+
+/* ---------------- model building (host) ---------------- */
+/* Simulation::add_region, src/simulation.rs:428-481 */
+cs_status cs_add_region(cs_sim* sim, const cs_region_desc* region, float diffusion_rate);
+/* Simulation::prepare_regions, src/simulation.rs:424-426 -> Regions::prepare_regions, src/region.rs:129-148 */
+cs_status cs_prepare_regions(cs_sim* sim);
+/* Simulation::add_particle_count, src/simulation.rs:792-814 */
+cs_status cs_add_particle_count(cs_sim* sim, const char* name, const char* to_region, uint32_t count,
+                                int32_t logging, int32_t is_reservoir);
+/* Simulation::add_particle_concentration, src/simulation.rs:816-823 */
+cs_status cs_add_particle_concentration(cs_sim* sim, const char* name, const char* to_region,
+                                        float concentration, int32_t logging, int32_t is_reservoir);
+/* Simulation::fill_region, src/simulation.rs:825-840 */
+cs_status cs_fill_region(cs_sim* sim, const char* name, const char* to_region, int32_t logging);
+/* Simulation::set_diffusion_rate, src/simulation.rs:867-874 */
+cs_status cs_set_diffusion_rate(cs_sim* sim, const char* region, float rate);
+/* Simulation::set_diffusion_rate_particle, src/simulation.rs:877-882 */
+cs_status cs_set_diffusion_rate_particle(cs_sim* sim, const char* particle, const char* region, float rate);
+/* Simulation::set_transition_rate, src/simulation.rs:885-893 */
+cs_status cs_set_transition_rate(cs_sim* sim, const char* from_region, const char* to_region, float rate);
+/* Simulation::set_transition_rate_particle, src/simulation.rs:896-902 */
+cs_status cs_set_transition_rate_particle(cs_sim* sim, const char* particle, const char* from_region,
+                                          const char* to_region, float rate);
+/* Simulation::add_reaction, src/simulation.rs:904-947 */
+cs_status cs_add_reaction(cs_sim* sim, const char* const* reactants, uint32_t n_reactants,
+                          const char* const* products, uint32_t n_products, float k);
+
+/* ---------------- introspection ---------------- */
+cs_status cs_get_info(const cs_sim* sim, cs_info* out);
+/* Copies the tables the shaders bind (src/simulation.rs:1156-1254); every
+ * pointer may be NULL.  Sizes: regions[V], diffusion[NReg*NReg*(S+1)],
+ * stoich[(R+1)*(S+1)], reactants[(R+1)*3], rates[R+1], reservoir[V]. */
+cs_status cs_get_tables(const cs_sim* sim, uint32_t* regions, float* diffusion, int32_t* stoich,
+                        uint32_t* reactants, float* rates, uint32_t* reservoir);
+/* Regions::volumes, src/region.rs:90 (NReg entries). */
+cs_status cs_get_region_volumes(const cs_sim* sim, uint32_t* volumes);
+/* kind 0 = species name (index 0 = "void"), 1 = region name, 2 = logged species index */
+cs_status cs_get_name(const cs_sim* sim, int32_t kind, uint32_t index, char* buf, uint32_t buf_len);
+
+/* ---------------- reference-layout state (drop-in buffers) ---------------- */
+/* Replaces all tables with prebuilt reference-layout arrays (the buffers
+ * created in Simulation::prepare_for_gpu, src/simulation.rs:152-208).
+ * Invalidates device state. */
+cs_status cs_set_tables(cs_sim* sim, uint32_t n_regions, uint32_t n_species, uint32_t n_reactions,
+                        const uint32_t* regions, const float* diffusion, const int32_t* stoich,
+                        const uint32_t* reactants, const float* rates, const uint32_t* reservoir);
+/* Lattice state: slots u32[V*K] (Lattice::lattice, src/lattice.rs:15),
+ * occupancy u32[V] and concentrations i32[V*(S+1)].  occupancy and
+ * concentrations may be NULL in cs_set_lattice, in which case they are
+ * derived from the slots (plus 1 for each reservoir species).  After
+ * cs_prepare_for_gpu the state lives on the device and these calls copy to
+ * or from it. */
+cs_status cs_set_lattice(cs_sim* sim, const uint32_t* slots, const uint32_t* occupancy,
+                         const int32_t* concentrations);
+cs_status cs_get_lattice(cs_sim* sim, uint32_t* slots, uint32_t* occupancy, int32_t* concentrations);
+
+/* ---------------- device ---------------- */
+/* Simulation::prepare_for_gpu, src/simulation.rs:152-208: allocates device
+ * buffers on `device`, uploads the model and initialises the species counts
+ * from the concentrations (create_statistics, src/simulation.rs:361-388). */
+cs_status cs_prepare_for_gpu(cs_sim* sim, int32_t rng_mode, int32_t device);
+/* Simulation::step, src/simulation.rs:99-150, driving RDME::step
+ * (src/rdme.rs:46-76) and CME::step (src/cme.rs:47-79) for n_steps frames
+ * in CS_RNG_REFERENCE mode.  itimes[n_steps] are the per-frame Uniform.itime
+ * values (src/uniforms.rs:8-14).  Before frame f with f > 0 and
+ * f % write_freq == 0 the logged species counts are sampled
+ * (start_error_buffer_readbacks, src/simulation.rs:391-418); write_freq 0
+ * disables sampling.  Returns after the work is enqueued. */
+cs_status cs_step(cs_sim* sim, uint32_t n_steps, const uint32_t* itimes, uint32_t write_freq);
+/* Production path (CS_RNG_PHILOX): n_steps frames keyed by `seed`. */
+cs_status cs_step_philox(cs_sim* sim, uint32_t n_steps, uint64_t seed, uint32_t write_freq);
+/* Precision form of the production path (cs_precision). */
+cs_status cs_set_precision(cs_sim* sim, int32_t precision);
+/* Global species counts, StatisticsGroup buffer 0 (src/statistics.rs:11-69):
+ * counts[S+1]; synchronises the stream. */
+cs_status cs_get_counts(cs_sim* sim, int64_t* counts);
+/* Drains the recorded samples (Simulation::stats, src/simulation.rs:36). */
+cs_status cs_pop_stats(cs_sim* sim, cs_stat_sample* out, uint32_t capacity, uint32_t* n_out);
+/* Diagnostic counters: capacity spills, occupancy range,
+ * serial-resolution steps, rollbacks, fired voxels, ... */
+cs_status cs_get_diagnostics(cs_sim* sim, uint32_t* diag, uint32_t n);
+cs_status cs_synchronize(cs_sim* sim);
+
+/* ---------------- timing and tiling (production path) ---------------- */
+/* Enqueue n frames between two CUDA events recorded on the handle's stream
+ * and return the device time in milliseconds (blocks until done).  No
+ * reference counterpart (the reference only prints FPS,
+ * examples/no_window.rs:141-163). */
+cs_status cs_step_timed(cs_sim* sim, uint32_t n_steps, const uint32_t* itimes, float* ms);
+cs_status cs_step_philox_timed(cs_sim* sim, uint32_t n_steps, uint64_t seed, float* ms);
+/* Compiled (K, TY, TZ, threads) variants of the fused step kernel and the
+ * x-segment length of a work item (0 = automatic); used by the autotuner. */
+cs_status cs_tiling_count(int32_t* n);
+cs_status cs_tiling_describe(int32_t index, int32_t* K, int32_t* TY, int32_t* TZ, int32_t* threads);
+cs_status cs_set_tiling(cs_sim* sim, int32_t index, uint32_t segment_length);
+cs_status cs_get_tiling(const cs_sim* sim, int32_t* index);
+
+/* ---------------- batched ensemble (production path) ---------------- */
+/* Replicates of one model on lattices of uneven sizes, all stepped by one
+ * persistent launch per frame over a (replicate, tile) work queue.  The
+ * model's species, reactions and region-0 diffusion rates are shared; each
+ * replicate is one region-0 lattice of resolution res[3r..3r+2] with its own
+ * Philox seed and reaction-rate multiplier, filled uniformly with
+ * initial_counts[s] particles of species s (initial_counts[S+1]).  No
+ * reference counterpart: the reference runs one Simulation per lattice. */
+cs_status cs_ensemble_create(const cs_sim* model, uint32_t n_replicates, const uint32_t* res, const uint64_t* seeds,
+                             const float* rate_multipliers, const uint32_t* initial_counts, int32_t device,
+                             cs_ensemble** out);
+void cs_ensemble_destroy(cs_ensemble* ens);
+/* batched != 0: one launch per frame for all replicates (CUDA-graph replayed);
+ * batched == 0: one launch per replicate per frame (the plain path). */
+cs_status cs_ensemble_step(cs_ensemble* ens, uint32_t n_steps, int32_t batched);
+cs_status cs_ensemble_step_timed(cs_ensemble* ens, uint32_t n_steps, int32_t batched, float* ms);
+cs_status cs_ensemble_set_precision(cs_ensemble* ens, int32_t precision);
+cs_status cs_ensemble_set_tiling(cs_ensemble* ens, int32_t index, uint32_t segment_length);
+/* counts[n_replicates][S+1] */
+cs_status cs_ensemble_get_counts(cs_ensemble* ens, int64_t* counts);
+/* packed slots of all replicates in order, K bytes per voxel */
+cs_status cs_ensemble_get_slots(cs_ensemble* ens, uint8_t* slots);
+cs_status cs_ensemble_get_diagnostics(cs_ensemble* ens, uint32_t* diag, uint32_t n);
+cs_status cs_ensemble_synchronize(cs_ensemble* ens);
+cs_status cs_ensemble_info(const cs_ensemble* ens, uint64_t* total_voxels, uint32_t* n_work_items);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,73 @@
+"""Shared fixtures: small models and state extraction for oracle/library comparisons."""
+from __future__ import annotations
+
+import numpy as np
+
+from cell_simulation_gb300 import configs
+from cell_simulation_gb300.simulation import LatticeParams, RegionType, Simulation
+
+LAM = configs.LAMBDA
+
+
+def itime_schedule(n, seed=987654321, stride=7919):
+    """Per-frame itime values itime_f = seed + stride * f (u32 wrap)."""
+    return ((np.uint64(seed) + np.uint64(stride) * np.arange(n, dtype=np.uint64)) & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+
+
+def ref_state(sim: Simulation):
+    i = sim.info()
+    s, o, c = sim.get_lattice()
+    stat = c.reshape(-1, i.n_species + 1).sum(0).astype(np.int32)
+    return s, o, c, stat
+
+
+def oracle_args(sim: Simulation):
+    i = sim.info()
+    return (tuple(int(x) for x in i.res), i.max_particles_site, i.n_regions, i.n_species, i.n_reactions,
+            float(np.float32(i.tau)), float(np.float32(i.lambda_)), sim.tables())
+
+
+def multi_region_model(res=(12, 10, 14), K=8, seed=7, counts=(40, 30, 20, 10), reservoir=False, D_scale=1.0,
+                       transition=False) -> Simulation:
+    """Sphere shell + inner sphere, 4 species, mixed first/second-order reactions."""
+    D = 1e-12 * D_scale
+    dims = [r * LAM for r in res]
+    sim = Simulation(LatticeParams(dims, list(res), configs.stable_tau(D), LAM, K))
+    sim.seed_placement(seed)
+    c = [res[0] / 2 * LAM, res[1] / 2 * LAM, res[2] / 2 * LAM]
+    sim.add_region(RegionType.SphericalShell("membrane", "cytoplasm", c, 3.5 * LAM, 4.6 * LAM), D)
+    sim.add_region(RegionType.Sphere("nucleus", c, 2.0 * LAM), D * 0.5)
+    sim.prepare_regions()
+    names = ["A", "B", "C", "R"]
+    homes = ["cytoplasm", "background", "cytoplasm", "membrane"]
+    for n, h, k in zip(names, homes, counts):
+        sim.add_particle_count(n, h, k, True, False)
+    if reservoir:
+        sim.add_particle_concentration("X", "membrane", 0.3, False, True)
+    if transition:
+        sim.set_transition_rate("cytoplasm", "nucleus", D * 0.3)
+        sim.set_transition_rate("nucleus", "cytoplasm", D * 0.3)
+        sim.set_transition_rate_particle("B", "background", "membrane", D)
+    sim.add_reaction(["A", "B"], ["C"], 800.0)
+    sim.add_reaction(["C"], ["A", "B"], 40.0)
+    sim.add_reaction(["A"], ["B"], 25.0)
+    sim.add_reaction(["R", "A"], ["C"], 900.0)
+    sim.add_reaction(["C"], ["R"], 15.0)
+    if reservoir:
+        sim.add_reaction(["X", "B"], ["A"], 500.0)
+    return sim
+
+
+def crowded_model(res=(6, 5, 4), K=4, counts=(30, 20, 10), seed=3, D=1e-12) -> Simulation:
+    """Small, nearly full lattice: moves into full voxels are common."""
+    dims = [r * LAM for r in res]
+    sim = Simulation(LatticeParams(dims, list(res), configs.stable_tau(D), LAM, K))
+    sim.seed_placement(seed)
+    sim.set_diffusion_rate("background", D)
+    sim.prepare_regions()
+    for n, k in zip(("A", "B", "C"), counts):
+        sim.add_particle_count(n, "background", k, True, False)
+    sim.set_diffusion_rate("background", D)
+    sim.add_reaction(["A", "B"], ["C"], 300.0)
+    sim.add_reaction(["C"], ["A", "B"], 200.0)
+    return sim

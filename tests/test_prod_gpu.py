@@ -1,0 +1,156 @@
+"""Production (Philox) fused kernel against the plain per-sweep oracle:
+identical lattices and counts after N frames for every tiling, plus exact
+conservation, region confinement and batched-ensemble equivalence."""
+import numpy as np
+import pytest
+
+from cell_simulation_gb300 import Ensemble, PREC_FP32, PREC_FP64, PREC_MIXED, RNG_PHILOX, configs, tiling_variants
+from tests.helpers import crowded_model, multi_region_model, oracle_args
+
+pytestmark = pytest.mark.gpu
+
+
+def compact(slots_u32, K):
+    s = slots_u32.reshape(-1, K)
+    out = np.zeros_like(s, dtype=np.uint8)
+    for v in np.flatnonzero((s > 0).any(1)):
+        nz = s[v][s[v] > 0]
+        out[v, :len(nz)] = nz
+    return out.reshape(-1)
+
+
+def oracle_prod(orc, sim, n, seed, frame0=0, precision=0):
+    res, K, NR, S, R, tau, lam, tab = oracle_args(sim)
+    s, o, c = sim.get_lattice()
+    slots = compact(s, K)
+    counts = np.bincount(s, minlength=S + 1).astype(np.int64)
+    counts[0] = 0
+    for q in tab.reservoir[tab.reservoir > 0]:
+        counts[q] += 1
+    diag = orc.prod_run(res, K, NR, S, R, tau, lam, tab, slots, counts, seed, frame0, n, precision=precision)
+    return slots, counts, diag
+
+
+def gpu_prod(sim, n, seed, tiling=None, seg=0, chunks=1, precision=PREC_MIXED):
+    sim.prepare_for_gpu(RNG_PHILOX, 0)
+    sim.set_precision(precision)
+    if tiling is not None:
+        sim.set_tiling(tiling, seg)
+    for part in np.array_split(np.arange(n), chunks):
+        if len(part):
+            sim.step_philox(len(part), seed)
+    s, o, c = sim.get_lattice()
+    K = sim.info().max_particles_site
+    return s.astype(np.uint8), sim.counts(), sim.diagnostics()
+
+
+def tilings_for(K):
+    return [i for i, t in enumerate(tiling_variants()) if t[0] == K]
+
+
+@pytest.mark.parametrize("K", [8, 16])
+def test_fused_kernel_matches_oracle(orc, K):
+    sim = multi_region_model(res=(11, 13, 37), K=K, counts=(60, 50, 40, 30))
+    want_s, want_c, want_d = oracle_prod(orc, sim, 40, seed=1234)
+    for ti in tilings_for(K):
+        got_s, got_c, got_d = gpu_prod(multi_region_model(res=(11, 13, 37), K=K, counts=(60, 50, 40, 30)), 40, 1234,
+                                       tiling=ti, seg=5)
+        assert np.array_equal(got_s, want_s), (ti, np.flatnonzero(got_s != want_s)[:8])
+        assert np.array_equal(got_c, want_c), ti
+        assert np.array_equal(got_d[:4], want_d[:4]), (ti, got_d, want_d)
+    assert want_d[0] > 0  # reactions fired
+
+
+@pytest.mark.parametrize("precision", [PREC_MIXED, PREC_FP32, PREC_FP64])
+def test_precision_modes_match_oracle(orc, precision):
+    mk = lambda: multi_region_model(res=(9, 8, 20), K=16, counts=(70, 60, 50, 40), reservoir=True)
+    want_s, want_c, want_d = oracle_prod(orc, mk(), 30, seed=99, precision=precision)
+    got_s, got_c, got_d = gpu_prod(mk(), 30, 99, precision=precision, chunks=3)
+    assert np.array_equal(got_s, want_s)
+    assert np.array_equal(got_c, want_c)
+    assert np.array_equal(got_d[:4], want_d[:4])
+
+
+def test_crowded_capacity_rule(orc):
+    mk = lambda: crowded_model(res=(6, 5, 7), K=8, counts=(60, 50, 40))
+    want_s, want_c, _ = oracle_prod(orc, mk(), 50, seed=5)
+    got_s, got_c, _ = gpu_prod(mk(), 50, 5)
+    assert np.array_equal(got_s, want_s)
+    assert np.array_equal(got_c, want_c)
+    v = got_s.reshape(-1, 8)
+    # compacted: no zero before a particle
+    assert not ((v[:, :-1] == 0) & (v[:, 1:] != 0)).any()
+
+
+def test_conservation_and_confinement():
+    sim = multi_region_model(res=(16, 16, 24), K=16, counts=(200, 150, 100, 80))
+    tab = sim.tables()
+    before = np.bincount(sim.get_lattice()[0], minlength=5)[1:]
+    sim.prepare_for_gpu(RNG_PHILOX, 0)
+    # no reactions: rates zeroed through the drop-in table setter is not allowed after prepare, so use a model copy
+    sim2 = multi_region_model(res=(16, 16, 24), K=16, counts=(200, 150, 100, 80))
+    t2 = sim2.tables()
+    i2 = sim2.info()
+    sim2.set_tables(i2.n_regions, i2.n_species, i2.n_reactions, t2.regions, t2.diffusion, t2.stoich, t2.reactants,
+                    np.zeros_like(t2.rates))
+    sim2.set_lattice(sim.get_lattice()[0])
+    sim2.prepare_for_gpu(RNG_PHILOX, 0)
+    sim2.step_philox(200, 7)
+    s, _, _ = sim2.get_lattice()
+    after = np.bincount(s, minlength=5)[1:]
+    assert np.array_equal(before, after)
+    assert np.array_equal(sim2.counts()[1:], before)
+    # off-diagonal D = 0: every particle stays in the region it started in
+    reg = tab.regions
+    s0 = sim.get_lattice()[0].reshape(-1, 16)
+    s1 = s.reshape(-1, 16)
+    for q in range(1, 5):
+        r0 = np.bincount(np.repeat(reg, (s0 == q).sum(1)), minlength=4)
+        r1 = np.bincount(np.repeat(reg, (s1 == q).sum(1)), minlength=4)
+        assert np.array_equal(r0, r1), q
+
+
+def test_graph_replay_equals_single_launches():
+    a = multi_region_model(res=(10, 12, 30), K=16)
+    b = multi_region_model(res=(10, 12, 30), K=16)
+    a.prepare_for_gpu(RNG_PHILOX, 0)
+    b.prepare_for_gpu(RNG_PHILOX, 0)
+    a.step_philox(25, 3)
+    for _ in range(25):
+        b.step_philox(1, 3)
+    assert np.array_equal(a.get_lattice()[0], b.get_lattice()[0])
+    assert np.array_equal(a.counts(), b.counts())
+
+
+def test_ensemble_batched_equals_plain_and_oracle(orc):
+    tmpl = configs.c4_ensemble_template(K=8)
+    res = np.array([[9, 9, 9], [12, 12, 12], [7, 7, 7], [16, 16, 16]], np.uint32)
+    seeds = np.array([11, 22, 33, 44], np.uint64)
+    mult = np.array([0.5, 1.0, 1.7, 2.0], np.float32)
+    init = np.array([0, 40, 40, 5], np.uint32)
+    eb = Ensemble(tmpl, res, seeds, mult, init)
+    ep = Ensemble(tmpl, res, seeds, mult, init)
+    s0 = eb.slots()
+    eb.step(30, batched=True)
+    ep.step(30, batched=False)
+    assert np.array_equal(eb.slots(), ep.slots())
+    assert np.array_equal(eb.counts(), ep.counts())
+    # each replicate against the oracle
+    tab = tmpl.tables()
+    info = tmpl.info()
+    off = 0
+    got = eb.slots()
+    counts = eb.counts()
+    for r in range(len(res)):
+        V = int(np.prod(res[r]))
+        sl = s0[off * 8:(off + V) * 8].copy()
+        c0 = np.bincount(sl, minlength=4).astype(np.int64)
+        c0[0] = 0
+        t = type(tab)(np.zeros(V, np.uint32), tab.diffusion, tab.stoich, tab.reactants, tab.rates,
+                      np.zeros(V, np.uint32))
+        orc.prod_run(tuple(int(x) for x in res[r]), 8, info.n_regions, info.n_species, info.n_reactions,
+                     float(np.float32(info.tau)), float(np.float32(info.lambda_)), t, sl, c0, int(seeds[r]), 0, 30,
+                     rate_mult=float(mult[r]))
+        assert np.array_equal(got[off * 8:(off + V) * 8], sl), r
+        assert np.array_equal(counts[r], c0), r
+        off += V
