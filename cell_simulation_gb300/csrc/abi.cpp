@@ -627,4 +627,8 @@ cs_status cs_ensemble_info(const cs_ensemble* ens, uint64_t* total_voxels, uint3
     });
 }
 
+cs_status cs_ref_frame_noalloc(const cs_ref_frame_noalloc_args* args) {
+    return guarded([&] { ref_frame_noalloc(args); });
+}
+
 }  // extern "C"

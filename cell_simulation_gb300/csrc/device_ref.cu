@@ -26,6 +26,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "cuda_check.h"
@@ -550,4 +552,90 @@ float ref_time_frames(DeviceRef* d, uint32_t n, const uint32_t* itimes, uint64_t
     (void)frame0;
     return ms;
 }
+}  // namespace cellsim
+
+// ------------------------------------------------------------------ allocation-free frame
+//
+// A reference-RNG frame on caller-owned device buffers that never allocates.
+// It serves hosts that own all device memory themselves: an engine that
+// reserves one arena at start-up and forbids further cudaMalloc (a cudaMalloc
+// can synchronise the device and fragments that budget), or a real-time loop
+// that cannot absorb an allocation's stall.  The only memory the frame needs
+// beyond the caller's inputs and outputs (the per-slot direction bytes and the
+// contention flag) lives in the fixed array below.  CUDA reserves that array
+// on every GPU where this library's module is loaded, and it stays there until
+// the process exits.
+namespace cellsim {
+
+constexpr size_t kNoAllocMaxSlots = (size_t)16 << 20;  // V * K <= 16 Mi slots (16 MiB of directions)
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocMaxSlots + 256];
+
+static std::mutex g_noalloc_mu;
+static uint8_t* g_noalloc_addr[256];
+
+// Device address of the scratch array on `device`, looked up once per device
+// with that device current.
+static uint8_t* noalloc_scratch(int device) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (device < 0 || device >= 256) throw Error(CS_ERR_INVALID_ARG, "device ordinal out of range");
+    if (!g_noalloc_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) throw Error(CS_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        g_noalloc_addr[device] = static_cast<uint8_t*>(p);
+    }
+    return g_noalloc_addr[device];
+}
+
+void ref_frame_noalloc(const cs_ref_frame_noalloc_args* a) {
+    if (!a) throw Error(CS_ERR_INVALID_ARG, "args is NULL");
+    const uint32_t K = a->max_particles_site;
+    if (a->res[0] == 0 || a->res[1] == 0 || a->res[2] == 0) throw Error(CS_ERR_INVALID_ARG, "resolution must be positive");
+    if (K < 1 || K > 16) throw Error(CS_ERR_LIMIT, "max_particles_site must be in 1..16");
+    if (a->n_regions < 1 || a->n_regions > 256) throw Error(CS_ERR_LIMIT, "n_regions must be in 1..256");
+    if (a->n_species > 255) throw Error(CS_ERR_LIMIT, "at most 255 species");
+    if (a->n_reactions > 99) throw Error(CS_ERR_LIMIT, "at most 99 reactions");
+    const uint64_t V = (uint64_t)a->res[0] * a->res[1] * a->res[2];
+    if (V * K > kNoAllocMaxSlots)
+        throw Error(CS_ERR_LIMIT, "cs_ref_frame_noalloc handles at most 16777216 slots (V*K); this lattice has " +
+                                      std::to_string(V * K) + ": use cs_step, which allocates its own scratch");
+    const void* ptrs[] = {a->slots_in, a->occupancy_in, a->conc_in, a->slots_out, a->occupancy_out, a->conc_out,
+                          a->regions, a->reservoir, a->probabilities, a->stoich, a->reactants, a->rates, a->itime,
+                          a->counts, a->diag};
+    for (const void* q : ptrs)
+        if (!q) throw Error(CS_ERR_INVALID_ARG, "every buffer pointer of cs_ref_frame_noalloc_args must be non-NULL");
+    DeviceGuard g(a->device);
+    uint8_t* scratch = noalloc_scratch(a->device);
+    uint8_t* dirs = scratch;
+    uint32_t* contended = reinterpret_cast<uint32_t*>(scratch + kNoAllocMaxSlots);
+    RefParams p{};
+    p.X = a->res[0]; p.Y = a->res[1]; p.Z = a->res[2];
+    p.K = K; p.S1 = a->n_species + 1; p.R = a->n_reactions; p.NR = a->n_regions;
+    p.YZ = p.Y * p.Z;
+    p.V = V;
+    p.tau = a->tau;
+    p.P = a->probabilities;
+    p.stoich = a->stoich;
+    p.reactants = a->reactants;
+    p.rates = a->rates;
+    p.regions = a->regions;
+    p.reservoir = a->reservoir;
+    cudaStream_t st = static_cast<cudaStream_t>(a->stream);
+    const int TB = 256;
+    unsigned nb = (unsigned)((V + TB - 1) / TB);
+    size_t smem = (p.S1 + 2) * sizeof(int32_t);
+    // ref_directions rewrites every direction byte and clears the contention
+    // flag before anything reads them, so stale scratch from an earlier call
+    // never leaks into this frame.
+    ref_directions<<<nb, TB, 0, st>>>(p, a->slots_in, a->occupancy_in, a->itime, 0u, dirs, a->diag, contended);
+    ref_gather<<<nb, TB, 0, st>>>(p, a->slots_in, a->occupancy_in, a->conc_in, dirs, a->slots_out, a->occupancy_out,
+                                  a->conc_out, contended);
+    ref_serial_copy<<<std::min<unsigned>(nb, 4096u), TB, 0, st>>>(p, contended, a->slots_in, a->occupancy_in, a->conc_in,
+                                                                  a->slots_out, a->occupancy_out, a->conc_out);
+    ref_serial<<<1, 32, 0, st>>>(p, contended, a->slots_in, a->occupancy_in, dirs, a->slots_out, a->occupancy_out,
+                                 a->conc_out, a->diag);
+    ref_cme<<<nb, TB, smem, st>>>(p, a->slots_out, a->occupancy_out, a->conc_out, a->itime, 0u, a->counts, a->diag);
+    CS_LAUNCH_CHECK();
+}
+
 }  // namespace cellsim

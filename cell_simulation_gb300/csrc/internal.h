@@ -172,6 +172,7 @@ int prod_tiling_current(const DeviceProd* d);
 void prod_seed(DeviceProd* d, uint64_t seed);
 float prod_time_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched);
 float ref_time_frames(DeviceRef* d, uint32_t n, const uint32_t* itimes, uint64_t frame0);
+void ref_frame_noalloc(const cs_ref_frame_noalloc_args* a);
 
 // model.cpp helpers shared with the device files
 void compute_ref_probabilities(const Model& m, std::vector<float>& P);

@@ -49,6 +49,15 @@ class InfoC(C.Structure):
                 ("dims", C.c_float * 3), ("rng_mode", C.c_int32), ("device", C.c_int32)]
 
 
+class RefFrameNoAllocArgsC(C.Structure):
+    _fields_ = [("device", C.c_int32), ("stream", C.c_void_p), ("res", C.c_uint32 * 3),
+                ("max_particles_site", C.c_uint32), ("n_regions", C.c_uint32), ("n_species", C.c_uint32),
+                ("n_reactions", C.c_uint32), ("tau", C.c_float)] + [
+        (n, C.c_void_p) for n in ("slots_in", "occupancy_in", "conc_in", "slots_out", "occupancy_out", "conc_out",
+                                  "regions", "reservoir", "probabilities", "stoich", "reactants", "rates", "itime",
+                                  "counts", "diag")]
+
+
 class StatSampleC(C.Structure):
     _fields_ = [("species", C.c_uint32), ("value", C.c_int32), ("iteration_count", C.c_uint32)]
 
@@ -92,6 +101,7 @@ SIGNATURES = {
     "cs_pop_stats": (st, [P, C.POINTER(StatSampleC), C.c_uint32, u32p]),
     "cs_get_diagnostics": (st, [P, u32p, C.c_uint32]),
     "cs_synchronize": (st, [P]),
+    "cs_ref_frame_noalloc": (st, [C.POINTER(RefFrameNoAllocArgsC)]),
     "cs_step_timed": (st, [P, C.c_uint32, u32p, f32p]),
     "cs_step_philox_timed": (st, [P, C.c_uint32, C.c_uint64, f32p]),
     "cs_tiling_count": (st, [i32p]),

@@ -211,6 +211,55 @@ cs_status cs_pop_stats(cs_sim* sim, cs_stat_sample* out, uint32_t capacity, uint
 cs_status cs_get_diagnostics(cs_sim* sim, uint32_t* diag, uint32_t n);
 cs_status cs_synchronize(cs_sim* sim);
 
+/* ---------------- allocation-free reference-RNG frame ---------------- */
+/* Arguments of cs_ref_frame_noalloc.  Every pointer is a device pointer on
+ * `device`, owned by the caller, in the library's device layout:
+ *   slots u8[V*K], occupancy u32[V], conc i32[V*(S+1)] (input frame and output
+ *   frame, distinct buffers); regions and reservoir u8[V]; probabilities
+ *   f32[NR][NR][S+1] holding (D[a][b][q] * tau) / (lambda * lambda) in
+ *   binary32; stoich i32[(R+1)*(S+1)]; reactants u32[(R+1)*3]; rates f32[R+1];
+ *   itime u32[1], this frame's seed; counts i32[S+1] and diag u32[8], updated
+ *   in place. */
+typedef struct {
+    int32_t device;
+    void* stream;  /* cudaStream_t; NULL = the legacy default stream */
+    uint32_t res[3];
+    uint32_t max_particles_site;
+    uint32_t n_regions, n_species, n_reactions;
+    float tau;
+    const uint8_t* slots_in;
+    const uint32_t* occupancy_in;
+    const int32_t* conc_in;
+    uint8_t* slots_out;
+    uint32_t* occupancy_out;
+    int32_t* conc_out;
+    const uint8_t* regions;
+    const uint8_t* reservoir;
+    const float* probabilities;
+    const int32_t* stoich;
+    const uint32_t* reactants;
+    const float* rates;
+    const uint32_t* itime;
+    int32_t* counts;
+    uint32_t* diag;
+} cs_ref_frame_noalloc_args;
+
+/* No counterpart in the reference.  One reference-RNG frame (the same
+ * kernels as cs_step) on caller-owned device buffers, for callers that must
+ * not allocate device memory: hosts that manage every device byte through
+ * their own arena and forbid cudaMalloc at run time, or loops that cannot
+ * absorb an allocation's device synchronisation.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine.  Its only scratch is a fixed
+ * 16 MiB + 256 B device array inside the library, held on every GPU where the
+ * library is loaded until the process exits; lattices with V*K above
+ * 16777216 slots are rejected with CS_ERR_LIMIT.  The first call on a device
+ * looks up that array's address (make this first call before any stream
+ * capture).  All calls share the array, so calls that overlap on the GPU
+ * (different streams, or different host threads on the same device) race;
+ * each call rewrites the scratch it reads, so back-to-back calls are safe.
+ * Work is enqueued on `stream` and the call returns without waiting. */
+cs_status cs_ref_frame_noalloc(const cs_ref_frame_noalloc_args* args);
+
 /* ---------------- timing and tiling (production path) ---------------- */
 /* Enqueue n frames between two CUDA events recorded on the handle's stream
  * and return the device time in milliseconds (blocks until done).  No
