@@ -31,235 +31,9 @@
 #include "cuda_check.h"
 #include "internal.h"
 #include "prod_common.cuh"
+#include "prod_kernel.cuh"
 
 namespace cellsim {
-
-struct ProdParams {
-    ProdTables T;
-    const RepDesc* reps;
-    const WorkItem* items;
-    uint32_t n_items;
-    uint32_t parity;
-    uint32_t* counters;  // [2]
-    uint32_t* stepbuf;   // [2]
-    const uint8_t* src;
-    uint8_t* dst;
-    const uint8_t* region_code;
-    const uint8_t* reservoir;  // may be null
-    unsigned long long* counts;  // [n_rep][S1]
-    uint32_t* diag;
-};
-
-template <int K, int TY, int TZ>
-struct Tile {
-    static constexpr int WY = TY + 2, WZ = TZ + 2, WIN = WY * WZ;
-    static constexpr int RWY = TY + 4, RWZ = TZ + 4, RWIN = RWY * RWZ;
-    static constexpr size_t vox_bytes = (size_t)(4 + 2) * WIN * K;    // raw[4], xp, yp
-    static constexpr size_t dec_bytes = (size_t)(4 + 2) * WIN * 4;    // decx[4], decy, decz
-    static constexpr size_t reg_bytes = ((size_t)4 * RWIN + 15) / 16 * 16;
-    static size_t smem(uint32_t S1) { return vox_bytes + dec_bytes + reg_bytes + (size_t)(S1 + PD_N) * 4; }
-};
-
-template <int K>
-__device__ __forceinline__ Vox<K> ld_vox(const uint8_t* p) {
-    Vox<K> c;
-    if (K == 16) {
-        uint4 t = __ldg(reinterpret_cast<const uint4*>(p));
-        c.w[0] = (uint64_t)t.x | ((uint64_t)t.y << 32);
-        c.w[K / 8 - 1] = (uint64_t)t.z | ((uint64_t)t.w << 32);
-    } else {
-        uint2 t = __ldg(reinterpret_cast<const uint2*>(p));
-        c.w[0] = (uint64_t)t.x | ((uint64_t)t.y << 32);
-    }
-    return c;
-}
-
-template <int K>
-__device__ __forceinline__ void st_vox(uint8_t* p, const Vox<K>& c) {
-    if (K == 16) {
-        uint4 t;
-        t.x = (uint32_t)c.w[0]; t.y = (uint32_t)(c.w[0] >> 32);
-        t.z = (uint32_t)c.w[K / 8 - 1]; t.w = (uint32_t)(c.w[K / 8 - 1] >> 32);
-        *reinterpret_cast<uint4*>(p) = t;
-    } else {
-        uint2 t;
-        t.x = (uint32_t)c.w[0]; t.y = (uint32_t)(c.w[0] >> 32);
-        *reinterpret_cast<uint2*>(p) = t;
-    }
-}
-
-template <int K, int TY, int TZ, int NT>
-__global__ void __launch_bounds__(NT) prod_step_kernel(ProdParams P) {
-    using C = Tile<K, TY, TZ>;
-    constexpr int WZ = C::WZ, WIN = C::WIN, RWZ = C::RWZ, RWIN = C::RWIN;
-    extern __shared__ __align__(16) uint8_t smem[];
-    Vox<K>* raw = reinterpret_cast<Vox<K>*>(smem);  // [4][WIN]
-    Vox<K>* xp = raw + 4 * WIN;
-    Vox<K>* yp = xp + WIN;
-    uint32_t* decx = reinterpret_cast<uint32_t*>(smem + C::vox_bytes);  // [4][WIN]
-    uint32_t* decy = decx + 4 * WIN;
-    uint32_t* decz = decy + WIN;
-    uint8_t* reg = smem + C::vox_bytes + C::dec_bytes;  // [4][RWIN]
-    int32_t* s_delta = reinterpret_cast<int32_t*>(smem + C::vox_bytes + C::dec_bytes + C::reg_bytes);
-    uint32_t* s_diag = reinterpret_cast<uint32_t*>(s_delta + P.T.S1);
-    __shared__ uint32_t s_item;
-
-    const int tid = threadIdx.x;
-    const uint32_t frame = P.stepbuf[P.parity];
-    if (blockIdx.x == 0 && tid == 0) {
-        P.counters[P.parity ^ 1u] = 0u;
-        P.stepbuf[P.parity ^ 1u] = frame + 1u;
-    }
-    for (int i = tid; i < PD_N; i += NT) s_diag[i] = 0u;
-
-    for (;;) {
-        __syncthreads();
-        if (tid == 0) s_item = atomicAdd(P.counters + P.parity, 1u);
-        __syncthreads();
-        const uint32_t it = s_item;
-        if (it >= P.n_items) break;
-        const WorkItem wi = P.items[it];
-        const RepDesc rd = P.reps[wi.rep];
-        const int X = (int)rd.X, Y = (int)rd.Y, Z = (int)rd.Z;
-        const int y0 = (int)wi.y0, z0 = (int)wi.z0, x0 = (int)wi.x0, x1 = (int)wi.x1;
-        const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
-        const uint8_t* src = P.src + rd.base * K;
-        uint8_t* dst = P.dst + rd.base * K;
-        const uint8_t* rcode = P.region_code + rd.base;
-        const uint8_t* resv = P.reservoir ? P.reservoir + rd.base : nullptr;
-        const uint32_t YZ = (uint32_t)Y * (uint32_t)Z;
-        for (uint32_t s = tid; s < P.T.S1; s += NT) s_delta[s] = 0;
-
-        auto reg_plane = [&](int p) -> uint8_t* { return reg + ((p + 8) & 3) * RWIN; };
-        auto load_reg = [&](int p) {
-            uint8_t* rp = reg_plane(p);
-            for (int e = tid; e < RWIN; e += NT) {
-                int ry = e / RWZ, rz = e - ry * RWZ;
-                int y = y0 - 2 + ry, z = z0 - 2 + rz;
-                uint8_t code = 0;
-                if (p >= 0 && p < X && y >= 0 && y < Y && z >= 0 && z < Z)
-                    code = rcode[((uint64_t)p * Y + y) * Z + z];
-                rp[e] = code;
-            }
-        };
-        // load raw plane p and decide its x-moves
-        auto load_raw = [&](int p) {
-            Vox<K>* cp = raw + ((p + 4) & 3) * WIN;
-            uint32_t* dp = decx + ((p + 4) & 3) * WIN;
-            const uint8_t* rs_p = reg_plane(p);
-            const uint8_t* rlo_p = reg_plane(p - 1);
-            const uint8_t* rhi_p = reg_plane(p + 1);
-            for (int e = tid; e < WIN; e += NT) {
-                int wy = e / WZ, wz = e - wy * WZ;
-                int y = y0 - 1 + wy, z = z0 - 1 + wz;
-                Vox<K> c = vox_zero<K>();
-                uint32_t d = 0;
-                if (p >= 0 && p < X && y >= 0 && y < Y && z >= 0 && z < Z) {
-                    uint32_t v = ((uint32_t)p * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
-                    c = ld_vox<K>(src + (uint64_t)v * K);
-                    if (!vox_empty<K>(c)) {
-                        int ri = (wy + 1) * RWZ + wz + 1;
-                        d = decide_moves<K>(c, v, frame, 0u, rs_p[ri], rlo_p[ri], rhi_p[ri], k0, k1, P.T);
-                    }
-                }
-                cp[e] = c;
-                dp[e] = d;
-            }
-        };
-
-        // prologue: regions x0-2..x0+1, raw x0-1 and x0 with their x-decisions
-        for (int p = x0 - 2; p <= x0 + 1; p++) load_reg(p);
-        __syncthreads();
-        load_raw(x0 - 1);
-        load_raw(x0);
-        __syncthreads();
-        for (int i = x0; i < x1; i++) {
-            load_reg(i + 2);
-            __syncthreads();
-            load_raw(i + 1);
-            __syncthreads();
-            // ---- X sweep of plane i, then y-decisions of the result
-            {
-                const Vox<K>* rlo = raw + ((i + 3) & 3) * WIN;
-                const Vox<K>* rme = raw + ((i + 4) & 3) * WIN;
-                const Vox<K>* rhi = raw + ((i + 5) & 3) * WIN;
-                const uint32_t* dlo = decx + ((i + 3) & 3) * WIN;
-                const uint32_t* dme = decx + ((i + 4) & 3) * WIN;
-                const uint32_t* dhi = decx + ((i + 5) & 3) * WIN;
-                const uint8_t* rg = reg_plane(i);
-                for (int e = tid; e < WIN; e += NT) {
-                    int wy = e / WZ, wz = e - wy * WZ;
-                    int y = y0 - 1 + wy, z = z0 - 1 + wz;
-                    uint32_t v = ((uint32_t)i * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
-                    uint32_t a = dme[e], b = dlo[e], c2 = dhi[e];
-                    Vox<K> own = rme[e];
-                    Vox<K> r = own;
-                    if ((a | (b >> 16) | (c2 & 0xFFFFu)) != 0u)
-                        r = combine<K>(own, a, rlo[e], b, rhi[e], c2, v, v - YZ, v + YZ, frame, 0u);
-                    xp[e] = r;
-                    uint32_t d = 0;
-                    if (!vox_empty<K>(r)) {
-                        int ri = (wy + 1) * RWZ + wz + 1;
-                        d = decide_moves<K>(r, v, frame, 1u, rg[ri], rg[ri - RWZ], rg[ri + RWZ], k0, k1, P.T);
-                    }
-                    decy[e] = d;
-                }
-            }
-            __syncthreads();
-            // ---- Y sweep (interior rows), then z-decisions
-            {
-                const uint8_t* rg = reg_plane(i);
-                for (int e = tid + WZ; e < WIN - WZ; e += NT) {
-                    int wy = e / WZ, wz = e - wy * WZ;
-                    int y = y0 - 1 + wy, z = z0 - 1 + wz;
-                    uint32_t v = ((uint32_t)i * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
-                    uint32_t a = decy[e], b = decy[e - WZ], c2 = decy[e + WZ];
-                    Vox<K> own = xp[e];
-                    Vox<K> r = own;
-                    if ((a | (b >> 16) | (c2 & 0xFFFFu)) != 0u)
-                        r = combine<K>(own, a, xp[e - WZ], b, xp[e + WZ], c2, v, v - (uint32_t)Z, v + (uint32_t)Z, frame, 1u);
-                    yp[e] = r;
-                    uint32_t d = 0;
-                    if (!vox_empty<K>(r)) {
-                        int ri = (wy + 1) * RWZ + wz + 1;
-                        d = decide_moves<K>(r, v, frame, 2u, rg[ri], rg[ri - 1], rg[ri + 1], k0, k1, P.T);
-                    }
-                    decz[e] = d;
-                }
-            }
-            __syncthreads();
-            // ---- Z sweep of the interior, reactions, store
-            {
-                float mult = rd.rate_mult;
-                for (int t = tid; t < TY * TZ; t += NT) {
-                    int ty = t / TZ, tz = t - ty * TZ;
-                    int y = y0 + ty, z = z0 + tz;
-                    if (y >= Y || z >= Z) continue;
-                    int e = (ty + 1) * WZ + tz + 1;
-                    uint32_t v = ((uint32_t)i * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
-                    uint32_t a = decz[e], b = decz[e - 1], c2 = decz[e + 1];
-                    Vox<K> own = yp[e];
-                    Vox<K> r = own;
-                    if ((a | (b >> 16) | (c2 & 0xFFFFu)) != 0u)
-                        r = combine<K>(own, a, yp[e - 1], b, yp[e + 1], c2, v, v - 1u, v + 1u, frame, 2u);
-                    uint32_t rv = resv ? (uint32_t)resv[v] : 0u;
-                    if (rv != 0u || P.T.n_zero_order != 0u || !vox_empty<K>(r))
-                        react_voxel<K>(r, rv, v, frame, k0, k1, mult, P.T, s_delta, s_diag);
-                    st_vox<K>(dst + (uint64_t)v * K, r);
-                }
-            }
-            __syncthreads();
-        }
-        // flush this work item's count deltas
-        for (uint32_t s = tid; s < P.T.S1; s += NT) {
-            int32_t d = s_delta[s];
-            if (d) atomicAdd(P.counts + (size_t)rd.counts_index * P.T.S1 + s, (unsigned long long)(long long)d);
-        }
-    }
-    __syncthreads();
-    for (int i = tid; i < PD_N; i += NT)
-        if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
-}
 
 // ------------------------------------------------------------------ configs
 
@@ -271,15 +45,16 @@ struct KernelCfg {
     size_t (*smem)(uint32_t);
 };
 
-template <int K, int TY, int TZ, int NT>
+template <int K, int TY, int TZ, int NT, int MINB>
 static KernelCfg make_cfg() {
-    return KernelCfg{K, TY, TZ, NT, prod_step_kernel<K, TY, TZ, NT>, &Tile<K, TY, TZ>::smem};
+    return KernelCfg{K, TY, TZ, NT, prod_step_kernel<K, TY, TZ, NT, MINB>, &Tile<K, TY, TZ>::smem};
 }
 
 static const std::vector<KernelCfg>& all_cfgs() {
     static const std::vector<KernelCfg> v = {
-        make_cfg<16, 8, 32, 256>(), make_cfg<16, 4, 64, 256>(), make_cfg<16, 16, 32, 256>(), make_cfg<16, 8, 64, 256>(),
-        make_cfg<8, 8, 32, 256>(),  make_cfg<8, 4, 64, 256>(),  make_cfg<8, 16, 32, 256>(),  make_cfg<8, 8, 64, 256>(),
+        make_cfg<16, 8, 32, 256, 3>(), make_cfg<16, 4, 64, 256, 3>(), make_cfg<16, 16, 32, 256, 1>(),
+        make_cfg<16, 8, 64, 256, 1>(),  make_cfg<8, 8, 32, 256, 3>(),  make_cfg<8, 4, 64, 256, 3>(),
+        make_cfg<8, 16, 32, 256, 2>(),  make_cfg<8, 8, 64, 256, 2>(),
     };
     return v;
 }
@@ -295,12 +70,17 @@ struct DeviceProd {
     std::vector<RepDesc> h_reps;
     DevBuf<RepDesc> reps;
     DevBuf<uint8_t> slots[2];
-    DevBuf<uint8_t> region_code, reservoir;
+    DevBuf<uint8_t> region_pad, reservoir;
     DevBuf<uint32_t> thr;
-    DevBuf<uint8_t> rx_reactants, rx_ch_sp, one_list;
+    DevBuf<uint8_t> rx_reactants, rx_ch_sp;
     DevBuf<int8_t> rx_ch_d;
     DevBuf<float> rx_rate;
-    DevBuf<uint16_t> one_off;
+    DevBuf<unsigned long long> rmask;
+    DevBuf<float> one;
+    std::vector<float> h_rate;
+    std::vector<uint8_t> h_rre;
+    std::vector<unsigned long long> h_rmask;
+    unsigned long long h_zmask[2] = {0ull, 0ull};
     DevBuf<unsigned long long> counts;
     DevBuf<uint32_t> diag, counters, stepbuf;
     DevBuf<WorkItem> items;      // batched order
@@ -363,37 +143,31 @@ static void build_tables(DeviceProd* d, const Model& m) {
             n++;
         }
     }
-    // reactions possible with exactly one particle q (q = 0: empty voxel)
-    std::vector<uint16_t> off(d->S1 + 1, 0);
-    std::vector<uint8_t> lst;
-    for (uint32_t q = 0; q < d->S1; q++) {
-        off[q] = (uint16_t)lst.size();
-        for (uint32_t r = 0; r < d->R; r++) {
-            uint32_t nv = 0, nq = 0;
-            for (int j = 0; j < 3; j++) {
-                uint32_t s = rre[3 * r + j];
-                if (s) { nv++; nq += (s == q); }
-            }
-            if (nv == 0 || (q != 0 && nv == 1 && nq == 1)) lst.push_back((uint8_t)r);
+    if (d->R > 128) throw Error(CS_ERR_LIMIT, "at most 128 reactions on the production path");
+    // candidate masks: bit r of rmask[s] when s is a reactant of reaction r
+    std::vector<unsigned long long> rmask(2 * (size_t)d->S1, 0ull);
+    unsigned long long zmask[2] = {0ull, 0ull};
+    uint32_t n_zero = 0;
+    for (uint32_t r = 0; r < d->R; r++) {
+        bool any = false;
+        for (int j = 0; j < 3; j++) {
+            uint32_t s = rre[3 * r + j];
+            if (s) { rmask[2 * s + (r >> 6)] |= 1ull << (r & 63); any = true; }
         }
+        if (!any) { zmask[r >> 6] |= 1ull << (r & 63); n_zero++; }
     }
-    off[d->S1] = (uint16_t)lst.size();
-    uint32_t n_zero = off[1] - off[0];
-    if (lst.empty()) lst.push_back(0);
     d->thr.alloc(thr.size());
     d->rx_reactants.alloc(rre.size());
     d->rx_ch_sp.alloc(csp.size());
     d->rx_ch_d.alloc(cdl.size());
     d->rx_rate.alloc(rate.size());
-    d->one_off.alloc(off.size());
-    d->one_list.alloc(lst.size());
+    d->rmask.alloc(rmask.size());
     CS_CUDA(cudaMemcpy(d->thr.p, thr.data(), thr.size() * 4, cudaMemcpyHostToDevice));
     CS_CUDA(cudaMemcpy(d->rx_reactants.p, rre.data(), rre.size(), cudaMemcpyHostToDevice));
     CS_CUDA(cudaMemcpy(d->rx_ch_sp.p, csp.data(), csp.size(), cudaMemcpyHostToDevice));
     CS_CUDA(cudaMemcpy(d->rx_ch_d.p, cdl.data(), cdl.size(), cudaMemcpyHostToDevice));
     CS_CUDA(cudaMemcpy(d->rx_rate.p, rate.data(), rate.size() * 4, cudaMemcpyHostToDevice));
-    CS_CUDA(cudaMemcpy(d->one_off.p, off.data(), off.size() * 2, cudaMemcpyHostToDevice));
-    CS_CUDA(cudaMemcpy(d->one_list.p, lst.data(), lst.size(), cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->rmask.p, rmask.data(), rmask.size() * 8, cudaMemcpyHostToDevice));
     ProdTables& T = d->T;
     T.S1 = d->S1;
     T.R = d->R;
@@ -409,8 +183,51 @@ static void build_tables(DeviceProd* d, const Model& m) {
     T.rx_rate = d->rx_rate.p;
     T.rx_ch_sp = d->rx_ch_sp.p;
     T.rx_ch_d = d->rx_ch_d.p;
-    T.one_off = d->one_off.p;
-    T.one_list = d->one_list.p;
+    T.rmask = d->rmask.p;
+    T.zmask[0] = zmask[0];
+    T.zmask[1] = zmask[1];
+    d->h_rate = rate;
+    d->h_rre = rre;
+    d->h_rmask = rmask;
+    d->h_zmask[0] = zmask[0];
+    d->h_zmask[1] = zmask[1];
+}
+
+// a0, max and min non-zero propensity of a voxel holding exactly one particle
+// of species q (q = 0: no particle), per replicate, with the device's binary32
+// operation sequence: a = (rate * mult) * ff, summed in reaction order over
+// the candidate reactions.
+static void build_one_table(DeviceProd* d) {
+    std::vector<float> one((size_t)d->n_rep * d->S1 * 3, 0.0f);
+    for (uint32_t ri = 0; ri < d->n_rep; ri++) {
+        float mult = d->h_reps[ri].rate_mult;
+        for (uint32_t q = 0; q < d->S1; q++) {
+            unsigned long long m[2] = {d->h_zmask[0], d->h_zmask[1]};
+            if (q) { m[0] |= d->h_rmask[2 * q]; m[1] |= d->h_rmask[2 * q + 1]; }
+            float a0 = 0.0f, amax = 0.0f, amin = INFINITY;
+            for (uint32_t r = 0; r < d->R; r++) {
+                if (!((m[r >> 6] >> (r & 63)) & 1ull)) continue;
+                uint32_t ff = 1;
+                for (int j = 0; j < 3; j++) {
+                    uint32_t s = d->h_rre[3 * r + j];
+                    if (!s) continue;
+                    uint32_t mm = 0;
+                    for (int i = 0; i < j; i++) mm += d->h_rre[3 * r + i] == s;
+                    uint32_t cnt = (q != 0 && s == q) ? 1u : 0u;
+                    ff = (cnt <= mm) ? 0u : ff * (cnt - mm);
+                }
+                float k = d->h_rate[r] * mult;
+                float a = k * (float)ff;
+                a0 = a0 + a;
+                if (a > 0.0f) { amax = std::fmax(amax, a); amin = std::fmin(amin, a); }
+            }
+            float* o = &one[((size_t)ri * d->S1 + q) * 3];
+            o[0] = a0; o[1] = amax; o[2] = amin;
+        }
+    }
+    d->one.alloc(one.size());
+    CS_CUDA(cudaMemcpy(d->one.p, one.data(), one.size() * 4, cudaMemcpyHostToDevice));
+    d->T.one = d->one.p;
 }
 
 static int pick_default_cfg(uint32_t K) {
@@ -462,6 +279,7 @@ static void set_cfg(DeviceProd* d, int idx) {
     const KernelCfg& cfg = all_cfgs()[idx];
     size_t sm = cfg.smem(d->S1);
     CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     d->cfg_index = idx;
     build_items(d);
     if (d->graph) {
@@ -488,7 +306,7 @@ static void launch_frame(DeviceProd* d, int parity, int rep) {
     P.stepbuf = d->stepbuf.p;
     P.src = d->slots[parity].p;
     P.dst = d->slots[parity ^ 1].p;
-    P.region_code = d->region_code.p;
+    P.region_pad = d->region_pad.p;
     P.reservoir = d->reservoir.n ? d->reservoir.p : nullptr;
     P.counts = d->counts.p;
     P.diag = d->diag.p;
@@ -522,8 +340,8 @@ static DeviceProd* prod_alloc(const Model& m, int device, const std::vector<RepD
     d->total_voxels = total_voxels;
     d->reps.alloc(reps.size());
     CS_CUDA(cudaMemcpy(d->reps.p, reps.data(), reps.size() * sizeof(RepDesc), cudaMemcpyHostToDevice));
+    build_one_table(d.get());
     for (int b = 0; b < 2; b++) d->slots[b].alloc(total_voxels * d->K);
-    d->region_code.alloc(total_voxels);
     d->counts.alloc((size_t)d->n_rep * d->S1);
     d->diag.alloc(PD_N);
     d->counters.alloc(2 * (1 + d->n_rep));
@@ -542,19 +360,28 @@ DeviceProd* prod_create(const Model& m, int device) {
     m.check_tables();
     RepDesc r{};
     r.base = 0;
+    r.rbase = 0;
     r.X = m.res[0]; r.Y = m.res[1]; r.Z = m.res[2];
+    r.Zr = (uint32_t)((m.res[2] + 4 + 15) / 16 * 16);
     r.seed_lo = 0; r.seed_hi = 0;
     r.rate_mult = 1.0f;
     r.counts_index = 0;
+    r.flags = 0;
     std::unique_ptr<DeviceProd> d(prod_alloc(m, device, {r}, m.V));
     DeviceGuard g(device);
-    std::vector<uint8_t> rc(m.V);
+    // region codes (id + 1) padded so that every tile's window row starts on a
+    // 16-byte boundary: z is stored at column z + 2 of a row of Zr bytes
+    const uint64_t XY = (uint64_t)m.res[0] * m.res[1];
+    std::vector<uint8_t> rc(XY * r.Zr, 0);
     bool any_res = false;
-    for (uint64_t v = 0; v < m.V; v++) {
-        rc[v] = (uint8_t)(m.regions[v] + 1);
-        any_res |= m.reservoir[v] != 0;
-    }
-    CS_CUDA(cudaMemcpy(d->region_code.p, rc.data(), m.V, cudaMemcpyHostToDevice));
+    for (uint64_t row = 0; row < XY; row++)
+        for (uint32_t z = 0; z < m.res[2]; z++) {
+            uint64_t v = row * m.res[2] + z;
+            rc[row * r.Zr + z + 2] = (uint8_t)(m.regions[v] + 1);
+            any_res |= m.reservoir[v] != 0;
+        }
+    d->region_pad.alloc(rc.size());
+    CS_CUDA(cudaMemcpy(d->region_pad.p, rc.data(), rc.size(), cudaMemcpyHostToDevice));
     if (any_res) {
         std::vector<uint8_t> r8(m.V);
         for (uint64_t v = 0; v < m.V; v++) r8[v] = (uint8_t)m.reservoir[v];
@@ -758,13 +585,17 @@ DeviceProd* prod_ensemble_create(const Model& m, uint32_t n, const uint32_t* res
         d.seed_hi = (uint32_t)(seeds[r] >> 32);
         d.rate_mult = mult ? mult[r] : 1.0f;
         d.counts_index = r;
+        d.flags = 1u;
         base += V;
     }
     std::unique_ptr<DeviceProd> d(prod_alloc(m, device, reps, base));
     DeviceGuard g(device);
     d->seed_set = true;  // per-replicate seeds, never overwritten by prod_seed
     d->cur_seed = ~0ull;
-    CS_CUDA(cudaMemset(d->region_code.p, 1, base));  // region 0 -> code 1
+    // every replicate is region 0 throughout: codes are computed from the
+    // coordinates (RepDesc flag bit 0), no region-code array is read
+    d->region_pad.alloc(16);
+    CS_CUDA(cudaMemset(d->region_pad.p, 0, 16));
     std::vector<unsigned long long> cnt((size_t)n * d->S1, 0ull);
     for (uint32_t r = 0; r < n; r++) {
         const RepDesc& rd = reps[r];

@@ -34,13 +34,17 @@ namespace cellsim {
 enum { PD_EVENTS = 0, PD_REJECT_CAP = 1, PD_EVENT_CAP = 2, PD_FP64_SEL = 3, PD_N = 8 };
 
 struct RepDesc {
-    uint64_t base;  // first voxel of this replicate in the packed arrays
+    uint64_t base;   // first voxel of this replicate in the packed slot/reservoir arrays
+    uint64_t rbase;  // first byte of this replicate's padded region-code array
     uint32_t X, Y, Z;
+    uint32_t Zr;     // padded row length of the region-code array (z stored at column z + 2)
     uint32_t seed_lo, seed_hi;
     float rate_mult;
     uint32_t counts_index;  // replicate index into the counts array
-    uint32_t pad[7];
+    uint32_t flags;         // bit 0: the whole lattice is region 0 (no region-code array)
+    uint32_t pad[3];
 };
+static_assert(sizeof(RepDesc) == 64, "RepDesc is 64 bytes");
 
 struct WorkItem {
     uint32_t rep, y0, z0, x0, x1, pad[3];
@@ -58,8 +62,10 @@ struct ProdTables {
     const float* rx_rate;         // [R]
     const uint8_t* rx_ch_sp;      // [R][8]
     const int8_t* rx_ch_d;        // [R][8]
-    const uint16_t* one_off;      // [S1+1] offsets into one_list
-    const uint8_t* one_list;      // reactions possible in a voxel holding exactly one particle q (or none, q = 0)
+    const unsigned long long* rmask;  // [S1][2] bit r set when species s is a reactant of reaction r (R <= 128)
+    unsigned long long zmask[2];      // reactions without reactants
+    const float* one;                 // [n_rep][S1][3]: a0, max a, min non-zero a for a voxel holding
+                                      // exactly one particle of species q (q = 0: an empty voxel)
 };
 
 // K slot bytes held in 64-bit words, byte s = slot s.
@@ -224,34 +230,70 @@ __device__ __forceinline__ float propensity(const ProdTables& T, uint32_t r, con
     return __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), (float)ff);
 }
 
+// Reactions whose propensity can be non-zero in the voxel: those with a
+// reactant present, and those without reactants.  Every other reaction has
+// propensity exactly +0, so summing only these in index order gives the
+// same binary32 and binary64 sums as summing all of them.
+template <int K>
+__device__ __forceinline__ void candidates(const ProdTables& T, const Vox<K>& c, uint32_t n, uint32_t resv,
+                                           unsigned long long& m0, unsigned long long& m1) {
+    m0 = T.zmask[0];
+    m1 = T.zmask[1];
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t q = vox_get<K>(c, i);
+        m0 |= __ldg(T.rmask + 2 * q);
+        m1 |= __ldg(T.rmask + 2 * q + 1);
+    }
+    if (resv) {
+        m0 |= __ldg(T.rmask + 2 * resv);
+        m1 |= __ldg(T.rmask + 2 * resv + 1);
+    }
+}
+
+__device__ __forceinline__ int next_bit(unsigned long long& m0, unsigned long long& m1) {
+    if (m0) {
+        int b = __ffsll((long long)m0) - 1;
+        m0 &= m0 - 1;
+        return b;
+    }
+    if (m1) {
+        int b = __ffsll((long long)m1) - 1;
+        m1 &= m1 - 1;
+        return 64 + b;
+    }
+    return -1;
+}
+
 // SSA within tau for one voxel.  Returns true when any reaction fired (the
 // content is then rewritten species-major).  s_delta[S1] and s_diag[PD_N]
 // are block-shared accumulators.
 template <int K>
-__device__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0, uint32_t k1, float mult,
-                            const ProdTables& T, int32_t* s_delta, uint32_t* s_diag) {
+__device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0, uint32_t k1,
+                                         float mult, uint32_t rep, const ProdTables& T, int32_t* s_delta,
+                                         uint32_t* s_diag) {
     if (T.R == 0) return false;
     uint32_t n = vox_n<K>(c);
-    bool fast_ok = (resv == 0u);
-    if (fast_ok && n == 0u) {
-        uint32_t q0 = 0;
-        if (__ldg(T.one_off + q0 + 1) == __ldg(T.one_off + q0)) return false;  // no zero-order reaction
-    }
     double td = 0.0;
     float tf = 0.0f;
     bool fired = false;
     uint32_t ev = 0;
     for (; ev < T.max_events; ev++) {
-        bool fast = fast_ok && n <= 1u;
-        uint32_t q = (n == 1u) ? vox_get<K>(c, 0) : 0u;
-        uint32_t lb = 0, le = T.R;
-        if (fast) { lb = __ldg(T.one_off + q); le = __ldg(T.one_off + q + 1); }
+        unsigned long long c0, c1;
+        candidates<K>(T, c, n, resv, c0, c1);
         float a0 = 0.0f, amax = 0.0f, amin = __int_as_float(0x7f800000);
-        for (uint32_t k = lb; k < le; k++) {
-            uint32_t r = fast ? (uint32_t)__ldg(T.one_list + k) : k;
-            float a = fast ? __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), 1.0f) : propensity<K>(T, r, c, resv, mult);
-            a0 = __fadd_rn(a0, a);
-            if (a > 0.0f) { amax = fmaxf(amax, a); amin = fminf(amin, a); }
+        if (resv == 0u && n <= 1u) {
+            // one particle or none: the candidate sum is tabulated (same binary32 sum)
+            const float* o = T.one + ((size_t)rep * T.S1 + (n ? vox_get<K>(c, 0) : 0u)) * 3;
+            a0 = __ldg(o);
+            amax = __ldg(o + 1);
+            amin = __ldg(o + 2);
+        } else {
+            unsigned long long m0 = c0, m1 = c1;
+            for (int r = next_bit(m0, m1); r >= 0; r = next_bit(m0, m1)) {
+                float a = propensity<K>(T, (uint32_t)r, c, resv, mult);
+                a0 = __fadd_rn(a0, a);
+                if (a > 0.0f) { amax = fmaxf(amax, a); amin = fminf(amin, a); }
+            }
         }
         if (!(a0 > 0.0f)) break;
         U4 ph = d_philox(v, frame, (3u << 24) | (ev >> 1), 0u, k0, k1);
@@ -271,28 +313,28 @@ __device__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame
         int last_pos = -1;
         if (!use64) {
             float target = __fmul_rn(u2, a0), run = 0.0f;
-            for (uint32_t k = lb; k < le; k++) {
-                uint32_t r = fast ? (uint32_t)__ldg(T.one_list + k) : k;
-                float a = fast ? __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), 1.0f) : propensity<K>(T, r, c, resv, mult);
-                if (a > 0.0f) last_pos = (int)r;
+            unsigned long long m0 = c0, m1 = c1;
+            for (int r = next_bit(m0, m1); r >= 0; r = next_bit(m0, m1)) {
+                float a = propensity<K>(T, (uint32_t)r, c, resv, mult);
+                if (a > 0.0f) last_pos = r;
                 run = __fadd_rn(run, a);
-                if (target < run) { sel = (int)r; break; }
+                if (target < run) { sel = r; break; }
             }
         } else {
             atomicAdd(s_diag + PD_FP64_SEL, 1u);
             double a0d = 0.0;
-            for (uint32_t k = lb; k < le; k++) {
-                uint32_t r = fast ? (uint32_t)__ldg(T.one_list + k) : k;
-                float a = fast ? __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), 1.0f) : propensity<K>(T, r, c, resv, mult);
-                a0d = __dadd_rn(a0d, (double)a);
+            {
+                unsigned long long m0 = c0, m1 = c1;
+                for (int r = next_bit(m0, m1); r >= 0; r = next_bit(m0, m1))
+                    a0d = __dadd_rn(a0d, (double)propensity<K>(T, (uint32_t)r, c, resv, mult));
             }
             double target = __dmul_rn((double)u2, a0d), run = 0.0;
-            for (uint32_t k = lb; k < le; k++) {
-                uint32_t r = fast ? (uint32_t)__ldg(T.one_list + k) : k;
-                float a = fast ? __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), 1.0f) : propensity<K>(T, r, c, resv, mult);
-                if (a > 0.0f) last_pos = (int)r;
+            unsigned long long m0 = c0, m1 = c1;
+            for (int r = next_bit(m0, m1); r >= 0; r = next_bit(m0, m1)) {
+                float a = propensity<K>(T, (uint32_t)r, c, resv, mult);
+                if (a > 0.0f) last_pos = r;
                 run = __dadd_rn(run, (double)a);
-                if (target < run) { sel = (int)r; break; }
+                if (target < run) { sel = r; break; }
             }
         }
         if (sel < 0) sel = last_pos;
