@@ -509,6 +509,15 @@ cs_status cs_tiling_describe(int32_t index, int32_t* K, int32_t* TY, int32_t* TZ
     });
 }
 
+cs_status cs_tiling_kind(int32_t index, int32_t* kind, int32_t* brick_planes) {
+    return guarded([&] {
+        need(kind, "kind"); need(brick_planes, "brick_planes");
+        int k, bx;
+        prod_tiling_kind(index, &k, &bx);
+        *kind = k; *brick_planes = bx;
+    });
+}
+
 cs_status cs_set_tiling(cs_sim* sim, int32_t index, uint32_t segment_length) {
     return guarded([&] {
         need(sim, "sim");

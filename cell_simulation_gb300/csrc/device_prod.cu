@@ -30,6 +30,7 @@
 
 #include "cuda_check.h"
 #include "internal.h"
+#include "brick_kernel.cuh"
 #include "prod_common.cuh"
 #include "prod_kernel.cuh"
 
@@ -39,25 +40,45 @@ namespace cellsim {
 
 typedef void (*ProdKernelFn)(ProdParams);
 
+// A compiled step configuration.  kind 0: the tile pipeline alone over
+// (TY x TZ tile, x-segment) items.  kind 1: the brick pass over BX x TY x 32
+// bricks, followed by the tile pipeline `spill` (same K and TY, TZ = 32) over
+// the bricks the brick pass handed over.
+enum { KIND_TILE = 0, KIND_BRICK = 1 };
+
 struct KernelCfg {
-    int K, TY, TZ, NT;
+    int kind, K, TY, TZ, NT, BX;
     ProdKernelFn fn;
-    size_t (*smem)(uint32_t);
+    size_t (*smem)(uint32_t S1, uint32_t thr_words);
+    int spill;  // kind 1: index of the tile configuration for spilled bricks
 };
 
+template <int K, int TY, int TZ>
+static size_t tile_smem(uint32_t S1, uint32_t) { return Tile<K, TY, TZ>::smem(S1); }
+
 template <int K, int TY, int TZ, int NT, int MINB>
-static KernelCfg make_cfg() {
-    return KernelCfg{K, TY, TZ, NT, prod_step_kernel<K, TY, TZ, NT, MINB>, &Tile<K, TY, TZ>::smem};
+static KernelCfg tile_cfg() {
+    return KernelCfg{KIND_TILE, K, TY, TZ, NT, 0, prod_step_kernel<K, TY, TZ, NT, MINB>, &tile_smem<K, TY, TZ>, -1};
+}
+
+template <int K, int BX, int BY, int NT, int MINB, int CAP>
+static KernelCfg brick_cfg(int spill) {
+    return KernelCfg{KIND_BRICK, K, BY, 32, NT, BX, brick_step_kernel<K, BX, BY, NT, MINB, CAP>,
+                     &Brick<K, BX, BY, NT, CAP>::smem, spill};
 }
 
 static const std::vector<KernelCfg>& all_cfgs() {
     static const std::vector<KernelCfg> v = {
-        make_cfg<16, 8, 32, 256, 3>(), make_cfg<16, 4, 64, 256, 3>(), make_cfg<16, 16, 32, 256, 1>(),
-        make_cfg<16, 8, 64, 256, 1>(),  make_cfg<8, 8, 32, 256, 3>(),  make_cfg<8, 4, 64, 256, 3>(),
-        make_cfg<8, 16, 32, 256, 2>(),  make_cfg<8, 8, 64, 256, 2>(),
+        tile_cfg<16, 8, 32, 256, 3>(),          tile_cfg<16, 4, 64, 256, 3>(), tile_cfg<16, 16, 32, 256, 1>(),
+        tile_cfg<16, 8, 64, 256, 1>(),          tile_cfg<8, 8, 32, 256, 3>(),  tile_cfg<8, 4, 64, 256, 3>(),
+        tile_cfg<8, 16, 32, 256, 2>(),          tile_cfg<8, 8, 64, 256, 2>(),
+        brick_cfg<16, 8, 8, 256, 3, 64>(0),     brick_cfg<8, 8, 8, 256, 3, 64>(4),
     };
     return v;
 }
+
+// Threshold tables up to this many words are staged in shared memory by the brick pass.
+static constexpr uint32_t kThrSmemWords = 4096;
 
 // ------------------------------------------------------------------ host side
 
@@ -77,6 +98,8 @@ struct DeviceProd {
     DevBuf<float> rx_rate;
     DevBuf<unsigned long long> rmask;
     DevBuf<float> one;
+    DevBuf<uint32_t> quiet;
+    DevBuf<WorkItem> spill;  // bricks handed from the brick pass to the tile pipeline
     std::vector<float> h_rate;
     std::vector<uint8_t> h_rre;
     std::vector<unsigned long long> h_rmask;
@@ -228,16 +251,40 @@ static void build_one_table(DeviceProd* d) {
     d->one.alloc(one.size());
     CS_CUDA(cudaMemcpy(d->one.p, one.data(), one.size() * 4, cudaMemcpyHostToDevice));
     d->T.one = d->one.p;
+    // Quiet thresholds.  A voxel holding one particle of species q (no
+    // reservoir, no zero-order reaction) has a0 = one[q][0], and its first
+    // event is rejected when dt = -logf(u1) / a0 > tau, u1 = m * 2^-24 with
+    // m = (B(v,0)[3] >> 8) + 1.  For m <= quiet[q] that holds for certain:
+    // u1 <= exp(-a0 tau (1 + 2^-12)) gives -log(u1) >= a0 tau (1 + 2^-12),
+    // and the device logf (within 3 ulp) and the correctly rounded division
+    // lose far less than the 2^-12 margin.  Larger m take the exact path.
+    std::vector<uint32_t> quiet((size_t)d->n_rep * d->S1, 0u);
+    const double tau = (double)d->T.tau;
+    for (size_t i = 0; i < quiet.size(); i++) {
+        const float a0 = one[i * 3];
+        uint32_t m = 1u << 24;  // no reaction can fire: every draw is quiet
+        if (a0 > 0.0f) {
+            const double x = (double)a0 * tau * (1.0 + std::ldexp(1.0, -12));
+            const double ub = std::exp(-x) * 16777216.0;
+            m = ub >= 16777215.0 ? 16777215u : (uint32_t)std::floor(ub);
+        }
+        quiet[i] = m;
+    }
+    d->quiet.alloc(quiet.size());
+    CS_CUDA(cudaMemcpy(d->quiet.p, quiet.data(), quiet.size() * 4, cudaMemcpyHostToDevice));
+    d->T.quiet = d->quiet.p;
 }
 
 static int pick_default_cfg(uint32_t K) {
     const auto& c = all_cfgs();
     for (size_t i = 0; i < c.size(); i++)
-        if (c[i].K == (int)K && c[i].TY == 8 && c[i].TZ == 32) return (int)i;
+        if (c[i].K == (int)K && c[i].kind == KIND_BRICK) return (int)i;
     return -1;
 }
 
-// Work items for the current tile config: (replicate, y0, z0, x-segment).
+// Work items for the current config: (replicate, y0, z0, x-segment).  A brick
+// configuration uses segments of BX planes, x fastest, so that bricks sharing
+// halo planes run close together in time and the halo re-reads hit L2.
 static void build_items(DeviceProd* d) {
     const KernelCfg& cfg = all_cfgs()[d->cfg_index];
     std::vector<WorkItem> all, per_rep;
@@ -249,13 +296,19 @@ static void build_items(DeviceProd* d) {
     for (uint32_t ri = 0; ri < d->n_rep; ri++) {
         const RepDesc& r = d->h_reps[ri];
         d->rep_item_off[ri] = (uint32_t)per_rep.size();
-        uint32_t nseg = 1;
-        if (d->seg_len) nseg = (r.X + d->seg_len - 1) / d->seg_len;
-        else if (cols_total < want) nseg = (uint32_t)std::min<uint64_t>((want + cols_total - 1) / cols_total, std::max<uint32_t>(r.X / 16, 1));
-        uint32_t seg = (r.X + nseg - 1) / nseg;
-        for (uint32_t x0 = 0; x0 < r.X; x0 += seg)
-            for (uint32_t y0 = 0; y0 < r.Y; y0 += cfg.TY)
-                for (uint32_t z0 = 0; z0 < r.Z; z0 += cfg.TZ) {
+        uint32_t seg;
+        if (cfg.kind == KIND_BRICK) {
+            seg = (uint32_t)cfg.BX;
+        } else {
+            uint32_t nseg = 1;
+            if (d->seg_len) nseg = (r.X + d->seg_len - 1) / d->seg_len;
+            else if (cols_total < want)
+                nseg = (uint32_t)std::min<uint64_t>((want + cols_total - 1) / cols_total, std::max<uint32_t>(r.X / 16, 1));
+            seg = (r.X + nseg - 1) / nseg;
+        }
+        for (uint32_t y0 = 0; y0 < r.Y; y0 += cfg.TY)
+            for (uint32_t z0 = 0; z0 < r.Z; z0 += cfg.TZ)
+                for (uint32_t x0 = 0; x0 < r.X; x0 += seg) {
                     WorkItem w{};
                     w.rep = ri; w.y0 = y0; w.z0 = z0; w.x0 = x0; w.x1 = std::min(r.X, x0 + seg);
                     per_rep.push_back(w);
@@ -263,23 +316,37 @@ static void build_items(DeviceProd* d) {
     }
     d->rep_item_off[d->n_rep] = (uint32_t)per_rep.size();
     all = per_rep;
-    // batched order: largest work first (longest processing time first)
-    std::stable_sort(all.begin(), all.end(), [&](const WorkItem& a, const WorkItem& b) {
-        uint64_t wa = (uint64_t)(a.x1 - a.x0), wb = (uint64_t)(b.x1 - b.x0);
-        return wa > wb;
-    });
+    if (cfg.kind == KIND_TILE) {
+        // batched order: largest work first (longest processing time first)
+        std::stable_sort(all.begin(), all.end(), [&](const WorkItem& a, const WorkItem& b) {
+            uint64_t wa = (uint64_t)(a.x1 - a.x0), wb = (uint64_t)(b.x1 - b.x0);
+            return wa > wb;
+        });
+    }
     d->n_items = (uint32_t)all.size();
     d->items.alloc(all.size());
     d->items_rep.alloc(per_rep.size());
+    d->spill.alloc(all.size());
     CS_CUDA(cudaMemcpy(d->items.p, all.data(), all.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
     CS_CUDA(cudaMemcpy(d->items_rep.p, per_rep.data(), per_rep.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
 }
 
+static uint32_t thr_words(const DeviceProd* d) {
+    const uint32_t n = d->NC * d->NC * d->S1;
+    return n <= kThrSmemWords ? n : 0u;
+}
+
+static size_t cfg_smem(const DeviceProd* d, const KernelCfg& cfg) { return cfg.smem(d->S1, thr_words(d)); }
+
+static void set_attrs(const DeviceProd* d, const KernelCfg& cfg) {
+    CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg_smem(d, cfg)));
+    CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+}
+
 static void set_cfg(DeviceProd* d, int idx) {
     const KernelCfg& cfg = all_cfgs()[idx];
-    size_t sm = cfg.smem(d->S1);
-    CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    set_attrs(d, cfg);
+    if (cfg.kind == KIND_BRICK) set_attrs(d, all_cfgs()[cfg.spill]);
     d->cfg_index = idx;
     build_items(d);
     if (d->graph) {
@@ -288,13 +355,18 @@ static void set_cfg(DeviceProd* d, int idx) {
     }
 }
 
-static int grid_for(DeviceProd* d, uint32_t n_items) {
-    const KernelCfg& cfg = all_cfgs()[d->cfg_index];
+static int grid_for(DeviceProd* d, const KernelCfg& cfg, uint32_t n_items) {
     int per_sm = 0;
-    CS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg.fn, cfg.NT, cfg.smem(d->S1)));
+    CS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg.fn, cfg.NT, cfg_smem(d, cfg)));
     if (per_sm < 1) throw Error(CS_ERR_CUDA, "production kernel does not fit on an SM");
-    return (int)std::min<uint64_t>((uint64_t)per_sm * d->num_sms, n_items);
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)per_sm * d->num_sms, n_items));
 }
+
+// Counters of launch group g (0 = all replicates, 1 + r = replicate r alone)
+// for frame parity p: [0] work queue of the first launch, [1] spilled bricks,
+// [2] work queue of the spill pass.
+static constexpr int kCtrPerParity = 3;
+static uint32_t* group_ctr(DeviceProd* d, int g, int p) { return d->counters.p + (size_t)(2 * g + p) * kCtrPerParity; }
 
 // One frame over all replicates (batched) or over replicate `rep` alone.
 static void launch_frame(DeviceProd* d, int parity, int rep) {
@@ -310,18 +382,46 @@ static void launch_frame(DeviceProd* d, int parity, int rep) {
     P.reservoir = d->reservoir.n ? d->reservoir.p : nullptr;
     P.counts = d->counts.p;
     P.diag = d->diag.p;
+    const int g = rep < 0 ? 0 : 1 + rep;
+    uint32_t off = 0;
     if (rep < 0) {
         P.items = d->items.p;
         P.n_items = d->n_items;
-        P.counters = d->counters.p;
     } else {
-        P.items = d->items_rep.p + d->rep_item_off[rep];
-        P.n_items = d->rep_item_off[rep + 1] - d->rep_item_off[rep];
-        P.counters = d->counters.p + 2 * (1 + rep);
+        off = d->rep_item_off[rep];
+        P.items = d->items_rep.p + off;
+        P.n_items = d->rep_item_off[rep + 1] - off;
     }
-    int grid = grid_for(d, P.n_items);
-    cfg.fn<<<grid, cfg.NT, cfg.smem(d->S1), d->stream>>>(P);
+    uint32_t* ctr = group_ctr(d, g, parity);
+    P.queue = ctr;
+    P.reset = group_ctr(d, g, parity ^ 1);
+    P.n_reset = kCtrPerParity;
+    P.advance = 1u;
+    P.thr_smem = thr_words(d) != 0u;
+    const uint32_t n = P.n_items;
+    if (cfg.kind == KIND_BRICK) {
+        P.spill = d->spill.p + off;
+        P.n_spill = ctr + 1;
+    }
+    cfg.fn<<<grid_for(d, cfg, n), cfg.NT, cfg_smem(d, cfg), d->stream>>>(P);
     CS_LAUNCH_CHECK();
+    if (cfg.kind == KIND_BRICK) {
+        // the tile pipeline over the spilled bricks (usually none: its CTAs take no item and exit)
+        const KernelCfg& sc = all_cfgs()[cfg.spill];
+        ProdParams Q = P;
+        Q.items = d->spill.p + off;
+        Q.n_items = 0;
+        Q.n_items_dev = ctr + 1;
+        Q.queue = ctr + 2;
+        Q.reset = nullptr;
+        Q.n_reset = 0;
+        Q.advance = 0u;
+        Q.thr_smem = 0u;
+        Q.spill = nullptr;
+        Q.n_spill = nullptr;
+        sc.fn<<<grid_for(d, sc, n), sc.NT, cfg_smem(d, sc), d->stream>>>(Q);
+        CS_LAUNCH_CHECK();
+    }
 }
 
 static DeviceProd* prod_alloc(const Model& m, int device, const std::vector<RepDesc>& reps, uint64_t total_voxels) {
@@ -344,7 +444,7 @@ static DeviceProd* prod_alloc(const Model& m, int device, const std::vector<RepD
     for (int b = 0; b < 2; b++) d->slots[b].alloc(total_voxels * d->K);
     d->counts.alloc((size_t)d->n_rep * d->S1);
     d->diag.alloc(PD_N);
-    d->counters.alloc(2 * (1 + d->n_rep));
+    d->counters.alloc((size_t)2 * kCtrPerParity * (1 + d->n_rep));
     d->stepbuf.alloc(2);
     CS_CUDA(cudaMemset(d->diag.p, 0, PD_N * 4));
     CS_CUDA(cudaMemset(d->counters.p, 0, d->counters.bytes()));
@@ -665,6 +765,11 @@ void prod_tiling_desc(int i, int* K, int* TY, int* TZ, int* NT) {
     const auto& c = all_cfgs();
     if (i < 0 || i >= (int)c.size()) throw Error(CS_ERR_INVALID_ARG, "tile configuration index out of range");
     *K = c[i].K; *TY = c[i].TY; *TZ = c[i].TZ; *NT = c[i].NT;
+}
+void prod_tiling_kind(int i, int* kind, int* BX) {
+    const auto& c = all_cfgs();
+    if (i < 0 || i >= (int)c.size()) throw Error(CS_ERR_INVALID_ARG, "tile configuration index out of range");
+    *kind = c[i].kind; *BX = c[i].BX;
 }
 int prod_tiling_current(const DeviceProd* d) { return d->cfg_index; }
 cudaStream_t prod_stream(const DeviceProd* d) { return d->stream; }

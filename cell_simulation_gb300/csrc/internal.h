@@ -168,6 +168,7 @@ void prod_get_slots_raw(DeviceProd* d, uint8_t* out);
 void prod_set_tiling(DeviceProd* d, int cfg_index, uint32_t seg_len);
 int prod_tiling_count();
 void prod_tiling_desc(int i, int* K, int* TY, int* TZ, int* NT);
+void prod_tiling_kind(int i, int* kind, int* BX);
 int prod_tiling_current(const DeviceProd* d);
 void prod_seed(DeviceProd* d, uint64_t seed);
 float prod_time_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched);

@@ -2,9 +2,15 @@
 // shared by the fused tile kernel.  The algorithm (restated on the CPU in
 // oracle/prod_semantics.c) is:
 //
+//  Random words: B(v, s) = Philox4x32-10({v, frame, s, 0}, seed) for slot s,
+//  E(v, e) = Philox4x32-10({v, frame, 0x80000000 | e, 0}, seed) for reaction
+//  event e.  One block B(v, 0) serves slot 0 of voxel v in all three sweeps
+//  and the first reaction event, so a voxel holding one particle needs one
+//  Philox evaluation per frame.
+//
 //  Diffusion, three sweeps per frame (x, then y, then z).  In the sweep
-//  along axis a every particle of voxel v (slot s of its compacted content)
-//  draws u = Philox(v, frame, sweep<<24 | s/4)[s%4] and moves to v-a when
+//  along axis a = 0, 1, 2 every particle of voxel v (slot s of its compacted
+//  content) draws u = B(v, s)[a] and moves to v-a when
 //  u < T[r(v)][r(v-a)][q], to v+a when T[.][r(v-a)][q] <= u < that + T[r(v)][r(v+a)][q],
 //  where T = floor(D*tau/lambda^2 * 2^32) for the region codes (id+1; code 0
 //  = outside the lattice, all thresholds 0) -- the move probabilities of
@@ -21,9 +27,11 @@
 //  Reactions: an exact SSA (Gillespie direct method) inside each voxel over
 //  one tau, with FP32 propensities and FP32 exponential waiting times, an
 //  FP64 clock, and FP64 cumulative selection when max/min non-zero
-//  propensity exceeds 1e6 (or always, or never, by precision mode).  A
-//  reaction that would exceed K particles is rejected.  If anything fired,
-//  the voxel's slots are rewritten species-major (cme.wgsl:90-97).
+//  propensity exceeds 1e6 (or always, or never, by precision mode).  Event e
+//  takes its waiting-time word from B(v, 0)[3] (e = 0) or E(v, e)[0], and its
+//  selection word from E(v, e)[1].  A reaction that would exceed K particles
+//  is rejected.  If anything fired, the voxel's slots are rewritten
+//  species-major (cme.wgsl:90-97).
 #pragma once
 #include <cstdint>
 
@@ -31,7 +39,7 @@
 
 namespace cellsim {
 
-enum { PD_EVENTS = 0, PD_REJECT_CAP = 1, PD_EVENT_CAP = 2, PD_FP64_SEL = 3, PD_N = 8 };
+enum { PD_EVENTS = 0, PD_REJECT_CAP = 1, PD_EVENT_CAP = 2, PD_FP64_SEL = 3, PD_DENSE_BRICKS = 4, PD_N = 8 };
 
 struct RepDesc {
     uint64_t base;   // first voxel of this replicate in the packed slot/reservoir arrays
@@ -66,6 +74,9 @@ struct ProdTables {
     unsigned long long zmask[2];      // reactions without reactants
     const float* one;                 // [n_rep][S1][3]: a0, max a, min non-zero a for a voxel holding
                                       // exactly one particle of species q (q = 0: an empty voxel)
+    const uint32_t* quiet;            // [n_rep][S1]: a voxel holding one particle of species q and no
+                                      // reservoir has no reaction event in the frame when
+                                      // (B(v,0)[3] >> 8) + 1 <= quiet[q]
 };
 
 // K slot bytes held in 64-bit words, byte s = slot s.
@@ -140,26 +151,25 @@ __device__ __forceinline__ uint32_t lowest_bits(uint32_t m, uint32_t c) {
     return m;
 }
 
+__device__ __forceinline__ uint32_t sweep_word(const U4& b, uint32_t sweep) {
+    return sweep == 0u ? b.x : sweep == 1u ? b.y : b.z;
+}
+
 // Move decisions of one voxel for one sweep: bit s = slot s moves to the
-// lower neighbour, bit 16+s = to the upper neighbour.
+// lower neighbour, bit 16+s = to the upper neighbour.  tlo / thi are the
+// threshold rows T[r(v)][r(lower)][.] and T[r(v)][r(upper)][.]; w0 is slot
+// 0's word B(v, 0)[sweep], evaluated by the caller.
 template <int K>
-__device__ __forceinline__ uint32_t decide_moves(const Vox<K>& c, uint32_t v, uint32_t frame, uint32_t sweep, uint32_t rs,
-                                                 uint32_t rlo, uint32_t rhi, uint32_t k0, uint32_t k1, const ProdTables& T) {
-    uint32_t n = vox_n<K>(c);
-    if (n == 0) return 0u;
-    const uint32_t* tlo = T.thr + ((size_t)rs * T.NC + rlo) * T.S1;
-    const uint32_t* thi = T.thr + ((size_t)rs * T.NC + rhi) * T.S1;
-    uint32_t mask = 0, group = 0xFFFFFFFFu;
-    U4 ph{0, 0, 0, 0};
+__device__ __forceinline__ uint32_t decide_moves(const Vox<K>& c, uint32_t v, uint32_t frame, uint32_t sweep,
+                                                 const uint32_t* tlo, const uint32_t* thi, uint32_t k0, uint32_t k1,
+                                                 uint32_t w0) {
+    const uint32_t n = vox_n<K>(c);
+    uint32_t mask = 0;
     for (uint32_t s = 0; s < n; s++) {
-        uint32_t q = vox_get<K>(c, s);
-        uint32_t tm = __ldg(tlo + q), tp = __ldg(thi + q);
+        const uint32_t q = vox_get<K>(c, s);
+        const uint32_t tm = tlo[q], tp = thi[q];
         if ((tm | tp) == 0u) continue;
-        if ((s >> 2) != group) {
-            group = s >> 2;
-            ph = d_philox(v, frame, (sweep << 24) | group, 0u, k0, k1);
-        }
-        uint32_t u = (s & 3u) == 0u ? ph.x : (s & 3u) == 1u ? ph.y : (s & 3u) == 2u ? ph.z : ph.w;
+        const uint32_t u = s == 0u ? w0 : sweep_word(d_philox(v, frame, s, 0u, k0, k1), sweep);
         if (u < tm) mask |= 1u << s;
         else if ((uint64_t)u < (uint64_t)tm + tp) mask |= 1u << (16 + s);
     }
@@ -267,10 +277,11 @@ __device__ __forceinline__ int next_bit(unsigned long long& m0, unsigned long lo
 // SSA within tau for one voxel.  Returns true when any reaction fired (the
 // content is then rewritten species-major).  s_delta[S1] and s_diag[PD_N]
 // are block-shared accumulators.
+// w3 is B(v, 0)[3], evaluated by the caller.
 template <int K>
 __device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0, uint32_t k1,
                                          float mult, uint32_t rep, const ProdTables& T, int32_t* s_delta,
-                                         uint32_t* s_diag) {
+                                         uint32_t* s_diag, uint32_t w3) {
     if (T.R == 0) return false;
     uint32_t n = vox_n<K>(c);
     double td = 0.0;
@@ -296,8 +307,12 @@ __device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, u
             }
         }
         if (!(a0 > 0.0f)) break;
-        U4 ph = d_philox(v, frame, (3u << 24) | (ev >> 1), 0u, k0, k1);
-        uint32_t w1 = (ev & 1u) ? ph.z : ph.x, w2 = (ev & 1u) ? ph.w : ph.y;
+        U4 ph{0u, 0u, 0u, 0u};
+        uint32_t w1 = w3;
+        if (ev != 0u) {
+            ph = d_philox(v, frame, 0x80000000u | ev, 0u, k0, k1);
+            w1 = ph.x;
+        }
         float u1 = __fmul_rn((float)((w1 >> 8) + 1u), 0x1p-24f);
         float dt = __fdiv_rn(-d_logf(u1), a0);
         if (T.precision == 1) {
@@ -307,6 +322,8 @@ __device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, u
             td = __dadd_rn(td, (double)dt);
             if (td > T.tau_d) break;
         }
+        if (ev == 0u) ph = d_philox(v, frame, 0x80000000u, 0u, k0, k1);
+        const uint32_t w2 = ph.y;
         float u2 = __fmul_rn((float)(w2 >> 8), 0x1p-24f);
         bool use64 = (T.precision == 2) || (T.precision == 0 && amax > __fmul_rn(1e6f, amin));
         int sel = -1;

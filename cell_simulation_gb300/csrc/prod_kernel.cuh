@@ -28,14 +28,22 @@
 
 namespace cellsim {
 
+// Launch parameters shared by the brick pass and the tile pipeline.
 struct ProdParams {
     ProdTables T;
     const RepDesc* reps;
     const WorkItem* items;
     uint32_t n_items;
+    const uint32_t* n_items_dev;  // when set, the item count is read here at kernel start
+    uint32_t* queue;              // work-queue counter of this launch (zero at launch)
+    uint32_t* reset;              // n_reset counters that block 0 zeroes for the next frame
+    uint32_t n_reset;
+    uint32_t advance;             // nonzero: block 0 writes frame + 1 to stepbuf[parity ^ 1]
+    uint32_t thr_smem;            // nonzero: the threshold table is staged in shared memory
     uint32_t parity;
-    uint32_t* counters;  // [2]
-    uint32_t* stepbuf;   // [2]
+    uint32_t* stepbuf;            // [2] frame numbers
+    WorkItem* spill;              // brick pass: bricks handed over to the tile pipeline
+    uint32_t* n_spill;
     const uint8_t* src;
     uint8_t* dst;
     const uint8_t* region_pad;   // padded region codes, see RepDesc::rbase
@@ -142,18 +150,19 @@ __global__ void __launch_bounds__(NT, MINB) prod_step_kernel(ProdParams P) {
     const int tid = threadIdx.x;
     const uint32_t frame = P.stepbuf[P.parity];
     if (blockIdx.x == 0 && tid == 0) {
-        P.counters[P.parity ^ 1u] = 0u;
-        P.stepbuf[P.parity ^ 1u] = frame + 1u;
+        for (uint32_t i = 0; i < P.n_reset; i++) P.reset[i] = 0u;
+        if (P.advance) P.stepbuf[P.parity ^ 1u] = frame + 1u;
     }
     for (int i = tid; i < PD_N; i += NT) s_diag[i] = 0u;
     const bool always_react = P.T.n_zero_order != 0u;
+    const uint32_t n_items = P.n_items_dev ? *P.n_items_dev : P.n_items;
 
     for (;;) {
         __syncthreads();
-        if (tid == 0) s_item = atomicAdd(P.counters + P.parity, 1u);
+        if (tid == 0) s_item = atomicAdd(P.queue, 1u);
         __syncthreads();
         const uint32_t it = s_item;
-        if (it >= P.n_items) break;
+        if (it >= n_items) break;
         const WorkItem wi = P.items[it];
         const RepDesc rd = P.reps[wi.rep];
         const int X = (int)rd.X, Y = (int)rd.Y, Z = (int)rd.Z, Zr = (int)rd.Zr;
@@ -173,6 +182,13 @@ __global__ void __launch_bounds__(NT, MINB) prod_step_kernel(ProdParams P) {
         auto dx_plane = [&](int p) -> uint32_t* { return dxb + ((p + 4) & 3) * WIN; };
         auto lin = [&](int p, int y, int z) -> uint32_t {
             return ((uint32_t)p * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
+        };
+        // move decisions of a non-empty voxel in sweep a between region codes rs (own), rlo, rhi
+        auto decide = [&](const Vox<K>& c, uint32_t v, uint32_t a, uint32_t rs, uint32_t rlo, uint32_t rhi) -> uint32_t {
+            const uint32_t* tlo = P.T.thr + ((size_t)rs * P.T.NC + rlo) * P.T.S1;
+            const uint32_t* thi = P.T.thr + ((size_t)rs * P.T.NC + rhi) * P.T.S1;
+            const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
+            return decide_moves<K>(c, v, frame, a, tlo, thi, k0, k1, sweep_word(b0, a));
         };
         // region code at window position (wy, wz) of plane p (wy, wz may step one past the window)
         auto code_at = [&](int p, int wy, int wz) -> uint32_t {
@@ -332,8 +348,13 @@ __global__ void __launch_bounds__(NT, MINB) prod_step_kernel(ProdParams P) {
                         if (move)
                             r = combine<K>(r, dz[e], yp[e - 1], dz[e - 1], yp[e + 1], dz[e + 1], v, v - 1u, v + 1u, frame, 2u);
                         uint32_t rv = resv ? (uint32_t)resv[v] : 0u;
-                        if (rv != 0u || always_react || !vox_empty<K>(r))
-                            react_voxel<K>(r, rv, v, frame, k0, k1, mult, rd.counts_index, P.T, s_delta, s_diag);
+                        if (rv != 0u || always_react || !vox_empty<K>(r)) {
+                            const uint32_t w3 = d_philox(v, frame, 0u, 0u, k0, k1).w;
+                            const bool quiet = rv == 0u && !always_react && vox_n<K>(r) == 1u &&
+                                               (w3 >> 8) + 1u <= P.T.quiet[(size_t)rd.counts_index * P.T.S1 + vox_get<K>(r, 0)];
+                            if (!quiet)
+                                react_voxel<K>(r, rv, v, frame, k0, k1, mult, rd.counts_index, P.T, s_delta, s_diag, w3);
+                        }
                         st_vox_g<K>(dst + (uint64_t)v * K, r);
                     } else if (k < bC) {  // B: X sweep (movers) and/or y-decisions
                         const uint32_t q = k - bB;
@@ -356,8 +377,7 @@ __global__ void __launch_bounds__(NT, MINB) prod_step_kernel(ProdParams P) {
                         }
                         uint32_t d = 0u;
                         if (!vox_empty<K>(r))
-                            d = decide_moves<K>(r, v, frame, 1u, code_at(pB, wy, wz), code_at(pB, wy - 1, wz),
-                                                code_at(pB, wy + 1, wz), k0, k1, P.T);
+                            d = decide(r, v, 1u, code_at(pB, wy, wz), code_at(pB, wy - 1, wz), code_at(pB, wy + 1, wz));
                         dyb[(pB & 1) * WIN + e] = d;
                     } else if (k < bA) {  // C: Y sweep (movers) and/or z-decisions
                         const uint32_t q = k - bC;
@@ -379,8 +399,7 @@ __global__ void __launch_bounds__(NT, MINB) prod_step_kernel(ProdParams P) {
                         }
                         uint32_t d = 0u;
                         if (!vox_empty<K>(r))
-                            d = decide_moves<K>(r, v, frame, 2u, code_at(pC, wy, wz), code_at(pC, wy, wz - 1),
-                                                code_at(pC, wy, wz + 1), k0, k1, P.T);
+                            d = decide(r, v, 2u, code_at(pC, wy, wz), code_at(pC, wy, wz - 1), code_at(pC, wy, wz + 1));
                         dzb[(pC & 1) * WIN + e] = d;
                     } else {  // A: x-decisions
                         const uint32_t q = k - bA;
@@ -388,8 +407,8 @@ __global__ void __launch_bounds__(NT, MINB) prod_step_kernel(ProdParams P) {
                         int e = wl[LA * WIN + q];
                         int wy = e / WZ, wz = e - wy * WZ;
                         uint32_t v = lin(pA, y0 - 1 + wy, z0 - 1 + wz);
-                        dx_plane(pA)[e] = decide_moves<K>(raw_plane(pA)[e], v, frame, 0u, code_at(pA, wy, wz),
-                                                          code_at(pA - 1, wy, wz), code_at(pA + 1, wy, wz), k0, k1, P.T);
+                        dx_plane(pA)[e] = decide(raw_plane(pA)[e], v, 0u, code_at(pA, wy, wz), code_at(pA - 1, wy, wz),
+                                                 code_at(pA + 1, wy, wz));
                     }
                 }
             }

@@ -106,6 +106,7 @@ SIGNATURES = {
     "cs_step_philox_timed": (st, [P, C.c_uint32, C.c_uint64, f32p]),
     "cs_tiling_count": (st, [i32p]),
     "cs_tiling_describe": (st, [C.c_int32, i32p, i32p, i32p, i32p]),
+    "cs_tiling_kind": (st, [C.c_int32, i32p, i32p]),
     "cs_set_tiling": (st, [P, C.c_int32, C.c_uint32]),
     "cs_get_tiling": (st, [P, i32p]),
     "cs_ensemble_create": (st, [P, C.c_uint32, u32p, u64p, f32p, u32p, C.c_int32, C.POINTER(P)]),

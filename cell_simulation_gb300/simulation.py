@@ -331,6 +331,20 @@ def tiling_variants() -> list[tuple[int, int, int, int]]:
     return out
 
 
+def tiling_kinds() -> list[tuple[int, int]]:
+    """(kind, brick_planes) of every compiled variant: kind 0 = tile pipeline,
+    kind 1 = sparse brick pass (crowded bricks finished by the tile pipeline)."""
+    lib = N.load()
+    n = C.c_int32()
+    N.check(lib.cs_tiling_count(C.byref(n)))
+    out = []
+    for i in range(n.value):
+        kind, bx = C.c_int32(), C.c_int32()
+        N.check(lib.cs_tiling_kind(i, C.byref(kind), C.byref(bx)))
+        out.append((kind.value, bx.value))
+    return out
+
+
 class Ensemble:
     """Replicates of one model stepped by one launch per frame (cs_ensemble_*)."""
 

@@ -267,10 +267,15 @@ cs_status cs_ref_frame_noalloc(const cs_ref_frame_noalloc_args* args);
  * examples/no_window.rs:141-163). */
 cs_status cs_step_timed(cs_sim* sim, uint32_t n_steps, const uint32_t* itimes, float* ms);
 cs_status cs_step_philox_timed(cs_sim* sim, uint32_t n_steps, uint64_t seed, float* ms);
-/* Compiled (K, TY, TZ, threads) variants of the fused step kernel and the
- * x-segment length of a work item (0 = automatic); used by the autotuner. */
+/* Compiled (K, TY, TZ, threads) variants of the step and the x-segment
+ * length of a work item (0 = automatic; tile pipeline only); used by the
+ * autotuner.  cs_tiling_kind: kind 0 = tile pipeline over (TY x TZ tile,
+ * x-segment) items; kind 1 = sparse brick pass over brick_planes x TY x TZ
+ * bricks, crowded bricks finished by the tile pipeline.  No reference
+ * counterpart (the reference has one fixed dispatch shape per shader). */
 cs_status cs_tiling_count(int32_t* n);
 cs_status cs_tiling_describe(int32_t index, int32_t* K, int32_t* TY, int32_t* TZ, int32_t* threads);
+cs_status cs_tiling_kind(int32_t index, int32_t* kind, int32_t* brick_planes);
 cs_status cs_set_tiling(cs_sim* sim, int32_t index, uint32_t segment_length);
 cs_status cs_get_tiling(const cs_sim* sim, int32_t* index);
 

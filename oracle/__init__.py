@@ -73,6 +73,8 @@ def load() -> C.CDLL:
         lib.orc_prod_run.restype = C.c_int
         lib.orc_prod_run.argtypes = [C.POINTER(ProdParams), C.POINTER(Tables), C.c_void_p, C.c_void_p, C.c_uint32,
                                      C.c_uint32, C.c_void_p]
+        lib.orc_first_event_inside.restype = C.c_uint32
+        lib.orc_first_event_inside.argtypes = [C.c_float, C.c_float, C.c_uint32, C.c_uint32]
         lib.orc_ssa_fp64_batch.restype = C.c_int64
         lib.orc_ssa_fp64_batch.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
@@ -132,6 +134,11 @@ def prod_run(res, K, n_regions, n_species, n_reactions, tau, lam, tab, slots_u8,
     if rc != 0:
         raise ValueError(f"orc_prod_run failed: {rc}")
     return diag
+
+
+def first_event_inside(a0, tau, lo, hi) -> int:
+    """Draws m in [lo, hi] (u1 = m 2^-24) whose first reaction event lands inside tau."""
+    return int(load().orc_first_event_inside(float(a0), float(tau), int(lo), int(hi)))
 
 
 def ssa_batch(S, reactants, rates, ch_species, ch_delta, x0, seed0, n_rep, t_samples, fpt_species=0, fpt_threshold=0):

@@ -103,6 +103,9 @@ enum { ORC_PD_EVENTS = 0, ORC_PD_REJECT_CAP = 1, ORC_PD_EVENT_CAP = 2, ORC_PD_FP
 int orc_prod_run(const orc_prod_params* p, const orc_tables* t, uint8_t* slots, int64_t* counts,
                  uint32_t frame0, uint32_t n_steps, uint32_t* diag);
 
+/* Draws m in [lo, hi] (u1 = m 2^-24) with -logf(u1)/a0 <= tau. */
+uint32_t orc_first_event_inside(float a0, float tau, uint32_t lo, uint32_t hi);
+
 /* ---- 3. well-mixed FP64 SSA ---- */
 /* Gillespie direct method.  reactants [R][3] (0 = void), ch_* as above,
  * rates [R] in well-mixed units (events per second per reactant tuple).

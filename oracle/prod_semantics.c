@@ -9,15 +9,19 @@
  *    T[a][b][q] = floor(min(D[a-1][b-1][q] * tau / lambda^2, 1) * 2^32) in
  *    FP64 (the probabilities of res/shader/rdme.wgsl:132-136), 0 if a or b
  *    is 0;
- *  - sweep a in (x, y, z): particle at slot s of voxel v draws
- *    u = Philox4x32-10(ctr = {v, frame, a<<24 | s/4, 0}, key = seed)[s%4];
- *    moves down if u < T[c(v)][c(v-a)][q], up if u < that + T[c(v)][c(v+a)][q];
+ *  - random words: B(v, s) = Philox4x32-10(ctr = {v, frame, s, 0}, key = seed)
+ *    for slot s < K, E(v, e) = Philox4x32-10(ctr = {v, frame, 0x80000000 | e, 0});
+ *  - sweep a in (x, y, z) = (0, 1, 2): the particle at slot s of voxel v draws
+ *    u = B(v, s)[a]; it moves down if u < T[c(v)][c(v-a)][q], up if
+ *    u < that + T[c(v)][c(v+a)][q];
  *  - room K - n(w) of a receiving voxel is split: lower neighbour gets
  *    (room + ((w + frame + a) & 1)) / 2, upper neighbour the rest; the first
  *    movers in slot order up to the share are accepted;
  *  - new content: own stayers (slot order), accepted arrivals from below,
  *    then from above;
- *  - reactions: SSA inside the voxel for one tau (see react below).
+ *  - reactions: SSA inside the voxel for one tau (see react below); event e
+ *    draws its waiting-time word from B(v, 0)[3] when e = 0 and from
+ *    E(v, e)[0] otherwise, and its selection word from E(v, e)[1].
  */
 #include <math.h>
 #include <stdint.h>
@@ -63,18 +67,15 @@ static uint32_t lowest_bits(uint32_t m, uint32_t c) {
 
 static uint32_t decide(const pctx* c, const uint8_t* cont, uint32_t v, uint32_t frame, uint32_t sweep, uint32_t rs,
                        uint32_t rlo, uint32_t rhi, const uint32_t key[2]) {
-    uint32_t n = nbytes(cont, c->K), mask = 0, group = 0xFFFFFFFFu, ph[4] = {0, 0, 0, 0};
+    uint32_t n = nbytes(cont, c->K), mask = 0, ph[4];
     for (uint32_t s = 0; s < n; s++) {
         uint32_t q = cont[s];
         uint32_t tm = c->thr[((size_t)rs * c->NC + rlo) * c->S1 + q];
         uint32_t tp = c->thr[((size_t)rs * c->NC + rhi) * c->S1 + q];
         if ((tm | tp) == 0u) continue;
-        if ((s >> 2) != group) {
-            group = s >> 2;
-            uint32_t ctr[4] = {v, frame, (sweep << 24) | group, 0u};
-            orc_philox4x32_10(ctr, key, ph);
-        }
-        uint32_t u = ph[s & 3u];
+        uint32_t ctr[4] = {v, frame, s, 0u};
+        orc_philox4x32_10(ctr, key, ph);
+        uint32_t u = ph[sweep];
         if (u < tm) mask |= 1u << s;
         else if ((uint64_t)u < (uint64_t)tm + tp) mask |= 1u << (16 + s);
     }
@@ -141,9 +142,16 @@ static void react(const pctx* c, const orc_prod_params* p, uint8_t* cont, uint32
             if (a > 0.0f) { amax = fmaxf(amax, a); amin = fminf(amin, a); }
         }
         if (!(a0 > 0.0f)) break;
-        uint32_t ctr[4] = {v, frame, (3u << 24) | (ev >> 1), 0u}, ph[4];
+        uint32_t ctr[4] = {v, frame, 0x80000000u | ev, 0u}, ph[4], w1;
         orc_philox4x32_10(ctr, key, ph);
-        uint32_t w1 = (ev & 1u) ? ph[2] : ph[0], w2 = (ev & 1u) ? ph[3] : ph[1];
+        if (ev == 0) {
+            uint32_t c0[4] = {v, frame, 0u, 0u}, b0[4];
+            orc_philox4x32_10(c0, key, b0);
+            w1 = b0[3];
+        } else {
+            w1 = ph[0];
+        }
+        uint32_t w2 = ph[1];
         float u1 = (float)((w1 >> 8) + 1u) * 0x1p-24f;
         float dt = -orc_logf(u1) / a0;
         if (p->precision == 1) {
@@ -275,4 +283,18 @@ int orc_prod_run(const orc_prod_params* p, const orc_tables* t, uint8_t* slots, 
     }
     free(nxt); free(dec); free(c.thr); free(c.code); free(c.rre); free(c.rate); free(c.csp); free(c.cd);
     return 0;
+}
+
+/* Number of draws m in [lo, hi] (u1 = m * 2^-24) whose first reaction event
+ * falls inside tau, dt = -logf(u1) / a0 <= tau, for a voxel with total
+ * propensity a0.  The production step skips the exact SSA for draws below a
+ * tabulated threshold; this counts the draws that would contradict it. */
+uint32_t orc_first_event_inside(float a0, float tau, uint32_t lo, uint32_t hi) {
+    uint32_t n = 0;
+    for (uint64_t m = lo; m <= hi; m++) {
+        float u1 = (float)(uint32_t)m * 0x1p-24f;
+        float dt = -orc_logf(u1) / a0;
+        if (!((double)dt > (double)tau)) n++;
+    }
+    return n;
 }

@@ -71,3 +71,24 @@ def crowded_model(res=(6, 5, 4), K=4, counts=(30, 20, 10), seed=3, D=1e-12) -> S
     sim.add_reaction(["A", "B"], ["C"], 300.0)
     sim.add_reaction(["C"], ["A", "B"], 200.0)
     return sim
+
+
+def patchy_model(res=(19, 21, 70), K=16, seed=11, dense=900, sparse=150, D=1e-12) -> Simulation:
+    """Mostly empty lattice with one crowded cube (about a third of its voxels
+    occupied): the production brick pass keeps the sparse bricks and hands the
+    crowded ones to the tile pipeline."""
+    dims = [r * LAM for r in res]
+    sim = Simulation(LatticeParams(dims, list(res), configs.stable_tau(D), LAM, K))
+    sim.seed_placement(seed)
+    sim.add_region(RegionType.Cube("dense", [2 * LAM, 3 * LAM, 5 * LAM], [12 * LAM, 11 * LAM, 30 * LAM]), D)
+    sim.prepare_regions()
+    sim.set_diffusion_rate("background", D)
+    sim.set_transition_rate("dense", "background", D * 0.5)
+    sim.set_transition_rate("background", "dense", D * 0.5)
+    sim.add_particle_count("A", "dense", dense, True, False)
+    sim.add_particle_count("B", "background", sparse, True, False)
+    sim.add_particle_count("C", "background", 0, True, False)
+    sim.add_reaction(["A", "B"], ["C"], 700.0)
+    sim.add_reaction(["C"], ["A", "B"], 60.0)
+    sim.add_reaction(["A"], ["B"], 20.0)
+    return sim

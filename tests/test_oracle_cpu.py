@@ -3,6 +3,7 @@ own two formulations (serial order vs gather + OpenMP)."""
 import numpy as np
 import pytest
 
+from cell_simulation_gb300 import configs
 from tests.helpers import crowded_model, itime_schedule, multi_region_model, oracle_args, ref_state
 
 # Random123 known-answer vectors for Philox4x32-10 (published with the algorithm)
@@ -141,3 +142,28 @@ def test_conservation_without_reactions(orc):
     sl = a.slots.reshape(-1, K)
     for q in range(1, S1):
         assert np.array_equal(conc[:, q], (sl == q).sum(1))
+
+
+def quiet_threshold(a0: np.float32, tau: np.float32) -> int:
+    """The production step's tabulated bound: draws m <= this give dt > tau."""
+    if not a0 > 0:
+        return 1 << 24
+    x = float(a0) * float(tau) * (1.0 + 2.0 ** -12)
+    ub = np.exp(-x) * 16777216.0
+    return 16777215 if ub >= 16777215.0 else int(np.floor(ub))
+
+
+@pytest.mark.parametrize("tau", [configs.stable_tau(1e-12), configs.stable_tau(1e-11)])
+def test_quiet_threshold_is_exact(orc, tau):
+    """Exhaustively over every draw m <= threshold: the exact waiting time
+    -logf(m 2^-24) / a0 exceeds tau, so skipping the SSA there changes nothing."""
+    tau = np.float32(tau)
+    for a0 in (1e-30, 1e-8, 1e-3, 0.37, 5.0, 120.0, 3e3, 1e4, 6e4, 1e6, 1e8):
+        a0 = np.float32(a0)
+        m = quiet_threshold(a0, tau)
+        if m >= 1:
+            assert orc.first_event_inside(a0, tau, 1, m) == 0, (a0, m)
+        # the bound is useful: the draws above it that are still quiet are few
+        if 1 <= m < (1 << 24) - 1:
+            hi = min((1 << 24), m + 4096)
+            assert orc.first_event_inside(a0, tau, m + 1, hi) > 0 or float(a0) * float(tau) < 1e-6, (a0, m)

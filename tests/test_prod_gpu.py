@@ -4,8 +4,9 @@ conservation, region confinement and batched-ensemble equivalence."""
 import numpy as np
 import pytest
 
-from cell_simulation_gb300 import Ensemble, PREC_FP32, PREC_FP64, PREC_MIXED, RNG_PHILOX, configs, tiling_variants
-from tests.helpers import crowded_model, multi_region_model, oracle_args
+from cell_simulation_gb300 import (Ensemble, PREC_FP32, PREC_FP64, PREC_MIXED, RNG_PHILOX, configs, tiling_kinds,
+                                   tiling_variants)
+from tests.helpers import crowded_model, multi_region_model, oracle_args, patchy_model
 
 pytestmark = pytest.mark.gpu
 
@@ -69,6 +70,32 @@ def test_precision_modes_match_oracle(orc, precision):
     assert np.array_equal(got_s, want_s)
     assert np.array_equal(got_c, want_c)
     assert np.array_equal(got_d[:4], want_d[:4])
+
+
+def brick_tilings(K):
+    return [i for i, (t, (kind, _)) in enumerate(zip(tiling_variants(), tiling_kinds())) if t[0] == K and kind == 1]
+
+
+@pytest.mark.parametrize("K", [8, 16])
+def test_brick_pass_with_spilled_bricks_matches_oracle(orc, K):
+    """Sparse bricks run in the brick pass, the crowded cube's bricks overflow
+    its pools and are finished by the tile pipeline: the frame is the same."""
+    mk = lambda: patchy_model(K=K)
+    want_s, want_c, want_d = oracle_prod(orc, mk(), 24, seed=77)
+    for ti in brick_tilings(K):
+        got_s, got_c, got_d = gpu_prod(mk(), 24, 77, tiling=ti, chunks=2)
+        assert np.array_equal(got_s, want_s), (ti, np.flatnonzero(got_s != want_s)[:8])
+        assert np.array_equal(got_c, want_c), ti
+        assert np.array_equal(got_d[:4], want_d[:4]), (ti, got_d, want_d)
+        spilled = int(got_d[4])
+        n_bricks = 3 * 3 * 3  # (19/8, 21/8, 70/32) rounded up
+        assert 0 < spilled < 24 * n_bricks, spilled  # some bricks spill, most do not
+
+
+def test_sparse_lattice_never_spills():
+    sim = multi_region_model(res=(24, 20, 40), K=16, counts=(60, 50, 40, 30))
+    _, _, d = gpu_prod(sim, 10, 5)
+    assert d[4] == 0
 
 
 def test_crowded_capacity_rule(orc):
