@@ -18,23 +18,25 @@
 // Shared memory holds the box only in compacted form.  Per box row there is
 // a 64-bit mask per quantity (occupied, moving down / up along an axis, has
 // content after a sweep), and the contents of the voxels a phase produces
-// are kept in a pool ordered by (row, column): the pool index of voxel
-// (row, c) is rowbase[row] + popcount(mask[row] below c).  Each warp owns a
-// fixed partition of every pool and fills it from the rows it handles
-// (rows w, w + NW, ...), so no CTA-wide scan is needed.  A phase enumerates
-// its voxels from the masks into a per-warp list and runs them with all 32
-// lanes.  The lattice is mostly empty, so a brick holds a few hundred
-// entries per pool where the dense box has thousands of voxels; the CTA
-// footprint stays small enough for several CTAs per SM.
+// are kept in a pool where every row's voxels are contiguous: the pool index
+// of voxel (row, c) is rowbase[row] + popcount(mask[row] below c).  Warps
+// handle rows w, w + NW, ... and reserve the pool range of their rows with
+// one shared-memory atomic, so no CTA-wide scan is needed.  A phase writes
+// the positions of its voxels into a list indexed like its pool, and after a
+// barrier the whole CTA runs the list with every lane busy.  The lattice is
+// mostly empty, so a brick holds a few hundred entries per pool where the
+// dense box has thousands of voxels, and the CTA footprint stays small
+// enough for three CTAs per SM.
 //
 // The Philox block B(v, 0) of a voxel is evaluated once per frame, in the
 // first phase that sees the voxel non-empty, and its words (x, y, z draw of
 // slot 0, first reaction event) are kept beside that phase's pool entry.
 //
-// A brick whose occupancy overflows a warp's partition is abandoned before
-// it writes anything to global memory and handed to the tile pipeline
-// (prod_kernel.cuh) through the spill list, so crowded regions still get the
-// exact result.
+// A brick whose occupancy overflows a pool is abandoned before it writes
+// anything to global memory and appended to the spill list.  A second launch
+// of this kernel with pools as large as the box (never overflows) finishes
+// the spilled bricks in groups of a few planes, so crowded regions get the
+// same result.
 #pragma once
 #include <cstdint>
 
@@ -43,7 +45,7 @@
 
 namespace cellsim {
 
-template <int K, int BX, int BY, int NT, int CAP>
+template <int K, int BX, int BY, int NT, int CAP0, int CAP1, int CAP2>
 struct Brick {
     static constexpr int NW = NT / 32;
     static constexpr int PX = BX + 2, WY = BY + 2, WZ = 34;
@@ -53,43 +55,58 @@ struct Brick {
     static constexpr int RW1 = (NROW1 + NW - 1) / NW, RW2 = (NROW2 + NW - 1) / NW;
     static constexpr int RPX = BX + 4, RWY = BY + 4, RWZB = 48, RPLANE = RWY * RWZB;
     static constexpr int NCH = RPX * RWY * (RWZB / 16);  // 16-byte region chunks
-    static constexpr int POOL = NW * CAP;
-    static constexpr int LCAP = CAP > RW2 * 32 ? CAP : RW2 * 32;  // per-warp list
+    static constexpr int C02 = CAP0 > CAP2 ? CAP0 : CAP2;
+    static constexpr int LCAP = CAP1 > CAP2 ? (CAP1 > NROW2 * 32 ? CAP1 : NROW2 * 32) : (CAP2 > NROW2 * 32 ? CAP2 : NROW2 * 32);
+    static constexpr bool DENSE = CAP0 >= NROW0 * WZ && CAP1 >= NROW1 * WZ && CAP2 >= NROW2 * WZ;  // never overflows
     static_assert(NT % 32 == 0 && RW1 <= 32 && RW2 <= 32, "one lane per row of a warp's share");
-    static_assert(NROW0 * 64 <= 65536 && POOL <= 65536, "positions and pool indices fit 16 bits");
+    static_assert(NROW0 * 64 <= 65536 && C02 < 65536 && CAP1 < 65536, "positions and pool indices fit 16 bits");
     enum : int {
         M_OCC0 = 0, M_XM = NROW0, M_XP = 2 * NROW0,
         M_S1 = 3 * NROW0, M_YM = M_S1 + NROW1, M_YP = M_YM + NROW1, M_PB1 = M_YP + NROW1,
         M_S2 = M_PB1 + NROW1, M_ZM = M_S2 + NROW2, M_ZP = M_ZM + NROW2, M_PB2 = M_ZP + NROW2,
         M_N = M_PB2 + NROW2
     };
-    enum : int { U_DEC0 = 0, U_W01, U_W02, U_W03, U_DEC1, U_W12, U_W13, U_DEC2, U_W23, U_N };
     static constexpr size_t a16(size_t x) { return (x + 15) / 16 * 16; }
-    static constexpr size_t off_c0 = 0;                                    // Vox [POOL] pool 0 contents
-    static constexpr size_t off_c1 = off_c0 + (size_t)POOL * K;            // Vox [POOL] pool 1
-    static constexpr size_t off_c2 = off_c1 + (size_t)POOL * K;            // Vox [POOL] pool 2
-    static constexpr size_t off_m = off_c2 + (size_t)POOL * K;             // u64 [M_N] row masks
-    static constexpr size_t off_u = off_m + (size_t)M_N * 8;               // u32 [U_N][POOL]
-    static constexpr size_t off_rb = off_u + (size_t)U_N * POOL * 4;       // u16 rowbases [NROW0+NROW1+NROW2]
-    static constexpr size_t off_pos = a16(off_rb + (size_t)(NROW0 + NROW1 + NROW2) * 2);  // u16 [POOL]
-    static constexpr size_t off_list = a16(off_pos + (size_t)POOL * 2);   // u16 [NW][LCAP]
-    static constexpr size_t off_reg = a16(off_list + (size_t)NW * LCAP * 2);  // u8 [RPX][RWY][RWZB]
-    static constexpr size_t off_tail = a16(off_reg + (size_t)RPX * RPLANE);   // u32 cnt0[NW], delta, diag, thr
-    static_assert(off_m % 16 == 0 && off_u % 16 == 0, "shared layout alignment");
-    static size_t smem(uint32_t S1, uint32_t thr_words) { return off_tail + (size_t)(NW + S1 + PD_N + thr_words) * 4; }
+    // pool 0 (box voxels occupied at the start) and pool 2 (Y-sweep results) share storage:
+    // pool 0's contents, x-decisions and x-words are dead once the X sweep is done
+    static constexpr size_t off_c02 = 0;                                   // Vox [C02]: pool 0, then pool 2 contents
+    static constexpr size_t off_c1 = off_c02 + (size_t)C02 * K;            // Vox [CAP1]: pool 1 contents
+    static constexpr size_t off_u02 = off_c1 + (size_t)CAP1 * K;           // u32 [4][C02]: DEC0|DEC2, W01|W23, W02, W03
+    static constexpr size_t off_u1 = off_u02 + (size_t)4 * C02 * 4;        // u32 [3][CAP1]: DEC1, W12, W13
+    static constexpr size_t off_m = a16(off_u1 + (size_t)3 * CAP1 * 4);    // u64 [M_N] row masks
+    static constexpr size_t off_rb = off_m + (size_t)M_N * 8;              // u16 rowbases [NROW0 + NROW1 + NROW2]
+    static constexpr size_t off_pos = a16(off_rb + (size_t)(NROW0 + NROW1 + NROW2) * 2);  // u16 [CAP0]
+    static constexpr size_t off_list = a16(off_pos + (size_t)CAP0 * 2);   // u16 [LCAP] positions of a phase's voxels
+    static constexpr size_t off_reg = a16(off_list + (size_t)LCAP * 2);   // u8 [RPX][RWY][RWZB]
+    static constexpr size_t off_tail = a16(off_reg + (size_t)RPX * RPLANE);  // u32 tops[4], delta[S1], diag, thr
+    static size_t smem(uint32_t S1, uint32_t thr_words) { return off_tail + (size_t)(4 + S1 + PD_N + thr_words) * 4; }
 };
 
-template <int K, int BX, int BY, int NT, int MINB, int CAP>
+// P.sub != 0 (the pass over spilled bricks): item i is plane group i % sub of
+// brick P.items[i / sub], BX planes each, and the item count is
+// *P.n_items_dev * sub.
+template <int K, int BX, int BY, int NT, int MINB, int CAP0, int CAP1, int CAP2>
 __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
-    using B = Brick<K, BX, BY, NT, CAP>;
+    using B = Brick<K, BX, BY, NT, CAP0, CAP1, CAP2>;
     constexpr int NW = B::NW, WY = B::WY, NROW0 = B::NROW0, NROW1 = B::NROW1, NROW2 = B::NROW2;
-    constexpr int RW1 = B::RW1, RW2 = B::RW2, RWY = B::RWY, RWZB = B::RWZB, NCH = B::NCH, LCAP = B::LCAP;
-    constexpr int POOL = B::POOL;
-    constexpr int RB = 4;  // box rows a warp has in flight during the load
+    constexpr int RW1 = B::RW1, RW2 = B::RW2, RWY = B::RWY, RWZB = B::RWZB, NCH = B::NCH, C02 = B::C02;
+    constexpr int LCAP = B::LCAP;
+    constexpr int RB = 8;  // box rows a warp has in flight during the load
     extern __shared__ __align__(16) uint8_t smem[];
-    Vox<K>* cont0 = reinterpret_cast<Vox<K>*>(smem + B::off_c0);
+    Vox<K>* cont0 = reinterpret_cast<Vox<K>*>(smem + B::off_c02);
+    Vox<K>* cont2 = cont0;
     Vox<K>* cont1 = reinterpret_cast<Vox<K>*>(smem + B::off_c1);
-    Vox<K>* cont2 = reinterpret_cast<Vox<K>*>(smem + B::off_c2);
+    uint32_t* U02 = reinterpret_cast<uint32_t*>(smem + B::off_u02);
+    uint32_t* DEC0 = U02;
+    uint32_t* DEC2 = U02;
+    uint32_t* W01 = U02 + C02;
+    uint32_t* W23 = U02 + C02;
+    uint32_t* W02 = U02 + 2 * C02;
+    uint32_t* W03 = U02 + 3 * C02;
+    uint32_t* U1 = reinterpret_cast<uint32_t*>(smem + B::off_u1);
+    uint32_t* DEC1 = U1;
+    uint32_t* W12 = U1 + CAP1;
+    uint32_t* W13 = U1 + 2 * CAP1;
     uint64_t* msk = reinterpret_cast<uint64_t*>(smem + B::off_m);
     uint64_t* OCC0 = msk + B::M_OCC0;  // occupied at the start of the frame (box rows)
     uint64_t* XM = msk + B::M_XM;      // has x-movers down / up (box rows)
@@ -97,35 +114,25 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
     uint64_t* S1m = msk + B::M_S1;     // X-sweep voxels (may end up empty)
     uint64_t* YM = msk + B::M_YM;
     uint64_t* YP = msk + B::M_YP;
-    uint64_t* PB1 = msk + B::M_PB1;    // B(v, 0) evaluated in phase B
+    uint64_t* PB1 = msk + B::M_PB1;    // B(v, 0) evaluated in the X-sweep phase
     uint64_t* S2m = msk + B::M_S2;     // Y-sweep voxels
     uint64_t* ZM = msk + B::M_ZM;
     uint64_t* ZP = msk + B::M_ZP;
-    uint64_t* PB2 = msk + B::M_PB2;    // B(v, 0) evaluated in phase C
-    uint32_t* U = reinterpret_cast<uint32_t*>(smem + B::off_u);
-    uint32_t* DEC0 = U + B::U_DEC0 * POOL;
-    uint32_t* W01 = U + B::U_W01 * POOL;
-    uint32_t* W02 = U + B::U_W02 * POOL;
-    uint32_t* W03 = U + B::U_W03 * POOL;
-    uint32_t* DEC1 = U + B::U_DEC1 * POOL;
-    uint32_t* W12 = U + B::U_W12 * POOL;
-    uint32_t* W13 = U + B::U_W13 * POOL;
-    uint32_t* DEC2 = U + B::U_DEC2 * POOL;
-    uint32_t* W23 = U + B::U_W23 * POOL;
+    uint64_t* PB2 = msk + B::M_PB2;    // B(v, 0) evaluated in the Y-sweep phase
     uint16_t* RB0 = reinterpret_cast<uint16_t*>(smem + B::off_rb);
     uint16_t* RB1 = RB0 + NROW0;
     uint16_t* RB2 = RB1 + NROW1;
     uint16_t* pos0 = reinterpret_cast<uint16_t*>(smem + B::off_pos);
+    uint16_t* L = reinterpret_cast<uint16_t*>(smem + B::off_list);
     uint8_t* reg = smem + B::off_reg;
-    uint32_t* cnt0 = reinterpret_cast<uint32_t*>(smem + B::off_tail);
-    int32_t* s_delta = reinterpret_cast<int32_t*>(cnt0 + NW);
+    uint32_t* top = reinterpret_cast<uint32_t*>(smem + B::off_tail);  // [4] pool 0, pool 1, pool 2, D list
+    int32_t* s_delta = reinterpret_cast<int32_t*>(top + 4);
     uint32_t* s_diag = reinterpret_cast<uint32_t*>(s_delta + P.T.S1);
     uint32_t* s_thr = s_diag + PD_N;
-    __shared__ uint32_t s_item, s_over;
+    __shared__ uint32_t s_item, s_over, s_next;
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const uint32_t lt = (1u << lane) - 1u;
-    uint16_t* L = reinterpret_cast<uint16_t*>(smem + B::off_list) + w * LCAP;
     const uint32_t frame = P.stepbuf[P.parity];
     if (blockIdx.x == 0 && tid == 0) {
         for (uint32_t i = 0; i < P.n_reset; i++) P.reset[i] = 0u;
@@ -142,192 +149,258 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
     for (int i = tid; i < PD_N; i += NT) s_diag[i] = 0u;
     if (tid == 0) s_over = 0xFFFFFFFFu;
     const bool zero_order = P.T.n_zero_order != 0u;
-    const uint32_t n_items = P.n_items_dev ? *P.n_items_dev : P.n_items;
+    const uint32_t sub = P.sub;
+    const uint32_t n_items = P.n_items_dev ? *P.n_items_dev * (sub ? sub : 1u) : P.n_items;
 
-    for (;;) {
-        if (tid == 0) s_item = atomicAdd(P.queue, 1u);
-        __syncthreads();
-        const uint32_t it = s_item;
-        if (it >= n_items) break;
-        const WorkItem wi = P.items[it];
-        const RepDesc rd = P.reps[wi.rep];
-        const int X = (int)rd.X, Y = (int)rd.Y, Z = (int)rd.Z, Zr = (int)rd.Zr;
-        const int x0 = (int)wi.x0, y0 = (int)wi.y0, z0 = (int)wi.z0;
-        const int np = (int)(wi.x1 - wi.x0);  // interior planes inside the lattice
-        const int ny = min(BY, Y - y0);       // interior rows inside the lattice
-        const uint64_t colv = ((1ull << min(32, Z - z0)) - 1ull) << 1;  // interior columns inside
-        const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
-        const bool uniform = (rd.flags & 1u) != 0u;
-        const uint8_t* src = P.src + rd.base * K;
-        uint8_t* dst = P.dst + rd.base * K;
-        const uint8_t* rpad = P.region_pad + rd.rbase;
-        const uint8_t* resv = P.reservoir ? P.reservoir + rd.base : nullptr;
-        const bool all_react = zero_order || resv != nullptr;
-        const uint32_t YZ = (uint32_t)Y * (uint32_t)Z;
-        const uint32_t* quiet = P.T.quiet + (size_t)rd.counts_index * S1;
-        auto lin = [&](int x, int y, int z) -> uint32_t {
-            return ((uint32_t)x * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
-        };
-        // region code of box voxel (p, r, c); p, r, c may step one outside the box
-        auto code = [&](int p, int r, int c) -> uint32_t {
-            if (uniform) {
-                const int x = x0 - 1 + p, y = y0 - 1 + r, z = z0 - 1 + c;
-                return (x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z) ? 1u : 0u;
-            }
-            return reg[((p + 1) * RWY + (r + 1)) * RWZB + c + 1];
-        };
-        auto trow = [&](uint32_t a, uint32_t b) -> const uint32_t* { return thr + ((size_t)a * NC + b) * S1; };
-        // pool index of column c of a row with mask m and rowbase rb (the bit must be set)
-        auto rank = [](uint64_t m, uint32_t rb, int c) -> uint32_t {
-            return rb + (uint32_t)__popcll(m & ((1ull << c) - 1ull));
-        };
-        // per-warp list of the set bits of one row mask per lane (lanes < nrows); returns the
-        // warp's total and sets off = this lane's offset
-        auto build_list = [&](uint64_t m, int row, bool valid, uint32_t& off) -> uint32_t {
-            const uint32_t c = valid ? (uint32_t)__popcll(m) : 0u;
-            uint32_t incl = c;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
-            }
-            off = incl - c;
-            uint64_t bits = valid ? m : 0ull;
-            uint32_t o = off;
-            while (bits) {
-                const int col = __ffsll((long long)bits) - 1;
-                bits &= bits - 1ull;
-                if (o < (uint32_t)LCAP) L[o] = (uint16_t)((row << 6) | col);
-                o++;
-            }
-            return __shfl_sync(0xffffffffu, incl, 31);
-        };
-        auto spill = [&]() {
-            if (tid == 0) {
-                const uint32_t at = atomicAdd(P.n_spill, 1u);
-                P.spill[at] = wi;
-                s_diag[PD_DENSE_BRICKS] += 1u;
-            }
-        };
-
-        // ---------------- L: load the box ----------------
-        if (!uniform) {
-            for (int c = tid; c < NCH; c += NT) {
-                const int rp = c / (RWY * 3), rem = c - rp * (RWY * 3), ry = rem / 3, cz = rem - ry * 3;
-                const int x = x0 - 2 + rp, y = y0 - 2 + ry, zp = z0 + 16 * cz;  // zp: padded column (z + 2)
-                const bool ok = x >= 0 && x < X && y >= 0 && y < Y && zp + 16 <= Zr;
-                const uint8_t* g = ok ? rpad + ((uint64_t)x * (uint64_t)Y + (uint64_t)y) * (uint64_t)Zr + zp : rpad;
-                cp_async<16>(reg + (rp * RWY + ry) * RWZB + 16 * cz, g, ok);
+    // L2 prefetch of item nx's box rows and region rows by the whole CTA, one
+    // 128-byte line per instruction, issued while the current item computes
+    // so that the next item's loads hit L2.
+    auto prefetch_next = [&](uint32_t nx) {
+        if (nx >= n_items) return;
+        const WorkItem nw = P.items[nx];
+        const RepDesc nr = P.reps[nw.rep];
+        const int nX = (int)nr.X, nY = (int)nr.Y, nZ = (int)nr.Z;
+        const int zs = max((int)nw.z0 - 1, 0), ze = min((int)nw.z0 + 33, nZ);
+        constexpr int LPR = (34 * K + 127) / 128 + 1;  // lines a box row can touch
+        const int nslot = NROW0 * LPR + ((nr.flags & 1u) ? 0 : B::RPX * RWY);
+        for (int k = tid; k < nslot; k += NT) {
+            if (k < NROW0 * LPR) {
+                const int i = k / LPR, l = k - i * LPR;
+                const int pp = i / WY, r = i - pp * WY, x = (int)nw.x0 - 1 + pp, y = (int)nw.y0 - 1 + r;
+                if (x < 0 || x >= nX || y < 0 || y >= nY || ze <= zs) continue;
+                const uint64_t vb = nr.base + ((uint64_t)x * (uint64_t)nY + (uint64_t)y) * (uint64_t)nZ;
+                const uint64_t b0 = ((vb + (uint64_t)zs) * K) & ~127ull, b1 = (vb + (uint64_t)ze) * K;
+                const uint64_t at = b0 + 128ull * (uint64_t)l;
+                if (at < b1) prefetch_l2(P.src + at);
+            } else {
+                const int j = k - NROW0 * LPR, rp = j / RWY, ry = j - rp * RWY;
+                const int x = (int)nw.x0 - 2 + rp, y = (int)nw.y0 - 2 + ry;
+                if (x < 0 || x >= nX || y < 0 || y >= nY) continue;
+                prefetch_l2(P.region_pad + nr.rbase + ((uint64_t)x * (uint64_t)nY + (uint64_t)y) * nr.Zr + nw.z0);
             }
         }
-        cp_async_commit();
-        for (int i = tid; i < NROW0; i += NT) { XM[i] = 0ull; XP[i] = 0ull; }
-        for (int i = tid; i < NROW1; i += NT) { YM[i] = 0ull; YP[i] = 0ull; PB1[i] = 0ull; }
-        for (int i = tid; i < NROW2; i += NT) { ZM[i] = 0ull; ZP[i] = 0ull; PB2[i] = 0ull; }
-        {
-            uint32_t wcnt = 0;  // entries of this warp's rows so far (warp-uniform)
+    };
+
+    if (tid == 0) {
+        s_item = atomicAdd(P.queue, 1u);
+        top[0] = 0u; top[1] = 0u; top[2] = 0u; top[3] = 0u;
+    }
+    for (;;) {
+        __syncthreads();  // s_item and the pool tops are set, the previous item's shared state is dead
+        const uint32_t it = s_item;
+        if (it >= n_items) break;
+        uint32_t nxt = 0u, cidx = 0u;
+        if (tid == 0) nxt = atomicAdd(P.queue, 1u);  // the next item, needed only at the end of this one
+        do {
+            WorkItem wi = P.items[sub ? it / sub : it];
+            if (sub) {
+                const uint32_t xs = wi.x0 + (it % sub) * (uint32_t)BX;
+                if (xs >= wi.x1) break;
+                wi.x0 = xs;
+                wi.x1 = min(wi.x1, xs + (uint32_t)BX);
+            }
+            const RepDesc rd = P.reps[wi.rep];
+            cidx = rd.counts_index;
+            const int X = (int)rd.X, Y = (int)rd.Y, Z = (int)rd.Z, Zr = (int)rd.Zr;
+            const int x0 = (int)wi.x0, y0 = (int)wi.y0, z0 = (int)wi.z0;
+            const int np = (int)(wi.x1 - wi.x0);  // interior planes inside the lattice
+            const int ny = min(BY, Y - y0);       // interior rows inside the lattice
+            const uint64_t colv = ((1ull << min(32, Z - z0)) - 1ull) << 1;  // interior columns inside
+            const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
+            const bool uniform = (rd.flags & 1u) != 0u;
+            const uint8_t* src = P.src + rd.base * K;
+            uint8_t* dst = P.dst + rd.base * K;
+            const uint8_t* rpad = P.region_pad + rd.rbase;
+            const uint8_t* resv = P.reservoir ? P.reservoir + rd.base : nullptr;
+            const bool all_react = zero_order || resv != nullptr;
+            const uint32_t YZ = (uint32_t)Y * (uint32_t)Z;
+            const uint32_t* quiet = P.T.quiet + (size_t)rd.counts_index * S1 * P.T.QS;
+            auto lin = [&](int x, int y, int z) -> uint32_t {
+                return ((uint32_t)x * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
+            };
+            // region code of box voxel (p, r, c); p, r, c may step one outside the box
+            auto code = [&](int p, int r, int c) -> uint32_t {
+                if (uniform) {
+                    const int x = x0 - 1 + p, y = y0 - 1 + r, z = z0 - 1 + c;
+                    return (x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z) ? 1u : 0u;
+                }
+                return reg[((p + 1) * RWY + (r + 1)) * RWZB + c + 1];
+            };
+            auto trow = [&](uint32_t a, uint32_t b) -> const uint32_t* { return thr + ((size_t)a * NC + b) * S1; };
+            // pool index of column c of a row with mask m and rowbase rb (the bit must be set)
+            auto rank = [](uint64_t m, uint32_t rb, int c) -> uint32_t {
+                return rb + (uint32_t)__popcll(m & ((1ull << c) - 1ull));
+            };
+            // Appends the set bits of one row mask per lane (row index `row`, only
+            // when `valid`) to the CTA-wide list and pool `t`: the warp reserves a
+            // contiguous range with one shared atomic.  Returns the lane's row base.
+            auto append_rows = [&](uint64_t m, int row, bool valid, int t, uint32_t cap) -> uint32_t {
+                const uint32_t c = valid ? (uint32_t)__popcll(m) : 0u;
+                uint32_t incl = c;
+    #pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += u;
+                }
+                const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                uint32_t base = 0u;
+                if (lane == 0 && total) base = atomicAdd(top + t, total);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                const uint32_t rb = base + incl - c;
+                uint64_t bits = valid ? m : 0ull;
+                uint32_t o = rb;
+                while (bits) {
+                    const int col = __ffsll((long long)bits) - 1;
+                    bits &= bits - 1ull;
+                    if (o < cap) L[o] = (uint16_t)((row << 6) | col);
+                    o++;
+                }
+                return rb;
+            };
+            auto spill = [&]() {
+                if (tid == 0) {
+                    if (P.spill) {
+                        const uint32_t at = atomicAdd(P.n_spill, 1u);
+                        P.spill[at] = wi;
+                        s_diag[PD_DENSE_BRICKS] += 1u;
+                    } else {
+                        s_diag[PD_LOST_BRICKS] += 1u;  // cannot happen with full-capacity pools
+                    }
+                }
+            };
+
+            // ---------------- L: load the box ----------------
+            if (!uniform) {
+                for (int c = tid; c < NCH; c += NT) {
+                    const int rp = c / (RWY * 3), rem = c - rp * (RWY * 3), ry = rem / 3, cz = rem - ry * 3;
+                    const int x = x0 - 2 + rp, y = y0 - 2 + ry, zp = z0 + 16 * cz;  // zp: padded column (z + 2)
+                    const bool ok = x >= 0 && x < X && y >= 0 && y < Y && zp + 16 <= Zr;
+                    const uint8_t* g = ok ? rpad + ((uint64_t)x * (uint64_t)Y + (uint64_t)y) * (uint64_t)Zr + zp : rpad;
+                    cp_async<16>(reg + (rp * RWY + ry) * RWZB + 16 * cz, g, ok);
+                }
+            }
+            cp_async_commit();
+            for (int i = tid; i < NROW0; i += NT) { XM[i] = 0ull; XP[i] = 0ull; }
+            for (int i = tid; i < NROW1; i += NT) { YM[i] = 0ull; YP[i] = 0ull; PB1[i] = 0ull; }
+            for (int i = tid; i < NROW2; i += NT) { ZM[i] = 0ull; ZP[i] = 0ull; PB2[i] = 0ull; }
             for (int ib = w; ib < NROW0; ib += NW * RB) {
-                Vox<K> a[RB], b[RB];
-#pragma unroll
+                // rows ib + u*NW: lane l loads column l; lanes 0..2RB-1 load column 32 + (l & 1) of row l >> 1
+                Vox<K> a[RB], xb = vox_zero<K>();
+    #pragma unroll
                 for (int u = 0; u < RB; u++) {
                     const int i = ib + u * NW;
                     a[u] = vox_zero<K>();
-                    b[u] = vox_zero<K>();
                     if (i < NROW0) {
-                        const int p = i / WY, r = i - p * WY;
-                        const int x = x0 - 1 + p, y = y0 - 1 + r;
-                        if (x >= 0 && x < X && y >= 0 && y < Y) {
-                            const uint8_t* row = src + (uint64_t)lin(x, y, 0) * K;
-                            const int za = z0 - 1 + lane, zb = z0 + 31 + lane;
-                            if (za >= 0 && za < Z) a[u] = ld_vox_g<K>(row + (uint64_t)za * K);
-                            if (lane < 2 && zb < Z) b[u] = ld_vox_g<K>(row + (uint64_t)zb * K);
-                        }
+                        const int p = i / WY, r = i - p * WY, x = x0 - 1 + p, y = y0 - 1 + r, z = z0 - 1 + lane;
+                        if (x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z)
+                            a[u] = ld_vox_g<K>(src + (uint64_t)lin(x, y, z) * K);
                     }
                 }
-#pragma unroll
+                if (lane < 2 * RB) {
+                    const int i = ib + (lane >> 1) * NW;
+                    if (i < NROW0) {
+                        const int p = i / WY, r = i - p * WY, x = x0 - 1 + p, y = y0 - 1 + r, z = z0 + 31 + (lane & 1);
+                        if (x >= 0 && x < X && y >= 0 && y < Y && z < Z) xb = ld_vox_g<K>(src + (uint64_t)lin(x, y, z) * K);
+                    }
+                }
+                const bool ox = !vox_empty<K>(xb);
+                const uint32_t xm = __ballot_sync(0xffffffffu, ox);
+                uint32_t lo[RB], run[RB], tot = 0u;
+    #pragma unroll
+                for (int u = 0; u < RB; u++) {
+                    lo[u] = __ballot_sync(0xffffffffu, !vox_empty<K>(a[u]));
+                    run[u] = tot;
+                    tot += (uint32_t)__popc(lo[u]) + (uint32_t)__popc((xm >> (2 * u)) & 3u);
+                }
+                uint32_t base = 0u;
+                if (lane == 0 && tot) base = atomicAdd(top + 0, tot);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (base + tot > (uint32_t)CAP0) {
+                    if (lane == 0) s_over = it;
+                    continue;
+                }
+                uint32_t xe = 0u;  // pool index of this lane's extra column (lanes < 2 RB)
+    #pragma unroll
                 for (int u = 0; u < RB; u++) {
                     const int i = ib + u * NW;
                     if (i >= NROW0) break;
-                    const bool oa = !vox_empty<K>(a[u]), ob = !vox_empty<K>(b[u]);
-                    const uint32_t lo = __ballot_sync(0xffffffffu, oa), hi = __ballot_sync(0xffffffffu, ob);
-                    const uint32_t cnt = (uint32_t)(__popc(lo) + __popc(hi));
+                    const uint32_t rb = base + run[u], hi = (xm >> (2 * u)) & 3u;
                     if (lane == 0) {
-                        OCC0[i] = (uint64_t)lo | ((uint64_t)hi << 32);
-                        RB0[i] = (uint16_t)(w * CAP + min(wcnt, (uint32_t)CAP));
+                        OCC0[i] = (uint64_t)lo[u] | ((uint64_t)hi << 32);
+                        RB0[i] = (uint16_t)rb;
                     }
-                    if (wcnt + cnt <= (uint32_t)CAP) {
-                        const uint32_t base = (uint32_t)(w * CAP) + wcnt;
-                        if (oa) {
-                            const uint32_t e = base + (uint32_t)__popc(lo & lt);
-                            cont0[e] = a[u];
-                            pos0[e] = (uint16_t)((i << 6) | lane);
-                        }
-                        if (ob) {
-                            const uint32_t e = base + (uint32_t)__popc(lo) + (uint32_t)__popc(hi & lt);
-                            cont0[e] = b[u];
-                            pos0[e] = (uint16_t)((i << 6) | (32 + lane));
-                        }
-                    } else if (lane == 0) {
-                        s_over = it;
+                    if ((lo[u] >> lane) & 1u) {
+                        const uint32_t e = rb + (uint32_t)__popc(lo[u] & lt);
+                        cont0[e] = a[u];
+                        pos0[e] = (uint16_t)((i << 6) | lane);
                     }
-                    wcnt += cnt;
+                    // column 32 follows the row's 32 main columns, column 33 follows column 32
+                    if ((lane >> 1) == u) xe = rb + (uint32_t)__popc(lo[u]) + ((lane & 1) ? (hi & 1u) : 0u);
+                }
+                if (ox) {
+                    const uint32_t e = xe;
+                    const int i = ib + (lane >> 1) * NW;
+                    cont0[e] = xb;
+                    pos0[e] = (uint16_t)((i << 6) | (32 + (lane & 1)));
                 }
             }
-            if (lane == 0) cnt0[w] = min(wcnt, (uint32_t)CAP);
-        }
-        cp_async_wait<0>();
-        __syncthreads();
-        if (s_over == it) {
-            spill();
-            continue;
-        }
-
-        // ---------------- A: x-decisions of the occupied box voxels ----------------
-        {
-            const uint32_t n0 = cnt0[w];
-            for (uint32_t t = lane; t < n0; t += 32) {
-                const uint32_t e = (uint32_t)(w * CAP) + t;
-                const uint32_t ps = pos0[e];
-                const int i = (int)(ps >> 6), c = (int)(ps & 63u), p = i / WY, r = i - p * WY;
-                const uint32_t v = lin(x0 - 1 + p, y0 - 1 + r, z0 - 1 + c);
-                const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
-                W01[e] = b0.y;
-                W02[e] = b0.z;
-                W03[e] = b0.w;
-                const uint32_t rs = code(p, r, c);
-                const uint32_t d = decide_moves<K>(cont0[e], v, frame, 0u, trow(rs, code(p - 1, r, c)),
-                                                   trow(rs, code(p + 1, r, c)), k0, k1, b0.x);
-                DEC0[e] = d;
-                if (d & 0xFFFFu) atomicOr(reinterpret_cast<unsigned long long*>(XM + i), 1ull << c);
-                if (d >> 16) atomicOr(reinterpret_cast<unsigned long long*>(XP + i), 1ull << c);
+            if (tid == 0) s_next = nxt;
+            cp_async_wait<0>();
+            __syncthreads();
+            if (s_over == it) {
+                spill();
+                break;
             }
-        }
-        __syncthreads();
 
-        // ---------------- B: X sweep of the interior planes, y-decisions ----------------
-        {
-            const int j = w + lane * NW;
-            const bool valid = lane < RW1 && j < NROW1;
-            uint64_t s1 = 0ull;
-            if (valid) {
-                const int pi = j / WY + 1, r = j - (pi - 1) * WY;
-                if (pi <= np) {
-                    const int i0 = pi * WY + r;
-                    // own voxel occupied, or +x movers of the plane below / -x movers of the plane above
-                    s1 = OCC0[i0] | XP[i0 - WY] | XM[i0 + WY];
+            // ---------------- A: x-decisions of the occupied box voxels ----------------
+            {
+                const uint32_t n0 = top[0];
+                for (uint32_t e = (uint32_t)tid; e < n0; e += NT) {
+                    const uint32_t ps = pos0[e];
+                    const int i = (int)(ps >> 6), c = (int)(ps & 63u), p = i / WY, r = i - p * WY;
+                    const uint32_t v = lin(x0 - 1 + p, y0 - 1 + r, z0 - 1 + c);
+                    const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
+                    W01[e] = b0.y;
+                    W02[e] = b0.z;
+                    W03[e] = b0.w;
+                    const uint32_t rs = code(p, r, c);
+                    const uint32_t d = decide_moves<K>(cont0[e], v, frame, 0u, trow(rs, code(p - 1, r, c)),
+                                                       trow(rs, code(p + 1, r, c)), k0, k1, b0.x);
+                    DEC0[e] = d;
+                    if (d & 0xFFFFu) atomicOr(reinterpret_cast<unsigned long long*>(XM + i), 1ull << c);
+                    if (d >> 16) atomicOr(reinterpret_cast<unsigned long long*>(XP + i), 1ull << c);
                 }
             }
-            uint32_t off;
-            const uint32_t total = build_list(s1, j, valid, off);
-            if (valid) {
-                S1m[j] = s1;
-                RB1[j] = (uint16_t)(w * CAP + min(off, (uint32_t)CAP));
+            if (sub == 0u) prefetch_next(s_next);
+            __syncthreads();
+
+            // ---------------- B: X sweep of the interior planes, y-decisions ----------------
+            {
+                const int j = w + lane * NW;
+                const bool valid = lane < RW1 && j < NROW1;
+                uint64_t s1 = 0ull;
+                if (valid) {
+                    const int pi = j / WY + 1, r = j - (pi - 1) * WY;
+                    if (pi <= np) {
+                        const int i0 = pi * WY + r;
+                        // own voxel occupied, or +x movers of the plane below / -x movers of the plane above
+                        s1 = OCC0[i0] | XP[i0 - WY] | XM[i0 + WY];
+                    }
+                }
+                const uint32_t rb = append_rows(s1, j, valid, 1, (uint32_t)CAP1);
+                if (valid) {
+                    S1m[j] = s1;
+                    RB1[j] = (uint16_t)min(rb, 65535u);
+                }
             }
-            if (total > (uint32_t)CAP && lane == 0) s_over = it;
-            __syncwarp();
-            const uint32_t n1 = min(total, (uint32_t)CAP);
-            for (uint32_t t = lane; t < n1; t += 32) {
-                const uint32_t ps = L[t];
+            __syncthreads();
+            const uint32_t n1 = top[1];
+            if (n1 > (uint32_t)CAP1) {
+                spill();
+                break;
+            }
+            for (uint32_t e1 = (uint32_t)tid; e1 < n1; e1 += NT) {
+                const uint32_t ps = L[e1];
                 const int jj = (int)(ps >> 6), c = (int)(ps & 63u);
                 const int pi = jj / WY + 1, r = jj - (pi - 1) * WY, i0 = pi * WY + r;
                 const uint64_t bc = 1ull << c;
@@ -348,7 +421,6 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                 }
                 const uint32_t v = lin(x0 - 1 + pi, y0 - 1 + r, z0 - 1 + c);
                 const Vox<K> r1 = combine<K>(own, dme, lo, dlo, hi, dhi, v, v - YZ, v + YZ, frame, 0u);
-                const uint32_t e1 = (uint32_t)(w * CAP) + t;
                 cont1[e1] = r1;
                 uint32_t d = 0u;
                 if (!vox_empty<K>(r1)) {
@@ -363,44 +435,42 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                         atomicOr(reinterpret_cast<unsigned long long*>(PB1 + jj), bc);
                     }
                     const uint32_t rs = code(pi, r, c);
-                    d = decide_moves<K>(r1, v, frame, 1u, trow(rs, code(pi, r - 1, c)), trow(rs, code(pi, r + 1, c)), k0,
-                                        k1, wy);
+                    d = decide_moves<K>(r1, v, frame, 1u, trow(rs, code(pi, r - 1, c)), trow(rs, code(pi, r + 1, c)), k0, k1,
+                                        wy);
                     if (d & 0xFFFFu) atomicOr(reinterpret_cast<unsigned long long*>(YM + jj), bc);
                     if (d >> 16) atomicOr(reinterpret_cast<unsigned long long*>(YP + jj), bc);
                 }
                 DEC1[e1] = d;
             }
-        }
-        __syncthreads();
-        if (s_over == it) {
-            spill();
-            continue;
-        }
+            __syncthreads();
 
-        // ---------------- C: Y sweep of the interior rows, z-decisions ----------------
-        {
-            const int j2 = w + lane * NW;
-            const bool valid = lane < RW2 && j2 < NROW2;
-            uint64_t s2 = 0ull;
-            if (valid) {
-                const int pi = j2 / BY + 1, r = j2 - (pi - 1) * BY + 1;
-                if (pi <= np && r <= ny) {
-                    const int j1 = (pi - 1) * WY + r;
-                    // own voxel, +y movers of the row below, -y movers of the row above
-                    s2 = S1m[j1] | YP[j1 - 1] | YM[j1 + 1];
+            // ---------------- C: Y sweep of the interior rows, z-decisions ----------------
+            {
+                const int j2 = w + lane * NW;
+                const bool valid = lane < RW2 && j2 < NROW2;
+                uint64_t s2 = 0ull;
+                if (valid) {
+                    const int pi = j2 / BY + 1, r = j2 - (pi - 1) * BY + 1;
+                    if (pi <= np && r <= ny) {
+                        const int j1 = (pi - 1) * WY + r;
+                        // own voxel, +y movers of the row below, -y movers of the row above
+                        s2 = S1m[j1] | YP[j1 - 1] | YM[j1 + 1];
+                    }
+                }
+                const uint32_t rb = append_rows(s2, j2, valid, 2, (uint32_t)CAP2);
+                if (valid) {
+                    S2m[j2] = s2;
+                    RB2[j2] = (uint16_t)min(rb, 65535u);
                 }
             }
-            uint32_t off;
-            const uint32_t total = build_list(s2, j2, valid, off);
-            if (valid) {
-                S2m[j2] = s2;
-                RB2[j2] = (uint16_t)(w * CAP + min(off, (uint32_t)CAP));
+            __syncthreads();
+            const uint32_t n2 = top[2];
+            if (n2 > (uint32_t)CAP2) {
+                spill();
+                break;
             }
-            if (total > (uint32_t)CAP && lane == 0) s_over = it;
-            __syncwarp();
-            const uint32_t n2 = min(total, (uint32_t)CAP);
-            for (uint32_t t = lane; t < n2; t += 32) {
-                const uint32_t ps = L[t];
+            for (uint32_t e2 = (uint32_t)tid; e2 < n2; e2 += NT) {
+                const uint32_t ps = L[e2];
                 const int jj = (int)(ps >> 6), c = (int)(ps & 63u);
                 const int pi = jj / BY + 1, r = jj - (pi - 1) * BY + 1, j1 = (pi - 1) * WY + r;
                 const uint64_t bc = 1ull << c;
@@ -421,8 +491,6 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                 }
                 const uint32_t v = lin(x0 - 1 + pi, y0 - 1 + r, z0 - 1 + c);
                 const Vox<K> r2 = combine<K>(own, dme, lo, dlo, hi, dhi, v, v - (uint32_t)Z, v + (uint32_t)Z, frame, 1u);
-                const uint32_t e2 = (uint32_t)(w * CAP) + t;
-                cont2[e2] = r2;
                 uint32_t d = 0u;
                 if (!vox_empty<K>(r2)) {
                     uint32_t wz;
@@ -439,86 +507,88 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                         atomicOr(reinterpret_cast<unsigned long long*>(PB2 + jj), bc);
                     }
                     const uint32_t rs = code(pi, r, c);
-                    d = decide_moves<K>(r2, v, frame, 2u, trow(rs, code(pi, r, c - 1)), trow(rs, code(pi, r, c + 1)), k0,
-                                        k1, wz);
+                    d = decide_moves<K>(r2, v, frame, 2u, trow(rs, code(pi, r, c - 1)), trow(rs, code(pi, r, c + 1)), k0, k1,
+                                        wz);
                     if (d & 0xFFFFu) atomicOr(reinterpret_cast<unsigned long long*>(ZM + jj), bc);
                     if (d >> 16) atomicOr(reinterpret_cast<unsigned long long*>(ZP + jj), bc);
                 }
+                cont2[e2] = r2;
                 DEC2[e2] = d;
             }
-        }
-        __syncthreads();
-        if (s_over == it) {
-            spill();
-            continue;
-        }
+            __syncthreads();
 
-        // ---------------- D: Z sweep, reactions, store ----------------
-        {
-            const int j2 = w + lane * NW;
-            const bool valid = lane < RW2 && j2 < NROW2;
-            bool row_in = false;
-            uint64_t s3 = 0ull;
-            if (valid) {
-                const int pi = j2 / BY + 1, r = j2 - (pi - 1) * BY + 1;
-                if (pi <= np && r <= ny) {
-                    row_in = true;
-                    // own voxel, +z movers of the column before, -z movers of the column after
-                    s3 = all_react ? colv : ((S2m[j2] | (ZP[j2] << 1) | (ZM[j2] >> 1)) & colv);
+            // ---------------- D: Z sweep, reactions, store ----------------
+            {
+                const int j2 = w + lane * NW;
+                const bool valid = lane < RW2 && j2 < NROW2;
+                bool row_in = false;
+                uint64_t s3 = 0ull;
+                if (valid) {
+                    const int pi = j2 / BY + 1, r = j2 - (pi - 1) * BY + 1;
+                    if (pi <= np && r <= ny) {
+                        row_in = true;
+                        // own voxel, +z movers of the column before, -z movers of the column after
+                        s3 = all_react ? colv : ((S2m[j2] | (ZP[j2] << 1) | (ZM[j2] >> 1)) & colv);
+                    }
+                }
+                // interior voxels that nothing reaches end the frame empty: coalesced zero stores
+                for (int k = 0; k < RW2; k++) {
+                    const int rk = __shfl_sync(0xffffffffu, (int)row_in, k);
+                    if (!rk) continue;
+                    const uint64_t sk = __shfl_sync(0xffffffffu, s3, k);
+                    const int jk = w + k * NW, pi = jk / BY + 1, r = jk - (pi - 1) * BY + 1, c = lane + 1;
+                    if (((colv >> c) & 1ull) && !((sk >> c) & 1ull))
+                        st_vox_g<K>(dst + (uint64_t)lin(x0 - 1 + pi, y0 - 1 + r, z0 + lane) * K, vox_zero<K>());
+                }
+                append_rows(s3, j2, valid && row_in, 3, (uint32_t)LCAP);
+            }
+            __syncthreads();
+            {
+                const uint32_t nd = top[3];
+                for (uint32_t t = (uint32_t)tid; t < nd; t += NT) {
+                    const uint32_t ps = L[t];
+                    const int jj = (int)(ps >> 6), c = (int)(ps & 63u);
+                    const int pi = jj / BY + 1, r = jj - (pi - 1) * BY + 1, j1 = (pi - 1) * WY + r;
+                    const uint64_t o2 = S2m[jj];
+                    const uint32_t rb = RB2[jj];
+                    Vox<K> own = vox_zero<K>(), lo = vox_zero<K>(), hi = vox_zero<K>();
+                    uint32_t dme = 0u, dlo = 0u, dhi = 0u;
+                    int e2 = -1;
+                    if ((o2 >> c) & 1ull) { e2 = (int)rank(o2, rb, c); own = cont2[e2]; dme = DEC2[e2]; }
+                    if ((o2 >> (c - 1)) & 1ull) { const uint32_t e = rank(o2, rb, c - 1); lo = cont2[e]; dlo = DEC2[e]; }
+                    if ((o2 >> (c + 1)) & 1ull) { const uint32_t e = rank(o2, rb, c + 1); hi = cont2[e]; dhi = DEC2[e]; }
+                    const uint32_t v = lin(x0 - 1 + pi, y0 - 1 + r, z0 - 1 + c);
+                    Vox<K> r3 = combine<K>(own, dme, lo, dlo, hi, dhi, v, v - 1u, v + 1u, frame, 2u);
+                    const uint32_t rv = resv ? (uint32_t)resv[v] : 0u;
+                    if (rv != 0u || zero_order || !vox_empty<K>(r3)) {
+                        uint32_t w3;
+                        const uint64_t bc = 1ull << c;
+                        const int i0 = pi * WY + r;
+                        const uint64_t o0 = OCC0[i0];
+                        if (o0 & bc) w3 = W03[rank(o0, RB0[i0], c)];
+                        else if (PB1[j1] & bc) w3 = W13[rank(S1m[j1], RB1[j1], c)];
+                        else if (PB2[jj] & bc) w3 = W23[e2];
+                        else w3 = d_philox(v, frame, 0u, 0u, k0, k1).w;
+                        const bool calm = rv == 0u && !zero_order && calm_voxel<K>(r3, w3, quiet, P.T.QS);
+                        if (!calm)
+                            react_voxel<K>(r3, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, P.T, s_delta, s_diag,
+                                           w3);
+                    }
+                    st_vox_g<K>(dst + (uint64_t)v * K, r3);
                 }
             }
-            // interior voxels that nothing reaches end the frame empty: coalesced zero stores
-            for (int k = 0; k < RW2; k++) {
-                const int rk = __shfl_sync(0xffffffffu, (int)row_in, k);
-                if (!rk) continue;
-                const uint64_t sk = __shfl_sync(0xffffffffu, s3, k);
-                const int jk = w + k * NW, pi = jk / BY + 1, r = jk - (pi - 1) * BY + 1, c = lane + 1;
-                if (((colv >> c) & 1ull) && !((sk >> c) & 1ull))
-                    st_vox_g<K>(dst + (uint64_t)lin(x0 - 1 + pi, y0 - 1 + r, z0 + lane) * K, vox_zero<K>());
-            }
-            uint32_t off;
-            const uint32_t nd = build_list(s3, j2, valid && row_in, off);
-            __syncwarp();
-            for (uint32_t t = lane; t < nd; t += 32) {
-                const uint32_t ps = L[t];
-                const int jj = (int)(ps >> 6), c = (int)(ps & 63u);
-                const int pi = jj / BY + 1, r = jj - (pi - 1) * BY + 1, j1 = (pi - 1) * WY + r;
-                const uint64_t o2 = S2m[jj];
-                const uint32_t rb = RB2[jj];
-                Vox<K> own = vox_zero<K>(), lo = vox_zero<K>(), hi = vox_zero<K>();
-                uint32_t dme = 0u, dlo = 0u, dhi = 0u;
-                int e2 = -1;
-                if ((o2 >> c) & 1ull) { e2 = (int)rank(o2, rb, c); own = cont2[e2]; dme = DEC2[e2]; }
-                if ((o2 >> (c - 1)) & 1ull) { const uint32_t e = rank(o2, rb, c - 1); lo = cont2[e]; dlo = DEC2[e]; }
-                if ((o2 >> (c + 1)) & 1ull) { const uint32_t e = rank(o2, rb, c + 1); hi = cont2[e]; dhi = DEC2[e]; }
-                const uint32_t v = lin(x0 - 1 + pi, y0 - 1 + r, z0 - 1 + c);
-                Vox<K> r3 = combine<K>(own, dme, lo, dlo, hi, dhi, v, v - 1u, v + 1u, frame, 2u);
-                const uint32_t rv = resv ? (uint32_t)resv[v] : 0u;
-                if (rv != 0u || zero_order || !vox_empty<K>(r3)) {
-                    uint32_t w3;
-                    const uint64_t bc = 1ull << c;
-                    const int i0 = pi * WY + r;
-                    const uint64_t o0 = OCC0[i0];
-                    if (o0 & bc) w3 = W03[rank(o0, RB0[i0], c)];
-                    else if (PB1[j1] & bc) w3 = W13[rank(S1m[j1], RB1[j1], c)];
-                    else if (PB2[jj] & bc) w3 = W23[e2];
-                    else w3 = d_philox(v, frame, 0u, 0u, k0, k1).w;
-                    const bool calm = rv == 0u && !zero_order && vox_n<K>(r3) == 1u &&
-                                      (w3 >> 8) + 1u <= quiet[vox_get<K>(r3, 0)];
-                    if (!calm)
-                        react_voxel<K>(r3, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, P.T, s_delta, s_diag,
-                                       w3);
-                }
-                st_vox_g<K>(dst + (uint64_t)v * K, r3);
-            }
-        }
+        } while (0);
         __syncthreads();
         for (uint32_t s = tid; s < S1; s += NT) {
             const int32_t dlt = s_delta[s];
             if (dlt) {
-                atomicAdd(P.counts + (size_t)rd.counts_index * S1 + s, (unsigned long long)(long long)dlt);
+                atomicAdd(P.counts + (size_t)cidx * S1 + s, (unsigned long long)(long long)dlt);
                 s_delta[s] = 0;
             }
+        }
+        if (tid == 0) {
+            s_item = nxt;
+            top[0] = 0u; top[1] = 0u; top[2] = 0u; top[3] = 0u;
         }
     }
     __syncthreads();

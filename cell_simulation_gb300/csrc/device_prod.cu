@@ -42,15 +42,17 @@ typedef void (*ProdKernelFn)(ProdParams);
 
 // A compiled step configuration.  kind 0: the tile pipeline alone over
 // (TY x TZ tile, x-segment) items.  kind 1: the brick pass over BX x TY x 32
-// bricks, followed by the tile pipeline `spill` (same K and TY, TZ = 32) over
-// the bricks the brick pass handed over.
+// bricks; when its pools can overflow, a second brick pass `spill` with
+// pools as large as its box finishes the spilled bricks in `sub` groups of
+// its own BX planes.
 enum { KIND_TILE = 0, KIND_BRICK = 1 };
 
 struct KernelCfg {
     int kind, K, TY, TZ, NT, BX;
     ProdKernelFn fn;
     size_t (*smem)(uint32_t S1, uint32_t thr_words);
-    int spill;  // kind 1: index of the tile configuration for spilled bricks
+    int spill;     // kind 1 with bounded pools: index of the configuration for spilled bricks, else -1
+    uint32_t sub;  // plane groups per spilled brick in that configuration
 };
 
 template <int K, int TY, int TZ>
@@ -58,21 +60,31 @@ static size_t tile_smem(uint32_t S1, uint32_t) { return Tile<K, TY, TZ>::smem(S1
 
 template <int K, int TY, int TZ, int NT, int MINB>
 static KernelCfg tile_cfg() {
-    return KernelCfg{KIND_TILE, K, TY, TZ, NT, 0, prod_step_kernel<K, TY, TZ, NT, MINB>, &tile_smem<K, TY, TZ>, -1};
+    return KernelCfg{KIND_TILE, K, TY, TZ, NT, 0, prod_step_kernel<K, TY, TZ, NT, MINB>, &tile_smem<K, TY, TZ>, -1, 0};
 }
 
-template <int K, int BX, int BY, int NT, int MINB, int CAP>
-static KernelCfg brick_cfg(int spill) {
-    return KernelCfg{KIND_BRICK, K, BY, 32, NT, BX, brick_step_kernel<K, BX, BY, NT, MINB, CAP>,
-                     &Brick<K, BX, BY, NT, CAP>::smem, spill};
+template <int K, int BX, int BY, int NT, int MINB, int CAP0, int CAP1, int CAP2>
+static KernelCfg brick_cfg(int spill, uint32_t sub) {
+    using B = Brick<K, BX, BY, NT, CAP0, CAP1, CAP2>;
+    return KernelCfg{KIND_BRICK, K, BY, 32, NT, BX, brick_step_kernel<K, BX, BY, NT, MINB, CAP0, CAP1, CAP2>,
+                     &B::smem, B::DENSE ? -1 : spill, sub};
+}
+
+// full-capacity pools for a brick of BX x BY x 32: never spills
+template <int K, int BX, int BY, int NT, int MINB>
+static KernelCfg dense_brick_cfg() {
+    constexpr int N0 = (BX + 2) * (BY + 2) * 34, N1 = BX * (BY + 2) * 34, N2 = BX * BY * 34;
+    return brick_cfg<K, BX, BY, NT, MINB, N0, N1, N2>(-1, 0);
 }
 
 static const std::vector<KernelCfg>& all_cfgs() {
     static const std::vector<KernelCfg> v = {
-        tile_cfg<16, 8, 32, 256, 3>(),          tile_cfg<16, 4, 64, 256, 3>(), tile_cfg<16, 16, 32, 256, 1>(),
-        tile_cfg<16, 8, 64, 256, 1>(),          tile_cfg<8, 8, 32, 256, 3>(),  tile_cfg<8, 4, 64, 256, 3>(),
-        tile_cfg<8, 16, 32, 256, 2>(),          tile_cfg<8, 8, 64, 256, 2>(),
-        brick_cfg<16, 8, 8, 256, 3, 64>(0),     brick_cfg<8, 8, 8, 256, 3, 64>(4),
+        tile_cfg<16, 8, 32, 256, 3>(),  tile_cfg<16, 4, 64, 256, 3>(), tile_cfg<16, 16, 32, 256, 1>(),
+        tile_cfg<16, 8, 64, 256, 1>(),  tile_cfg<8, 8, 32, 256, 3>(),  tile_cfg<8, 4, 64, 256, 3>(),
+        tile_cfg<8, 16, 32, 256, 2>(),  tile_cfg<8, 8, 64, 256, 2>(),
+        // sparse bricks (8 planes) whose crowded bricks go to the dense 2-plane pass of the same K
+        brick_cfg<16, 8, 8, 256, 3, 768, 768, 768>(10, 4), brick_cfg<8, 8, 8, 256, 3, 768, 768, 768>(11, 4),
+        dense_brick_cfg<16, 2, 8, 256, 3>(), dense_brick_cfg<8, 2, 8, 256, 3>(),
     };
     return v;
 }
@@ -251,25 +263,51 @@ static void build_one_table(DeviceProd* d) {
     d->one.alloc(one.size());
     CS_CUDA(cudaMemcpy(d->one.p, one.data(), one.size() * 4, cudaMemcpyHostToDevice));
     d->T.one = d->one.p;
-    // Quiet thresholds.  A voxel holding one particle of species q (no
-    // reservoir, no zero-order reaction) has a0 = one[q][0], and its first
-    // event is rejected when dt = -logf(u1) / a0 > tau, u1 = m * 2^-24 with
-    // m = (B(v,0)[3] >> 8) + 1.  For m <= quiet[q] that holds for certain:
-    // u1 <= exp(-a0 tau (1 + 2^-12)) gives -log(u1) >= a0 tau (1 + 2^-12),
-    // and the device logf (within 3 ulp) and the correctly rounded division
-    // lose far less than the 2^-12 margin.  Larger m take the exact path.
-    std::vector<uint32_t> quiet((size_t)d->n_rep * d->S1, 0u);
+    // Quiet thresholds.  A voxel without reservoir or zero-order reaction
+    // holding one particle of species p (q = 0) or one of p and one of q has
+    // total propensity a0, and its first event is rejected when
+    // dt = -logf(u1) / a0 > tau, u1 = m * 2^-24 with m = (B(v,0)[3] >> 8) + 1.
+    // For m <= quiet[p][q] that holds for certain: u1 <= exp(-a0 tau (1 + 2^-12))
+    // gives -log(u1) >= a0 tau (1 + 2^-12), while the device's binary32 sum of
+    // a0 (at most 128 terms), its logf (within 3 ulp) and the correctly
+    // rounded division together lose far less than the 2^-12 margin.  Larger m
+    // take the exact path.  Two-particle entries are tabulated when the table
+    // stays small.
+    const uint32_t S1 = d->S1;
+    const uint32_t QS = (uint64_t)d->n_rep * S1 * S1 <= (1ull << 22) ? S1 : 1u;
+    std::vector<uint32_t> quiet((size_t)d->n_rep * S1 * QS, 0u);
     const double tau = (double)d->T.tau;
-    for (size_t i = 0; i < quiet.size(); i++) {
-        const float a0 = one[i * 3];
-        uint32_t m = 1u << 24;  // no reaction can fire: every draw is quiet
-        if (a0 > 0.0f) {
-            const double x = (double)a0 * tau * (1.0 + std::ldexp(1.0, -12));
-            const double ub = std::exp(-x) * 16777216.0;
-            m = ub >= 16777215.0 ? 16777215u : (uint32_t)std::floor(ub);
+    auto threshold = [&](double a0) -> uint32_t {
+        if (!(a0 > 0.0)) return 1u << 24;  // no reaction can fire: every draw is quiet
+        const double ub = std::exp(-a0 * tau * (1.0 + std::ldexp(1.0, -12))) * 16777216.0;
+        return ub >= 16777215.0 ? 16777215u : (uint32_t)std::floor(ub);
+    };
+    std::vector<uint32_t> cnt(S1, 0u);
+    for (uint32_t ri = 0; ri < d->n_rep; ri++) {
+        const double mult = (double)d->h_reps[ri].rate_mult;
+        for (uint32_t p = 1; p < S1; p++) {
+            quiet[((size_t)ri * S1 + p) * QS] = threshold((double)one[((size_t)ri * S1 + p) * 3]);
+            for (uint32_t q = 1; q < QS; q++) {
+                std::fill(cnt.begin(), cnt.end(), 0u);
+                cnt[p]++;
+                cnt[q]++;
+                double a0 = 0.0;
+                for (uint32_t r = 0; r < d->R; r++) {
+                    double ff = 1.0;
+                    for (int j = 0; j < 3; j++) {
+                        const uint32_t s = d->h_rre[3 * r + j];
+                        if (!s) continue;
+                        uint32_t mm = 0;
+                        for (int i = 0; i < j; i++) mm += d->h_rre[3 * r + i] == s;
+                        ff = cnt[s] <= mm ? 0.0 : ff * (double)(cnt[s] - mm);
+                    }
+                    a0 += (double)d->h_rate[r] * mult * ff;
+                }
+                quiet[((size_t)ri * S1 + p) * QS + q] = threshold(a0);
+            }
         }
-        quiet[i] = m;
     }
+    d->T.QS = QS;
     d->quiet.alloc(quiet.size());
     CS_CUDA(cudaMemcpy(d->quiet.p, quiet.data(), quiet.size() * 4, cudaMemcpyHostToDevice));
     d->T.quiet = d->quiet.p;
@@ -346,7 +384,7 @@ static void set_attrs(const DeviceProd* d, const KernelCfg& cfg) {
 static void set_cfg(DeviceProd* d, int idx) {
     const KernelCfg& cfg = all_cfgs()[idx];
     set_attrs(d, cfg);
-    if (cfg.kind == KIND_BRICK) set_attrs(d, all_cfgs()[cfg.spill]);
+    if (cfg.spill >= 0) set_attrs(d, all_cfgs()[cfg.spill]);
     d->cfg_index = idx;
     build_items(d);
     if (d->graph) {
@@ -399,27 +437,28 @@ static void launch_frame(DeviceProd* d, int parity, int rep) {
     P.advance = 1u;
     P.thr_smem = thr_words(d) != 0u;
     const uint32_t n = P.n_items;
-    if (cfg.kind == KIND_BRICK) {
+    if (cfg.spill >= 0) {
         P.spill = d->spill.p + off;
         P.n_spill = ctr + 1;
     }
     cfg.fn<<<grid_for(d, cfg, n), cfg.NT, cfg_smem(d, cfg), d->stream>>>(P);
     CS_LAUNCH_CHECK();
-    if (cfg.kind == KIND_BRICK) {
-        // the tile pipeline over the spilled bricks (usually none: its CTAs take no item and exit)
+    if (cfg.spill >= 0) {
+        // the full-capacity brick pass over the spilled bricks, cfg.sub plane groups each (usually
+        // none: its CTAs take no item and exit)
         const KernelCfg& sc = all_cfgs()[cfg.spill];
         ProdParams Q = P;
         Q.items = d->spill.p + off;
         Q.n_items = 0;
         Q.n_items_dev = ctr + 1;
+        Q.sub = cfg.sub;
         Q.queue = ctr + 2;
         Q.reset = nullptr;
         Q.n_reset = 0;
         Q.advance = 0u;
-        Q.thr_smem = 0u;
         Q.spill = nullptr;
         Q.n_spill = nullptr;
-        sc.fn<<<grid_for(d, sc, n), sc.NT, cfg_smem(d, sc), d->stream>>>(Q);
+        sc.fn<<<grid_for(d, sc, n * cfg.sub), sc.NT, cfg_smem(d, sc), d->stream>>>(Q);
         CS_LAUNCH_CHECK();
     }
 }

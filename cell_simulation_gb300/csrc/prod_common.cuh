@@ -39,7 +39,7 @@
 
 namespace cellsim {
 
-enum { PD_EVENTS = 0, PD_REJECT_CAP = 1, PD_EVENT_CAP = 2, PD_FP64_SEL = 3, PD_DENSE_BRICKS = 4, PD_N = 8 };
+enum { PD_EVENTS = 0, PD_REJECT_CAP = 1, PD_EVENT_CAP = 2, PD_FP64_SEL = 3, PD_DENSE_BRICKS = 4, PD_LOST_BRICKS = 5, PD_N = 8 };
 
 struct RepDesc {
     uint64_t base;   // first voxel of this replicate in the packed slot/reservoir arrays
@@ -74,10 +74,12 @@ struct ProdTables {
     unsigned long long zmask[2];      // reactions without reactants
     const float* one;                 // [n_rep][S1][3]: a0, max a, min non-zero a for a voxel holding
                                       // exactly one particle of species q (q = 0: an empty voxel)
-    const uint32_t* quiet;            // [n_rep][S1]: a voxel holding one particle of species q and no
-                                      // reservoir has no reaction event in the frame when
-                                      // (B(v,0)[3] >> 8) + 1 <= quiet[q]
+    const uint32_t* quiet;            // [n_rep][S1][QS]: a voxel without reservoir holding one particle of
+                                      // species p (q = 0), or one of p and one of q, has no reaction event
+                                      // in the frame when (B(v,0)[3] >> 8) + 1 <= quiet[p][q]
+    uint32_t QS;                      // S1 when two-particle entries are tabulated, else 1
 };
+
 
 // K slot bytes held in 64-bit words, byte s = slot s.
 template <int K>
@@ -143,6 +145,16 @@ __device__ __forceinline__ uint32_t vox_count(const Vox<K>& c, uint32_t q) {
     for (int i = 0; i < K / 8; i++)
         n += __popc(__vcmpeq4((uint32_t)c.w[i], rep)) + __popc(__vcmpeq4((uint32_t)(c.w[i] >> 32), rep));
     return n >> 3;
+}
+
+// True when the first reaction event of a voxel with content c (no
+// reservoir, no zero-order reaction) certainly falls beyond tau.
+template <int K>
+__device__ __forceinline__ bool calm_voxel(const Vox<K>& c, uint32_t w3, const uint32_t* quiet_rep, uint32_t QS) {
+    const uint32_t n = vox_n<K>(c);
+    if (n == 0u || n > 2u || (n == 2u && QS == 1u)) return false;
+    const uint32_t p = vox_get<K>(c, 0), q = n == 2u ? vox_get<K>(c, 1) : 0u;
+    return (w3 >> 8) + 1u <= quiet_rep[p * QS + q];
 }
 
 // Keep the c lowest set bits of m.

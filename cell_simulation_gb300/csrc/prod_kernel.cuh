@@ -42,8 +42,9 @@ struct ProdParams {
     uint32_t thr_smem;            // nonzero: the threshold table is staged in shared memory
     uint32_t parity;
     uint32_t* stepbuf;            // [2] frame numbers
-    WorkItem* spill;              // brick pass: bricks handed over to the tile pipeline
+    WorkItem* spill;              // brick pass: crowded bricks handed to the second pass
     uint32_t* n_spill;
+    uint32_t sub;                 // brick pass over spilled bricks: plane groups per brick
     const uint8_t* src;
     uint8_t* dst;
     const uint8_t* region_pad;   // padded region codes, see RepDesc::rbase
@@ -81,6 +82,8 @@ __device__ __forceinline__ void cp_async(void* sdst, const void* gsrc, bool vali
     else
         asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(smem_u32(sdst)), "l"(gsrc), "r"(n) : "memory");
 }
+// Prefetch of the L2 line holding p.
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p)); }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
@@ -350,8 +353,9 @@ __global__ void __launch_bounds__(NT, MINB) prod_step_kernel(ProdParams P) {
                         uint32_t rv = resv ? (uint32_t)resv[v] : 0u;
                         if (rv != 0u || always_react || !vox_empty<K>(r)) {
                             const uint32_t w3 = d_philox(v, frame, 0u, 0u, k0, k1).w;
-                            const bool quiet = rv == 0u && !always_react && vox_n<K>(r) == 1u &&
-                                               (w3 >> 8) + 1u <= P.T.quiet[(size_t)rd.counts_index * P.T.S1 + vox_get<K>(r, 0)];
+                            const bool quiet =
+                                rv == 0u && !always_react &&
+                                calm_voxel<K>(r, w3, P.T.quiet + (size_t)rd.counts_index * P.T.S1 * P.T.QS, P.T.QS);
                             if (!quiet)
                                 react_voxel<K>(r, rv, v, frame, k0, k1, mult, rd.counts_index, P.T, s_delta, s_diag, w3);
                         }

@@ -79,7 +79,8 @@ def brick_tilings(K):
 @pytest.mark.parametrize("K", [8, 16])
 def test_brick_pass_with_spilled_bricks_matches_oracle(orc, K):
     """Sparse bricks run in the brick pass, the crowded cube's bricks overflow
-    its pools and are finished by the tile pipeline: the frame is the same."""
+    its pools and are finished by the full-capacity second pass: the frame is
+    the same."""
     mk = lambda: patchy_model(K=K)
     want_s, want_c, want_d = oracle_prod(orc, mk(), 24, seed=77)
     for ti in brick_tilings(K):
@@ -87,9 +88,13 @@ def test_brick_pass_with_spilled_bricks_matches_oracle(orc, K):
         assert np.array_equal(got_s, want_s), (ti, np.flatnonzero(got_s != want_s)[:8])
         assert np.array_equal(got_c, want_c), ti
         assert np.array_equal(got_d[:4], want_d[:4]), (ti, got_d, want_d)
-        spilled = int(got_d[4])
-        n_bricks = 3 * 3 * 3  # (19/8, 21/8, 70/32) rounded up
-        assert 0 < spilled < 24 * n_bricks, spilled  # some bricks spill, most do not
+        spilled, lost = int(got_d[4]), int(got_d[5])
+        assert lost == 0
+        if tiling_kinds()[ti][1] == 2:
+            assert spilled == 0  # full-capacity pools
+        else:
+            n_bricks = 3 * 3 * 3  # (19/8, 21/8, 70/32) rounded up
+            assert 0 < spilled < 24 * n_bricks, spilled  # some bricks spill, most do not
 
 
 def test_sparse_lattice_never_spills():
