@@ -78,8 +78,11 @@ struct Brick {
     static constexpr size_t off_pos = a16(off_rb + (size_t)(NROW0 + NROW1 + NROW2) * 2);  // u16 [CAP0]
     static constexpr size_t off_list = a16(off_pos + (size_t)CAP0 * 2);   // u16 [LCAP] positions of a phase's voxels
     static constexpr size_t off_reg = a16(off_list + (size_t)LCAP * 2);   // u8 [RPX][RWY][RWZB]
-    static constexpr size_t off_tail = a16(off_reg + (size_t)RPX * RPLANE);  // u32 tops[4], delta[S1], diag, thr
-    static size_t smem(uint32_t S1, uint32_t thr_words) { return off_tail + (size_t)(4 + S1 + PD_N + thr_words) * 4; }
+    // u32 tops[4], old and new occupancy words of the interior rows [2][NROW2], delta[S1], diag, thr
+    static constexpr size_t off_tail = a16(off_reg + (size_t)RPX * RPLANE);
+    static size_t smem(uint32_t S1, uint32_t thr_words) {
+        return off_tail + (size_t)(4 + 2 * NROW2 + S1 + PD_N + thr_words) * 4;
+    }
 };
 
 // P.sub != 0 (the pass over spilled bricks): item i is plane group i % sub of
@@ -91,7 +94,6 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
     constexpr int NW = B::NW, WY = B::WY, NROW0 = B::NROW0, NROW1 = B::NROW1, NROW2 = B::NROW2;
     constexpr int RW1 = B::RW1, RW2 = B::RW2, RWY = B::RWY, RWZB = B::RWZB, NCH = B::NCH, C02 = B::C02;
     constexpr int LCAP = B::LCAP;
-    constexpr int RB = 8;  // box rows a warp has in flight during the load
     extern __shared__ __align__(16) uint8_t smem[];
     Vox<K>* cont0 = reinterpret_cast<Vox<K>*>(smem + B::off_c02);
     Vox<K>* cont2 = cont0;
@@ -126,10 +128,12 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
     uint16_t* L = reinterpret_cast<uint16_t*>(smem + B::off_list);
     uint8_t* reg = smem + B::off_reg;
     uint32_t* top = reinterpret_cast<uint32_t*>(smem + B::off_tail);  // [4] pool 0, pool 1, pool 2, D list
-    int32_t* s_delta = reinterpret_cast<int32_t*>(top + 4);
+    uint32_t* OLDW = top + 4;       // destination occupancy word of each interior row before the frame
+    uint32_t* NEWW = OLDW + NROW2;  // and after it
+    int32_t* s_delta = reinterpret_cast<int32_t*>(NEWW + NROW2);
     uint32_t* s_diag = reinterpret_cast<uint32_t*>(s_delta + P.T.S1);
     uint32_t* s_thr = s_diag + PD_N;
-    __shared__ uint32_t s_item, s_over, s_next;
+    __shared__ uint32_t s_item, s_next;
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const uint32_t lt = (1u << lane) - 1u;
@@ -147,33 +151,26 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
     }
     for (uint32_t s = tid; s < S1; s += NT) s_delta[s] = 0;
     for (int i = tid; i < PD_N; i += NT) s_diag[i] = 0u;
-    if (tid == 0) s_over = 0xFFFFFFFFu;
     const bool zero_order = P.T.n_zero_order != 0u;
     const uint32_t sub = P.sub;
     const uint32_t n_items = P.n_items_dev ? *P.n_items_dev * (sub ? sub : 1u) : P.n_items;
 
-    // L2 prefetch of item nx's box rows and region rows by the whole CTA, one
-    // 128-byte line per instruction, issued while the current item computes
-    // so that the next item's loads hit L2.
+    // L2 prefetch of item nx's box rows in the occupancy bitmap and of its
+    // region rows, issued while the current item computes so that the next
+    // item's bitmap and region loads hit L2.
     auto prefetch_next = [&](uint32_t nx) {
         if (nx >= n_items) return;
         const WorkItem nw = P.items[nx];
         const RepDesc nr = P.reps[nw.rep];
-        const int nX = (int)nr.X, nY = (int)nr.Y, nZ = (int)nr.Z;
-        const int zs = max((int)nw.z0 - 1, 0), ze = min((int)nw.z0 + 33, nZ);
-        constexpr int LPR = (34 * K + 127) / 128 + 1;  // lines a box row can touch
-        const int nslot = NROW0 * LPR + ((nr.flags & 1u) ? 0 : B::RPX * RWY);
+        const int nX = (int)nr.X, nY = (int)nr.Y;
+        const int nslot = NROW0 + ((nr.flags & 1u) ? 0 : B::RPX * RWY);
         for (int k = tid; k < nslot; k += NT) {
-            if (k < NROW0 * LPR) {
-                const int i = k / LPR, l = k - i * LPR;
-                const int pp = i / WY, r = i - pp * WY, x = (int)nw.x0 - 1 + pp, y = (int)nw.y0 - 1 + r;
-                if (x < 0 || x >= nX || y < 0 || y >= nY || ze <= zs) continue;
-                const uint64_t vb = nr.base + ((uint64_t)x * (uint64_t)nY + (uint64_t)y) * (uint64_t)nZ;
-                const uint64_t b0 = ((vb + (uint64_t)zs) * K) & ~127ull, b1 = (vb + (uint64_t)ze) * K;
-                const uint64_t at = b0 + 128ull * (uint64_t)l;
-                if (at < b1) prefetch_l2(P.src + at);
+            if (k < NROW0) {
+                const int pp = k / WY, r = k - pp * WY, x = (int)nw.x0 - 1 + pp, y = (int)nw.y0 - 1 + r;
+                if (x < 0 || x >= nX || y < 0 || y >= nY) continue;
+                prefetch_l2(P.osrc + nr.obase + ((uint64_t)x * (uint64_t)nY + (uint64_t)y) * nr.Wz + (nw.z0 >> 5));
             } else {
-                const int j = k - NROW0 * LPR, rp = j / RWY, ry = j - rp * RWY;
+                const int j = k - NROW0, rp = j / RWY, ry = j - rp * RWY;
                 const int x = (int)nw.x0 - 2 + rp, y = (int)nw.y0 - 2 + ry;
                 if (x < 0 || x >= nX || y < 0 || y >= nY) continue;
                 prefetch_l2(P.region_pad + nr.rbase + ((uint64_t)x * (uint64_t)nY + (uint64_t)y) * nr.Zr + nw.z0);
@@ -190,6 +187,13 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
         const uint32_t it = s_item;
         if (it >= n_items) break;
         uint32_t nxt = 0u, cidx = 0u;
+        bool done = false;  // the item ran to the end (not abandoned)
+        int dnp = 0, dny = 0;
+        uint64_t orow0 = 0;  // bitmap word of interior row (pi, r) = orow0 + (pi - 1) * Y Wz + (r - 1) * Wz
+        uint32_t oY = 0, oWz = 0;
+        auto orow = [&](int pi, int r) -> uint64_t {
+            return orow0 + ((uint64_t)(pi - 1) * oY + (uint64_t)(r - 1)) * oWz;
+        };
         if (tid == 0) nxt = atomicAdd(P.queue, 1u);  // the next item, needed only at the end of this one
         do {
             WorkItem wi = P.items[sub ? it / sub : it];
@@ -205,6 +209,11 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
             const int x0 = (int)wi.x0, y0 = (int)wi.y0, z0 = (int)wi.z0;
             const int np = (int)(wi.x1 - wi.x0);  // interior planes inside the lattice
             const int ny = min(BY, Y - y0);       // interior rows inside the lattice
+            dnp = np;
+            dny = ny;
+            oY = (uint32_t)Y;
+            oWz = rd.Wz;
+            orow0 = rd.obase + ((uint64_t)x0 * (uint64_t)Y + (uint64_t)y0) * rd.Wz + (uint64_t)(z0 >> 5);
             const uint64_t colv = ((1ull << min(32, Z - z0)) - 1ull) << 1;  // interior columns inside
             const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
             const bool uniform = (rd.flags & 1u) != 0u;
@@ -232,9 +241,11 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                 return rb + (uint32_t)__popcll(m & ((1ull << c) - 1ull));
             };
             // Appends the set bits of one row mask per lane (row index `row`, only
-            // when `valid`) to the CTA-wide list and pool `t`: the warp reserves a
-            // contiguous range with one shared atomic.  Returns the lane's row base.
-            auto append_rows = [&](uint64_t m, int row, bool valid, int t, uint32_t cap) -> uint32_t {
+            // when `valid`) to list `out` of capacity `cap`, counted by top[t]:
+            // the warp reserves a contiguous range with one shared atomic.  Returns
+            // the lane's row base.  A total beyond `cap` is an overflow (top[t] >
+            // cap); nothing is written past `cap`.
+            auto append_list = [&](uint64_t m, int row, bool valid, int t, uint32_t cap, uint16_t* out) -> uint32_t {
                 const uint32_t c = valid ? (uint32_t)__popcll(m) : 0u;
                 uint32_t incl = c;
     #pragma unroll
@@ -252,10 +263,16 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                 while (bits) {
                     const int col = __ffsll((long long)bits) - 1;
                     bits &= bits - 1ull;
-                    if (o < cap) L[o] = (uint16_t)((row << 6) | col);
+                    if (o < cap) out[o] = (uint16_t)((row << 6) | col);
                     o++;
                 }
                 return rb;
+            };
+            auto append_rows = [&](uint64_t m, int row, bool valid, int t, uint32_t cap) -> uint32_t {
+                return append_list(m, row, valid, t, cap, L);
+            };
+            auto append_rows_pos = [&](uint64_t m, int row, bool valid, uint32_t cap, uint16_t* out) -> uint32_t {
+                return append_list(m, row, valid, 0, cap, out);
             };
             auto spill = [&]() {
                 if (tid == 0) {
@@ -283,71 +300,34 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
             for (int i = tid; i < NROW0; i += NT) { XM[i] = 0ull; XP[i] = 0ull; }
             for (int i = tid; i < NROW1; i += NT) { YM[i] = 0ull; YP[i] = 0ull; PB1[i] = 0ull; }
             for (int i = tid; i < NROW2; i += NT) { ZM[i] = 0ull; ZP[i] = 0ull; PB2[i] = 0ull; }
-            for (int ib = w; ib < NROW0; ib += NW * RB) {
-                // rows ib + u*NW: lane l loads column l; lanes 0..2RB-1 load column 32 + (l & 1) of row l >> 1
-                Vox<K> a[RB], xb = vox_zero<K>();
-    #pragma unroll
-                for (int u = 0; u < RB; u++) {
-                    const int i = ib + u * NW;
-                    a[u] = vox_zero<K>();
-                    if (i < NROW0) {
-                        const int p = i / WY, r = i - p * WY, x = x0 - 1 + p, y = y0 - 1 + r, z = z0 - 1 + lane;
-                        if (x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z)
-                            a[u] = ld_vox_g<K>(src + (uint64_t)lin(x, y, z) * K);
+            // box rows from the input occupancy bitmap: lane l of warp w takes row 32 w + l
+            for (int ib = w * 32; ib < NROW0; ib += NT) {
+                const int i = ib + lane;
+                uint64_t m = 0ull;
+                if (i < NROW0) {
+                    const int p = i / WY, r = i - p * WY, x = x0 - 1 + p, y = y0 - 1 + r;
+                    if (x >= 0 && x < X && y >= 0 && y < Y) {
+                        // columns c = 0..33 are z = z0 - 1 + c: bit 31 of the word before, the word at
+                        // z0 (z0 is a multiple of 32), bit 0 of the word after
+                        const uint32_t* wr = P.osrc + rd.obase + ((uint64_t)x * (uint64_t)Y + (uint64_t)y) * rd.Wz;
+                        const int wz = z0 >> 5;
+                        const uint32_t cur = __ldg(wr + wz);
+                        const uint32_t prv = wz > 0 ? __ldg(wr + wz - 1) : 0u;
+                        const uint32_t nx = wz + 1 < (int)rd.Wz ? __ldg(wr + wz + 1) : 0u;
+                        m = (uint64_t)(prv >> 31) | ((uint64_t)cur << 1) | ((uint64_t)(nx & 1u) << 33);
                     }
                 }
-                if (lane < 2 * RB) {
-                    const int i = ib + (lane >> 1) * NW;
-                    if (i < NROW0) {
-                        const int p = i / WY, r = i - p * WY, x = x0 - 1 + p, y = y0 - 1 + r, z = z0 + 31 + (lane & 1);
-                        if (x >= 0 && x < X && y >= 0 && y < Y && z < Z) xb = ld_vox_g<K>(src + (uint64_t)lin(x, y, z) * K);
-                    }
-                }
-                const bool ox = !vox_empty<K>(xb);
-                const uint32_t xm = __ballot_sync(0xffffffffu, ox);
-                uint32_t lo[RB], run[RB], tot = 0u;
-    #pragma unroll
-                for (int u = 0; u < RB; u++) {
-                    lo[u] = __ballot_sync(0xffffffffu, !vox_empty<K>(a[u]));
-                    run[u] = tot;
-                    tot += (uint32_t)__popc(lo[u]) + (uint32_t)__popc((xm >> (2 * u)) & 3u);
-                }
-                uint32_t base = 0u;
-                if (lane == 0 && tot) base = atomicAdd(top + 0, tot);
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (base + tot > (uint32_t)CAP0) {
-                    if (lane == 0) s_over = it;
-                    continue;
-                }
-                uint32_t xe = 0u;  // pool index of this lane's extra column (lanes < 2 RB)
-    #pragma unroll
-                for (int u = 0; u < RB; u++) {
-                    const int i = ib + u * NW;
-                    if (i >= NROW0) break;
-                    const uint32_t rb = base + run[u], hi = (xm >> (2 * u)) & 3u;
-                    if (lane == 0) {
-                        OCC0[i] = (uint64_t)lo[u] | ((uint64_t)hi << 32);
-                        RB0[i] = (uint16_t)rb;
-                    }
-                    if ((lo[u] >> lane) & 1u) {
-                        const uint32_t e = rb + (uint32_t)__popc(lo[u] & lt);
-                        cont0[e] = a[u];
-                        pos0[e] = (uint16_t)((i << 6) | lane);
-                    }
-                    // column 32 follows the row's 32 main columns, column 33 follows column 32
-                    if ((lane >> 1) == u) xe = rb + (uint32_t)__popc(lo[u]) + ((lane & 1) ? (hi & 1u) : 0u);
-                }
-                if (ox) {
-                    const uint32_t e = xe;
-                    const int i = ib + (lane >> 1) * NW;
-                    cont0[e] = xb;
-                    pos0[e] = (uint16_t)((i << 6) | (32 + (lane & 1)));
+                // reserve this warp's pool range, then list the occupied voxels of each row
+                const uint32_t rb = append_rows_pos(m, i, i < NROW0, CAP0, pos0);
+                if (i < NROW0) {
+                    OCC0[i] = m;
+                    RB0[i] = (uint16_t)min(rb, 65535u);
                 }
             }
             if (tid == 0) s_next = nxt;
             cp_async_wait<0>();
             __syncthreads();
-            if (s_over == it) {
+            if (top[0] > (uint32_t)CAP0) {
                 spill();
                 break;
             }
@@ -359,12 +339,14 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                     const uint32_t ps = pos0[e];
                     const int i = (int)(ps >> 6), c = (int)(ps & 63u), p = i / WY, r = i - p * WY;
                     const uint32_t v = lin(x0 - 1 + p, y0 - 1 + r, z0 - 1 + c);
+                    const Vox<K> own = ld_vox_g<K>(src + (uint64_t)v * K);  // occupied: fetch its slots
                     const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
+                    cont0[e] = own;
                     W01[e] = b0.y;
                     W02[e] = b0.z;
                     W03[e] = b0.w;
                     const uint32_t rs = code(p, r, c);
-                    const uint32_t d = decide_moves<K>(cont0[e], v, frame, 0u, trow(rs, code(p - 1, r, c)),
+                    const uint32_t d = decide_moves<K>(own, v, frame, 0u, trow(rs, code(p - 1, r, c)),
                                                        trow(rs, code(p + 1, r, c)), k0, k1, b0.x);
                     DEC0[e] = d;
                     if (d & 0xFFFFu) atomicOr(reinterpret_cast<unsigned long long*>(XM + i), 1ull << c);
@@ -531,13 +513,24 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                         s3 = all_react ? colv : ((S2m[j2] | (ZP[j2] << 1) | (ZM[j2] >> 1)) & colv);
                     }
                 }
-                // interior voxels that nothing reaches end the frame empty: coalesced zero stores
+                // The destination's bitmap says which of its voxels hold stale particles.
+                // Interior voxels that nothing reaches end the frame empty: only the stale
+                // ones among them need a zero store.
+                uint32_t oldw = 0u;
+                if (row_in) {
+                    const int pi = j2 / BY + 1, r = j2 - (pi - 1) * BY + 1;
+                    oldw = P.odst[orow(pi, r)];
+                }
+                if (valid) {
+                    OLDW[j2] = oldw;
+                    NEWW[j2] = 0u;
+                }
+                const uint32_t zb = oldw & ~(uint32_t)(s3 >> 1);  // bit b: column b + 1
                 for (int k = 0; k < RW2; k++) {
-                    const int rk = __shfl_sync(0xffffffffu, (int)row_in, k);
-                    if (!rk) continue;
-                    const uint64_t sk = __shfl_sync(0xffffffffu, s3, k);
-                    const int jk = w + k * NW, pi = jk / BY + 1, r = jk - (pi - 1) * BY + 1, c = lane + 1;
-                    if (((colv >> c) & 1ull) && !((sk >> c) & 1ull))
+                    const uint32_t zk = __shfl_sync(0xffffffffu, zb, k);
+                    if (!zk) continue;
+                    const int jk = w + k * NW, pi = jk / BY + 1, r = jk - (pi - 1) * BY + 1;
+                    if ((zk >> lane) & 1u)
                         st_vox_g<K>(dst + (uint64_t)lin(x0 - 1 + pi, y0 - 1 + r, z0 + lane) * K, vox_zero<K>());
                 }
                 append_rows(s3, j2, valid && row_in, 3, (uint32_t)LCAP);
@@ -574,11 +567,24 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                             react_voxel<K>(r3, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, P.T, s_delta, s_diag,
                                            w3);
                     }
-                    st_vox_g<K>(dst + (uint64_t)v * K, r3);
+                    if (!vox_empty<K>(r3)) {
+                        st_vox_g<K>(dst + (uint64_t)v * K, r3);
+                        atomicOr(NEWW + jj, 1u << (c - 1));
+                    } else if ((OLDW[jj] >> (c - 1)) & 1u) {
+                        st_vox_g<K>(dst + (uint64_t)v * K, vox_zero<K>());
+                    }
                 }
             }
+            done = true;
         } while (0);
         __syncthreads();
+        if (done) {
+            // the interior rows' new occupancy words (each interior row is one word: z0 % 32 == 0)
+            for (int j = tid; j < NROW2; j += NT) {
+                const int pi = j / BY + 1, r = j - (pi - 1) * BY + 1;
+                if (pi <= dnp && r <= dny) P.odst[orow(pi, r)] = NEWW[j];
+            }
+        }
         for (uint32_t s = tid; s < S1; s += NT) {
             const int32_t dlt = s_delta[s];
             if (dlt) {

@@ -82,9 +82,10 @@ static const std::vector<KernelCfg>& all_cfgs() {
         tile_cfg<16, 8, 32, 256, 3>(),  tile_cfg<16, 4, 64, 256, 3>(), tile_cfg<16, 16, 32, 256, 1>(),
         tile_cfg<16, 8, 64, 256, 1>(),  tile_cfg<8, 8, 32, 256, 3>(),  tile_cfg<8, 4, 64, 256, 3>(),
         tile_cfg<8, 16, 32, 256, 2>(),  tile_cfg<8, 8, 64, 256, 2>(),
-        // sparse bricks (8 planes) whose crowded bricks go to the dense 2-plane pass of the same K
+        // sparse bricks whose crowded bricks go to the dense 2-plane pass of the same K (entries 10, 11)
         brick_cfg<16, 8, 8, 256, 3, 768, 768, 768>(10, 4), brick_cfg<8, 8, 8, 256, 3, 768, 768, 768>(11, 4),
         dense_brick_cfg<16, 2, 8, 256, 3>(), dense_brick_cfg<8, 2, 8, 256, 3>(),
+        brick_cfg<16, 8, 8, 256, 4, 512, 512, 512>(10, 4), brick_cfg<16, 4, 8, 128, 6, 384, 384, 384>(10, 2),
     };
     return v;
 }
@@ -103,6 +104,9 @@ struct DeviceProd {
     std::vector<RepDesc> h_reps;
     DevBuf<RepDesc> reps;
     DevBuf<uint8_t> slots[2];
+    DevBuf<uint32_t> occ[2];  // occupancy bitmaps of slots[0] and slots[1]
+    uint64_t occ_words = 0;
+    bool occ_valid = false;   // the bitmaps describe the slot buffers (false after uploads and tile frames)
     DevBuf<uint8_t> region_pad, reservoir;
     DevBuf<uint32_t> thr;
     DevBuf<uint8_t> rx_reactants, rx_ch_sp;
@@ -393,6 +397,46 @@ static void set_cfg(DeviceProd* d, int idx) {
     }
 }
 
+// Occupancy bitmap of one replicate's slot buffer: one warp per (x, y) row,
+// one ballot per 32 voxels.
+template <int K>
+__global__ void occ_rebuild_kernel(const uint8_t* slots, uint32_t* occ, RepDesc rd) {
+    const uint64_t rows = (uint64_t)rd.X * rd.Y;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x / 32);
+    for (uint64_t row = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); row < rows; row += nwarps) {
+        const uint8_t* sr = slots + (rd.base + row * rd.Z) * K;
+        for (uint32_t k = 0; k < rd.Wz; k++) {
+            const uint32_t z = 32u * k + (uint32_t)lane;
+            bool nz = false;
+            if (z < rd.Z) {
+                const uint8_t* p = sr + (uint64_t)z * K;
+                if (K == 16) {
+                    const uint4 t = *reinterpret_cast<const uint4*>(p);
+                    nz = (t.x | t.y | t.z | t.w) != 0u;
+                } else {
+                    const uint2 t = *reinterpret_cast<const uint2*>(p);
+                    nz = (t.x | t.y) != 0u;
+                }
+            }
+            const uint32_t m = __ballot_sync(0xffffffffu, nz);
+            if (lane == 0) occ[rd.obase + row * rd.Wz + k] = m;
+        }
+    }
+}
+
+static void rebuild_occupancy(DeviceProd* d) {
+    for (int b = 0; b < 2; b++)
+        for (const RepDesc& r : d->h_reps) {
+            const uint64_t rows = (uint64_t)r.X * r.Y;
+            const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((rows + 7) / 8, (uint64_t)d->num_sms * 8));
+            if (d->K == 16) occ_rebuild_kernel<16><<<blocks, 256, 0, d->stream>>>(d->slots[b].p, d->occ[b].p, r);
+            else occ_rebuild_kernel<8><<<blocks, 256, 0, d->stream>>>(d->slots[b].p, d->occ[b].p, r);
+            CS_LAUNCH_CHECK();
+        }
+    d->occ_valid = true;
+}
+
 static int grid_for(DeviceProd* d, const KernelCfg& cfg, uint32_t n_items) {
     int per_sm = 0;
     CS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg.fn, cfg.NT, cfg_smem(d, cfg)));
@@ -416,6 +460,8 @@ static void launch_frame(DeviceProd* d, int parity, int rep) {
     P.stepbuf = d->stepbuf.p;
     P.src = d->slots[parity].p;
     P.dst = d->slots[parity ^ 1].p;
+    P.osrc = d->occ[parity].p;
+    P.odst = d->occ[parity ^ 1].p;
     P.region_pad = d->region_pad.p;
     P.reservoir = d->reservoir.n ? d->reservoir.p : nullptr;
     P.counts = d->counts.p;
@@ -481,6 +527,15 @@ static DeviceProd* prod_alloc(const Model& m, int device, const std::vector<RepD
     CS_CUDA(cudaMemcpy(d->reps.p, reps.data(), reps.size() * sizeof(RepDesc), cudaMemcpyHostToDevice));
     build_one_table(d.get());
     for (int b = 0; b < 2; b++) d->slots[b].alloc(total_voxels * d->K);
+    d->occ_words = 0;
+    for (auto& r : d->h_reps) {
+        r.Wz = (r.Z + 31) / 32;
+        r.obase = d->occ_words;
+        d->occ_words += (uint64_t)r.X * r.Y * r.Wz;
+    }
+    CS_CUDA(cudaMemcpy(d->reps.p, d->h_reps.data(), d->h_reps.size() * sizeof(RepDesc), cudaMemcpyHostToDevice));
+    for (int b = 0; b < 2; b++) d->occ[b].alloc(d->occ_words);
+    d->occ_valid = false;
     d->counts.alloc((size_t)d->n_rep * d->S1);
     d->diag.alloc(PD_N);
     d->counters.alloc((size_t)2 * kCtrPerParity * (1 + d->n_rep));
@@ -557,6 +612,7 @@ void prod_set_lattice(DeviceProd* d, const Model& m, const uint32_t* slots) {
     CS_CUDA(cudaStreamSynchronize(d->stream));
     d->cur = 0;
     CS_CUDA(cudaMemcpy(d->slots[0].p, s8.data(), s8.size(), cudaMemcpyHostToDevice));
+    d->occ_valid = false;
     std::vector<unsigned long long> c(d->S1);
     for (uint32_t s = 0; s < d->S1; s++) c[s] = (unsigned long long)cnt[s];
     CS_CUDA(cudaMemcpy(d->counts.p, c.data(), c.size() * 8, cudaMemcpyHostToDevice));
@@ -612,6 +668,9 @@ static void run_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched)
 
 // Enqueues n frames; the frame number must already be in stepbuf[cur].
 static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched) {
+    const bool brick = all_cfgs()[d->cfg_index].kind == KIND_BRICK;
+    if (n && brick && !d->occ_valid) rebuild_occupancy(d);
+    if (n && !brick) d->occ_valid = false;  // the tile pipeline does not keep the bitmaps
     uint32_t k = 0;
     if (batched) {
         if (d->cur == 1 && k < n) {
@@ -758,6 +817,7 @@ DeviceProd* prod_ensemble_create(const Model& m, uint32_t n, const uint32_t* res
         }
         CS_CUDA(cudaMemcpy(d->slots[0].p + rd.base * d->K, s8.data(), s8.size(), cudaMemcpyHostToDevice));
     }
+    d->occ_valid = false;
     CS_CUDA(cudaMemcpy(d->counts.p, cnt.data(), cnt.size() * 8, cudaMemcpyHostToDevice));
     d->cur = 0;
     return d.release();

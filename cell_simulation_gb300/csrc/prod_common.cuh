@@ -50,7 +50,8 @@ struct RepDesc {
     float rate_mult;
     uint32_t counts_index;  // replicate index into the counts array
     uint32_t flags;         // bit 0: the whole lattice is region 0 (no region-code array)
-    uint32_t pad[3];
+    uint32_t Wz;            // occupancy-bitmap words per (x, y) row: ceil(Z / 32)
+    uint64_t obase;         // first word of this replicate in the occupancy bitmaps
 };
 static_assert(sizeof(RepDesc) == 64, "RepDesc is 64 bytes");
 

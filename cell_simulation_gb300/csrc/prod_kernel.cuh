@@ -47,6 +47,10 @@ struct ProdParams {
     uint32_t sub;                 // brick pass over spilled bricks: plane groups per brick
     const uint8_t* src;
     uint8_t* dst;
+    // occupancy bitmaps of src and dst (bit z % 32 of word obase + (x Y + y) Wz + z / 32 is set
+    // exactly when the voxel holds a particle); maintained by the brick pass
+    const uint32_t* osrc;
+    uint32_t* odst;
     const uint8_t* region_pad;   // padded region codes, see RepDesc::rbase
     const uint8_t* reservoir;    // may be null
     unsigned long long* counts;  // [n_rep][S1]

@@ -186,3 +186,26 @@ def test_ensemble_batched_equals_plain_and_oracle(orc):
         assert np.array_equal(got[off * 8:(off + V) * 8], sl), r
         assert np.array_equal(counts[r], c0), r
         off += V
+
+
+def test_switching_step_kinds_mid_run_matches_oracle(orc):
+    """Tile-pipeline frames do not maintain the occupancy bitmaps of the brick
+    pass; switching back rebuilds them.  A lattice upload in between does too."""
+    mk = lambda: multi_region_model(res=(13, 17, 40), K=16, counts=(90, 70, 50, 40))
+    want_s, want_c, _ = oracle_prod(orc, mk(), 18, seed=321)
+    sim = mk()
+    sim.prepare_for_gpu(RNG_PHILOX, 0)
+    kinds = tiling_kinds()
+    tile = next(i for i, (t, k) in enumerate(zip(tiling_variants(), kinds)) if t[0] == 16 and k[0] == 0)
+    brick = next(i for i, (t, k) in enumerate(zip(tiling_variants(), kinds)) if t[0] == 16 and k == (1, 8))
+    sim.set_tiling(brick)
+    sim.step_philox(6, 321)
+    sim.set_tiling(tile)
+    sim.step_philox(6, 321)
+    sim.set_tiling(brick)
+    s_mid = sim.get_lattice()[0]
+    sim.set_lattice(s_mid)  # same content, fresh upload
+    sim.step_philox(6, 321)
+    got_s, _, _ = sim.get_lattice()
+    assert np.array_equal(got_s.astype(np.uint8), want_s)
+    assert np.array_equal(sim.counts(), want_c)
