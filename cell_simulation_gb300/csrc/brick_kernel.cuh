@@ -78,8 +78,9 @@ struct Brick {
     static constexpr size_t off_pos = a16(off_rb + (size_t)(NROW0 + NROW1 + NROW2) * 2);  // u16 [CAP0]
     static constexpr size_t off_list = a16(off_pos + (size_t)CAP0 * 2);   // u16 [LCAP] positions of a phase's voxels
     static constexpr size_t off_reg = a16(off_list + (size_t)LCAP * 2);   // u8 [RPX][RWY][RWZB]
+    static constexpr size_t off_nocc = a16(off_reg + (size_t)RPX * RPLANE);  // u64 [NROW0] next item's OCC0
     // u32 tops[4], old and new occupancy words of the interior rows [2][NROW2], delta[S1], diag, thr
-    static constexpr size_t off_tail = a16(off_reg + (size_t)RPX * RPLANE);
+    static constexpr size_t off_tail = off_nocc + (size_t)NROW0 * 8;
     static size_t smem(uint32_t S1, uint32_t thr_words) {
         return off_tail + (size_t)(4 + 2 * NROW2 + S1 + PD_N + thr_words) * 4;
     }
@@ -127,13 +128,16 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
     uint16_t* pos0 = reinterpret_cast<uint16_t*>(smem + B::off_pos);
     uint16_t* L = reinterpret_cast<uint16_t*>(smem + B::off_list);
     uint8_t* reg = smem + B::off_reg;
+    uint64_t* nocc = reinterpret_cast<uint64_t*>(smem + B::off_nocc);  // box masks staged for item s_staged
     uint32_t* top = reinterpret_cast<uint32_t*>(smem + B::off_tail);  // [4] pool 0, pool 1, pool 2, D list
     uint32_t* OLDW = top + 4;       // destination occupancy word of each interior row before the frame
     uint32_t* NEWW = OLDW + NROW2;  // and after it
     int32_t* s_delta = reinterpret_cast<int32_t*>(NEWW + NROW2);
     uint32_t* s_diag = reinterpret_cast<uint32_t*>(s_delta + P.T.S1);
     uint32_t* s_thr = s_diag + PD_N;
-    __shared__ uint32_t s_item, s_next;
+    __shared__ uint32_t s_item, s_next, s_staged;
+    __shared__ WorkItem s_nwi;  // item s_staged and its replicate, loaded during the previous item
+    __shared__ RepDesc s_nrd;
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const uint32_t lt = (1u << lane) - 1u;
@@ -155,31 +159,45 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
     const uint32_t sub = P.sub;
     const uint32_t n_items = P.n_items_dev ? *P.n_items_dev * (sub ? sub : 1u) : P.n_items;
 
-    // L2 prefetch of item nx's box rows in the occupancy bitmap and of its
-    // region rows, issued while the current item computes so that the next
-    // item's bitmap and region loads hit L2.
-    auto prefetch_next = [&](uint32_t nx) {
+    // Staging of item nx (the next item of this CTA) while the current one
+    // computes: its work item and replicate go to shared memory, its region
+    // rows are prefetched into L2 (phase A), and its box occupancy masks are
+    // read from the bitmap into shared memory (phase B), so that the next
+    // item starts without waiting on global memory.
+    auto stage_item = [&](uint32_t nx) {
         if (nx >= n_items) return;
+        if (tid == NT - 32) {
+            s_nwi = P.items[nx];
+            s_nrd = P.reps[s_nwi.rep];
+        }
         const WorkItem nw = P.items[nx];
         const RepDesc nr = P.reps[nw.rep];
+        if (nr.flags & 1u) return;
         const int nX = (int)nr.X, nY = (int)nr.Y;
-        const int nslot = NROW0 + ((nr.flags & 1u) ? 0 : B::RPX * RWY);
-        for (int k = tid; k < nslot; k += NT) {
-            if (k < NROW0) {
-                const int pp = k / WY, r = k - pp * WY, x = (int)nw.x0 - 1 + pp, y = (int)nw.y0 - 1 + r;
-                if (x < 0 || x >= nX || y < 0 || y >= nY) continue;
-                prefetch_l2(P.osrc + nr.obase + ((uint64_t)x * (uint64_t)nY + (uint64_t)y) * nr.Wz + (nw.z0 >> 5));
-            } else {
-                const int j = k - NROW0, rp = j / RWY, ry = j - rp * RWY;
-                const int x = (int)nw.x0 - 2 + rp, y = (int)nw.y0 - 2 + ry;
-                if (x < 0 || x >= nX || y < 0 || y >= nY) continue;
-                prefetch_l2(P.region_pad + nr.rbase + ((uint64_t)x * (uint64_t)nY + (uint64_t)y) * nr.Zr + nw.z0);
-            }
+        for (int k = tid; k < B::RPX * RWY; k += NT) {
+            const int rp = k / RWY, ry = k - rp * RWY;
+            const int x = (int)nw.x0 - 2 + rp, y = (int)nw.y0 - 2 + ry;
+            if (x < 0 || x >= nX || y < 0 || y >= nY) continue;
+            prefetch_l2(P.region_pad + nr.rbase + ((uint64_t)x * (uint64_t)nY + (uint64_t)y) * nr.Zr + nw.z0);
         }
+    };
+    // OCC0 row i of item (nw, nr) from the occupancy bitmap: columns c = 0..33 are
+    // z = z0 - 1 + c: bit 31 of the word before, the word at z0 (z0 is a multiple
+    // of 32), bit 0 of the word after
+    auto box_mask = [&](const WorkItem& nw, const RepDesc& nr, int i) -> uint64_t {
+        const int p = i / WY, r = i - p * WY, x = (int)nw.x0 - 1 + p, y = (int)nw.y0 - 1 + r;
+        if (x < 0 || x >= (int)nr.X || y < 0 || y >= (int)nr.Y) return 0ull;
+        const uint32_t* wr = P.osrc + nr.obase + ((uint64_t)x * (uint64_t)nr.Y + (uint64_t)y) * nr.Wz;
+        const int wz = (int)(nw.z0 >> 5);
+        const uint32_t cur = __ldg(wr + wz);
+        const uint32_t prv = wz > 0 ? __ldg(wr + wz - 1) : 0u;
+        const uint32_t nx = wz + 1 < (int)nr.Wz ? __ldg(wr + wz + 1) : 0u;
+        return (uint64_t)(prv >> 31) | ((uint64_t)cur << 1) | ((uint64_t)(nx & 1u) << 33);
     };
 
     if (tid == 0) {
         s_item = atomicAdd(P.queue, 1u);
+        s_staged = 0xFFFFFFFFu;
         top[0] = 0u; top[1] = 0u; top[2] = 0u; top[3] = 0u;
     }
     for (;;) {
@@ -196,14 +214,15 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
         };
         if (tid == 0) nxt = atomicAdd(P.queue, 1u);  // the next item, needed only at the end of this one
         do {
-            WorkItem wi = P.items[sub ? it / sub : it];
+            const bool staged = s_staged == it;  // wi, rd and the box masks are in shared memory
+            WorkItem wi = staged ? s_nwi : P.items[sub ? it / sub : it];
             if (sub) {
                 const uint32_t xs = wi.x0 + (it % sub) * (uint32_t)BX;
                 if (xs >= wi.x1) break;
                 wi.x0 = xs;
                 wi.x1 = min(wi.x1, xs + (uint32_t)BX);
             }
-            const RepDesc rd = P.reps[wi.rep];
+            const RepDesc rd = staged ? s_nrd : P.reps[wi.rep];
             cidx = rd.counts_index;
             const int X = (int)rd.X, Y = (int)rd.Y, Z = (int)rd.Z, Zr = (int)rd.Zr;
             const int x0 = (int)wi.x0, y0 = (int)wi.y0, z0 = (int)wi.z0;
@@ -304,19 +323,7 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
             for (int ib = w * 32; ib < NROW0; ib += NT) {
                 const int i = ib + lane;
                 uint64_t m = 0ull;
-                if (i < NROW0) {
-                    const int p = i / WY, r = i - p * WY, x = x0 - 1 + p, y = y0 - 1 + r;
-                    if (x >= 0 && x < X && y >= 0 && y < Y) {
-                        // columns c = 0..33 are z = z0 - 1 + c: bit 31 of the word before, the word at
-                        // z0 (z0 is a multiple of 32), bit 0 of the word after
-                        const uint32_t* wr = P.osrc + rd.obase + ((uint64_t)x * (uint64_t)Y + (uint64_t)y) * rd.Wz;
-                        const int wz = z0 >> 5;
-                        const uint32_t cur = __ldg(wr + wz);
-                        const uint32_t prv = wz > 0 ? __ldg(wr + wz - 1) : 0u;
-                        const uint32_t nx = wz + 1 < (int)rd.Wz ? __ldg(wr + wz + 1) : 0u;
-                        m = (uint64_t)(prv >> 31) | ((uint64_t)cur << 1) | ((uint64_t)(nx & 1u) << 33);
-                    }
-                }
+                if (i < NROW0) m = staged ? nocc[i] : box_mask(wi, rd, i);
                 // reserve this warp's pool range, then list the occupied voxels of each row
                 const uint32_t rb = append_rows_pos(m, i, i < NROW0, CAP0, pos0);
                 if (i < NROW0) {
@@ -353,7 +360,7 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                     if (d >> 16) atomicOr(reinterpret_cast<unsigned long long*>(XP + i), 1ull << c);
                 }
             }
-            if (sub == 0u) prefetch_next(s_next);
+            if (sub == 0u) stage_item(s_next);
             __syncthreads();
 
             // ---------------- B: X sweep of the interior planes, y-decisions ----------------
@@ -423,6 +430,22 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                     if (d >> 16) atomicOr(reinterpret_cast<unsigned long long*>(YP + jj), bc);
                 }
                 DEC1[e1] = d;
+            }
+            if (sub == 0u && s_next < n_items) {
+                // the next item's box masks, by the highest threads (the least busy here), and an L2
+                // prefetch of the slots of its occupied voxels
+                for (int i = NT - 1 - tid; i < NROW0; i += NT) {
+                    const uint64_t m = box_mask(s_nwi, s_nrd, i);
+                    nocc[i] = m;
+                    if (m) {
+                        const int p = i / WY, r = i - p * WY;
+                        const uint64_t vrow = s_nrd.base + ((uint64_t)((int)s_nwi.x0 - 1 + p) * s_nrd.Y +
+                                                            (uint64_t)((int)s_nwi.y0 - 1 + r)) * s_nrd.Z;
+                        for (uint64_t b = m; b; b &= b - 1ull)
+                            prefetch_l2(P.src + (vrow + (uint64_t)((int)s_nwi.z0 - 1 + __ffsll((long long)b) - 1)) * K);
+                    }
+                }
+                if (tid == 0) s_staged = s_next;
             }
             __syncthreads();
 

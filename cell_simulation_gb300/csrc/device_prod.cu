@@ -86,6 +86,7 @@ static const std::vector<KernelCfg>& all_cfgs() {
         brick_cfg<16, 8, 8, 256, 3, 768, 768, 768>(10, 4), brick_cfg<8, 8, 8, 256, 3, 768, 768, 768>(11, 4),
         dense_brick_cfg<16, 2, 8, 256, 3>(), dense_brick_cfg<8, 2, 8, 256, 3>(),
         brick_cfg<16, 8, 8, 256, 4, 512, 512, 512>(10, 4), brick_cfg<16, 4, 8, 128, 6, 384, 384, 384>(10, 2),
+        brick_cfg<16, 8, 8, 192, 4, 544, 544, 544>(10, 4),
     };
     return v;
 }
