@@ -122,10 +122,11 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(workload: str):
-    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu summaries."""
+    key = re.escape(f"{kernel}/{workload}")
     for f in sorted((ROOT / "profiles").glob("*.md")):
-        m = re.search(rf"traffic_bytes_per_launch\[{re.escape(workload)}\]:\s*([0-9.eE+]+)", f.read_text())
+        m = re.search(rf"traffic_bytes_per_launch\[{key}\]:\s*([0-9.eE+]+)", f.read_text())
         if m:
             return float(m.group(1))
     return None
@@ -199,6 +200,23 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def describe_variant(i):
+    from cell_simulation_gb300 import tiling_kinds, tiling_variants
+    k, ty, tz, nt = tiling_variants()[i]
+    kind, bx = tiling_kinds()[i]
+    if kind == 1:
+        return {"index": i, "kind": "brick", "slots": k, "brick": [bx, ty, tz], "threads": nt}
+    return {"index": i, "kind": "tile", "slots": k, "tile": [ty, tz], "threads": nt}
+
+
+def launches_per_frame(i):
+    """Kernel launches per frame of variant i: a brick pass with bounded pools is
+    followed by the pass over its spilled bricks."""
+    from cell_simulation_gb300 import tiling_kinds
+    kind, bx = tiling_kinds()[i]
+    return 2 if kind == 1 and bx > 2 else 1
+
+
 def ensemble_numbers(device, steps_batched=200, steps_plain=20):
     from cell_simulation_gb300 import Ensemble, configs
 
@@ -206,6 +224,8 @@ def ensemble_numbers(device, steps_batched=200, steps_plain=20):
     res, seeds, mult, init = configs.c4_ensemble_spec()
     ens = Ensemble(tmpl, res, seeds, mult, init, device=device)
     tot, items = ens.info()
+    variant, _ = ens.autotune(3)
+    per_frame = launches_per_frame(variant)
     ens.step(3, batched=True)
     ms_b = ens.step_timed(steps_batched, batched=True)
     ens.step(1, batched=False)
@@ -217,7 +237,8 @@ def ensemble_numbers(device, steps_batched=200, steps_plain=20):
            "replicate_steps_per_s_batched": rb, "replicate_steps_per_s_plain": rp,
            "voxel_steps_per_s_batched": tot * steps_batched / (ms_b / 1e3),
            "batched_over_plain": rb / rp, "steps_batched": steps_batched, "steps_plain": steps_plain,
-           "launches_per_frame_batched": 1, "launches_per_frame_plain": n}
+           "launches_per_frame_batched": per_frame, "launches_per_frame_plain": n * per_frame,
+           "variant": describe_variant(variant)}
     ens.close()
     return out
 
@@ -230,6 +251,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip ensemble, reference-RNG, e2e and CPU legs")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--variant", type=int, default=-1, help="step variant index (default: autotuned)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = env_rank()
@@ -254,6 +276,11 @@ def main():
     sim.prepare_for_gpu(RNG_PHILOX, device)
     t_upload = time.perf_counter() - t0
     sim.set_precision(PREC_MIXED)
+    if args.variant >= 0:
+        variant = args.variant
+        sim.set_tiling(variant)
+    else:
+        variant, _ = sim.autotune(10)  # state restored: the timed frames start from the same lattice
     sim.step_philox(args.warmup, seed)
     sim.synchronize()
     clocks = ClockSampler(device)
@@ -268,7 +295,8 @@ def main():
     peak, peak_kind = measured_peaks()
     alg_bytes = V * (2 * K + 1)
     achieved = alg_bytes / per_launch_s / 1e9
-    traffic = profiled_traffic(w.name)
+    kernel = "brick_step_kernel" if describe_variant(variant)["kind"] == "brick" else "prod_step_kernel"
+    traffic = profiled_traffic(kernel, w.name)
     diag = sim.diagnostics()
 
     # end to end through the C ABI: every frame one step call (frame number up)
@@ -311,13 +339,15 @@ def main():
         "dtype": "u8", "data": "synthetic",
         "config": {"workload": w.name, "voxels": V, "slots_per_voxel": K, "species": S1 - 1,
                    "reactions": int(info.n_reactions), "rng": "philox4x32-10", "precision": "fp32 propensities, fp64 clock",
-                   "l2": "inputs larger than L2 (2 x 256 MiB lattice buffers)", "parallelism": f"replicas x{world}"},
+                   "l2": "inputs larger than L2 (2 x 256 MiB lattice buffers)", "parallelism": f"replicas x{world}",
+                   "variant": describe_variant(variant)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": alg_bytes, "kernel": "prod_step_kernel"},
+                     "algorithmic_bytes_per_launch": alg_bytes, "kernel": kernel,
+                     "achieved_over": "frame time (every launch of the frame)"},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * launches_per_frame(variant),
         "clocks": clk,
         "diagnostics": {"events": int(diag[0]), "rejected_capacity": int(diag[1]), "event_cap": int(diag[2]),
                         "fp64_selections": int(diag[3])},

@@ -526,6 +526,17 @@ cs_status cs_set_tiling(cs_sim* sim, int32_t index, uint32_t segment_length) {
     });
 }
 
+cs_status cs_autotune(cs_sim* sim, uint32_t frames_per_trial, int32_t* chosen_index, float* ms_per_frame) {
+    return guarded([&] {
+        need(sim, "sim");
+        if (!sim->prod) throw Error(CS_ERR_STATE, "autotuning applies to the production path (cs_prepare_for_gpu(CS_RNG_PHILOX))");
+        float ms = 0.0f;
+        int best = prod_autotune(sim->prod.get(), frames_per_trial, sim->frame, true, &ms);
+        if (chosen_index) *chosen_index = best;
+        if (ms_per_frame) *ms_per_frame = ms;
+    });
+}
+
 cs_status cs_get_tiling(const cs_sim* sim, int32_t* index) {
     return guarded([&] {
         need(sim, "sim");
@@ -594,6 +605,16 @@ cs_status cs_ensemble_set_tiling(cs_ensemble* ens, int32_t index, uint32_t segme
     return guarded([&] {
         need(ens, "ens");
         prod_set_tiling(ens->prod.get(), index, segment_length);
+    });
+}
+
+cs_status cs_ensemble_autotune(cs_ensemble* ens, uint32_t frames_per_trial, int32_t* chosen_index, float* ms_per_frame) {
+    return guarded([&] {
+        need(ens, "ens");
+        float ms = 0.0f;
+        int best = prod_autotune(ens->prod.get(), frames_per_trial, ens->frame, true, &ms);
+        if (chosen_index) *chosen_index = best;
+        if (ms_per_frame) *ms_per_frame = ms;
     });
 }
 

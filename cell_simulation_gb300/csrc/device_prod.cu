@@ -26,6 +26,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "cuda_check.h"
@@ -903,5 +906,78 @@ float prod_time_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched)
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     return ms;
+}
+}  // namespace cellsim
+
+namespace cellsim {
+// Autotuner: times every compiled configuration for this K on the handle's
+// own lattice and keeps the fastest.  Each trial starts from a device copy of
+// the current state and the state is restored afterwards, so tuning does not
+// advance or change the simulation (every configuration computes the same
+// frame anyway).  Choices are cached per (K, species, reactions, regions,
+// lattice shapes, device) for the life of the process.
+int prod_autotune(DeviceProd* d, uint32_t frames, uint64_t frame0, bool batched, float* best_ms) {
+    DeviceGuard g(d->device);
+    static std::mutex mu;
+    static std::map<std::string, std::pair<int, float>> cache;
+    cudaDeviceProp prop{};
+    CS_CUDA(cudaGetDeviceProperties(&prop, d->device));
+    std::string key = std::string(prop.name) + "|" + std::to_string(d->K) + "," + std::to_string(d->S1) + "," +
+                      std::to_string(d->R) + "," + std::to_string(d->NC) + "," + std::to_string(batched ? 1 : 0);
+    for (const RepDesc& r : d->h_reps) key += "|" + std::to_string(r.X) + "x" + std::to_string(r.Y) + "x" + std::to_string(r.Z);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) {
+            if (d->cfg_index != it->second.first) {
+                CS_CUDA(cudaStreamSynchronize(d->stream));
+                d->seg_len = 0;
+                set_cfg(d, it->second.first);
+            }
+            if (best_ms) *best_ms = it->second.second;
+            return it->second.first;
+        }
+    }
+    if (frames == 0) frames = 1;
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    const size_t bytes = (size_t)d->total_voxels * d->K;
+    DevBuf<uint8_t> keep;
+    keep.alloc(bytes);
+    DevBuf<unsigned long long> keep_counts;
+    keep_counts.alloc(d->counts.n);
+    DevBuf<uint32_t> keep_diag;
+    keep_diag.alloc(PD_N);
+    const int cur0 = d->cur;
+    CS_CUDA(cudaMemcpyAsync(keep.p, d->slots[cur0].p, bytes, cudaMemcpyDeviceToDevice, d->stream));
+    CS_CUDA(cudaMemcpyAsync(keep_counts.p, d->counts.p, d->counts.bytes(), cudaMemcpyDeviceToDevice, d->stream));
+    CS_CUDA(cudaMemcpyAsync(keep_diag.p, d->diag.p, PD_N * 4, cudaMemcpyDeviceToDevice, d->stream));
+    auto restore = [&]() {
+        CS_CUDA(cudaMemcpyAsync(d->slots[cur0].p, keep.p, bytes, cudaMemcpyDeviceToDevice, d->stream));
+        CS_CUDA(cudaMemcpyAsync(d->counts.p, keep_counts.p, d->counts.bytes(), cudaMemcpyDeviceToDevice, d->stream));
+        CS_CUDA(cudaMemcpyAsync(d->diag.p, keep_diag.p, PD_N * 4, cudaMemcpyDeviceToDevice, d->stream));
+        CS_CUDA(cudaStreamSynchronize(d->stream));
+        d->cur = cur0;
+        d->occ_valid = false;
+    };
+    const auto& c = all_cfgs();
+    int best = -1;
+    float best_t = 0.0f;
+    for (int i = 0; i < (int)c.size(); i++) {
+        if (c[i].K != (int)d->K) continue;
+        d->seg_len = 0;
+        set_cfg(d, i);
+        prod_time_frames(d, 2, frame0, batched);  // warm-up: graph, bitmaps, caches
+        restore();
+        const float t = prod_time_frames(d, frames, frame0, batched) / (float)frames;
+        restore();
+        if (best < 0 || t < best_t) { best = i; best_t = t; }
+    }
+    set_cfg(d, best);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        cache[key] = {best, best_t};
+    }
+    if (best_ms) *best_ms = best_t;
+    return best;
 }
 }  // namespace cellsim

@@ -172,6 +172,7 @@ void prod_tiling_kind(int i, int* kind, int* BX);
 int prod_tiling_current(const DeviceProd* d);
 void prod_seed(DeviceProd* d, uint64_t seed);
 float prod_time_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched);
+int prod_autotune(DeviceProd* d, uint32_t frames, uint64_t frame0, bool batched, float* best_ms);
 float ref_time_frames(DeviceRef* d, uint32_t n, const uint32_t* itimes, uint64_t frame0);
 void ref_frame_noalloc(const cs_ref_frame_noalloc_args* a);
 

@@ -107,6 +107,8 @@ SIGNATURES = {
     "cs_tiling_count": (st, [i32p]),
     "cs_tiling_describe": (st, [C.c_int32, i32p, i32p, i32p, i32p]),
     "cs_tiling_kind": (st, [C.c_int32, i32p, i32p]),
+    "cs_autotune": (st, [P, C.c_uint32, i32p, C.POINTER(C.c_float)]),
+    "cs_ensemble_autotune": (st, [P, C.c_uint32, i32p, C.POINTER(C.c_float)]),
     "cs_set_tiling": (st, [P, C.c_int32, C.c_uint32]),
     "cs_get_tiling": (st, [P, i32p]),
     "cs_ensemble_create": (st, [P, C.c_uint32, u32p, u64p, f32p, u32p, C.c_int32, C.POINTER(P)]),

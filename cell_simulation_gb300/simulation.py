@@ -284,6 +284,13 @@ class Simulation:
     def set_tiling(self, index: int, segment_length: int = 0) -> None:
         N.check(self._lib.cs_set_tiling(self._h, index, segment_length))
 
+    def autotune(self, frames_per_trial: int = 10) -> tuple[int, float]:
+        """Time every compiled variant on this lattice (state restored afterwards)
+        and keep the fastest: (chosen variant index, ms per frame)."""
+        i, ms = C.c_int32(), C.c_float()
+        N.check(self._lib.cs_autotune(self._h, frames_per_trial, C.byref(i), C.byref(ms)))
+        return i.value, ms.value
+
     def get_tiling(self) -> int:
         i = C.c_int32()
         N.check(self._lib.cs_get_tiling(self._h, C.byref(i)))
@@ -386,6 +393,13 @@ class Ensemble:
 
     def set_tiling(self, index: int, segment_length: int = 0) -> None:
         N.check(self._lib.cs_ensemble_set_tiling(self._h, index, segment_length))
+
+    def autotune(self, frames_per_trial: int = 5) -> tuple[int, float]:
+        """Time every compiled variant on these replicates (state restored
+        afterwards) and keep the fastest: (chosen variant index, ms per frame)."""
+        i, ms = C.c_int32(), C.c_float()
+        N.check(self._lib.cs_ensemble_autotune(self._h, frames_per_trial, C.byref(i), C.byref(ms)))
+        return i.value, ms.value
 
     def counts(self) -> np.ndarray:
         out = np.zeros((self.n, self.S1), np.int64)

@@ -278,6 +278,12 @@ cs_status cs_tiling_describe(int32_t index, int32_t* K, int32_t* TY, int32_t* TZ
 cs_status cs_tiling_kind(int32_t index, int32_t* kind, int32_t* brick_planes);
 cs_status cs_set_tiling(cs_sim* sim, int32_t index, uint32_t segment_length);
 cs_status cs_get_tiling(const cs_sim* sim, int32_t* index);
+/* Autotuner: times every compiled variant for this K on the handle's own
+ * lattice (frames_per_trial frames each, from a device copy of the current
+ * state, which is restored afterwards, so the simulation does not advance),
+ * selects the fastest and caches the choice per model shape and device for
+ * the life of the process.  chosen_index / ms_per_frame may be NULL. */
+cs_status cs_autotune(cs_sim* sim, uint32_t frames_per_trial, int32_t* chosen_index, float* ms_per_frame);
 
 /* ---------------- batched ensemble (production path) ---------------- */
 /* Replicates of one model on lattices of uneven sizes, all stepped by one
@@ -297,6 +303,7 @@ cs_status cs_ensemble_step(cs_ensemble* ens, uint32_t n_steps, int32_t batched);
 cs_status cs_ensemble_step_timed(cs_ensemble* ens, uint32_t n_steps, int32_t batched, float* ms);
 cs_status cs_ensemble_set_precision(cs_ensemble* ens, int32_t precision);
 cs_status cs_ensemble_set_tiling(cs_ensemble* ens, int32_t index, uint32_t segment_length);
+cs_status cs_ensemble_autotune(cs_ensemble* ens, uint32_t frames_per_trial, int32_t* chosen_index, float* ms_per_frame);
 /* counts[n_replicates][S+1] */
 cs_status cs_ensemble_get_counts(cs_ensemble* ens, int64_t* counts);
 /* packed slots of all replicates in order, K bytes per voxel */

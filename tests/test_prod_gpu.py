@@ -209,3 +209,22 @@ def test_switching_step_kinds_mid_run_matches_oracle(orc):
     got_s, _, _ = sim.get_lattice()
     assert np.array_equal(got_s.astype(np.uint8), want_s)
     assert np.array_equal(sim.counts(), want_c)
+
+
+def test_autotune_keeps_state_and_results(orc):
+    """The autotuner times every variant on a copy of the live state: the
+    simulation does not advance and the following frames equal the oracle."""
+    mk = lambda: multi_region_model(res=(16, 18, 45), K=16, counts=(90, 70, 50, 40))
+    want_s, want_c, _ = oracle_prod(orc, mk(), 12, seed=5150)
+    sim = mk()
+    sim.prepare_for_gpu(RNG_PHILOX, 0)
+    sim.step_philox(4, 5150)
+    before = sim.get_lattice()[0].copy()
+    idx, ms = sim.autotune(frames_per_trial=2)
+    assert 0 <= idx < len(tiling_variants()) and tiling_variants()[idx][0] == 16 and ms > 0
+    assert sim.get_tiling() == idx
+    assert np.array_equal(sim.get_lattice()[0], before)
+    sim.step_philox(8, 5150)
+    got_s, _, _ = sim.get_lattice()
+    assert np.array_equal(got_s.astype(np.uint8), want_s)
+    assert np.array_equal(sim.counts(), want_c)
