@@ -4,13 +4,14 @@
  * loads or calls this code; only tests/, __graft_entry__.smoke() and the
  * cpu_baseline / --impl reference legs of bench.py do.
  *
- * Parity status: the reference (javirk/cell_simulation) ships no tests, no
- * golden vectors and no CPU path, and its WGSL shaders cannot run in this
- * environment (no Vulkan, no Rust toolchain).  The reference-semantics
- * restatement below is pinned against fixtures produced by a serial
- * interpreter that executes the reference's own shader source
- * (tests/golden/wgsl_interp.py) when those fixtures are present; otherwise
- * parity is unpinned.
+ * Parity status: parity unpinned.  The reference (javirk/cell_simulation)
+ * ships no tests, no golden vectors and no CPU path, and its WGSL shaders
+ * cannot run in this environment (no Vulkan, no Rust toolchain), so the
+ * reference-semantics restatement below follows the shader source as read
+ * (res/shader/rdme.wgsl, cme.wgsl, final_stage.wgsl, random.wgsl,
+ * functions.wgsl) without outputs of the reference to check it against.  Its
+ * own outputs on fixed cases are stored in tests/golden/ (make_golden.py)
+ * and guard it against regressions.
  *
  * Three models live here:
  *   1. ref_semantics.c  — the reference algorithm (res/shader/rdme.wgsl,
