@@ -174,9 +174,30 @@ def c4_ensemble_spec(seed: int = MASTER_SEED, n_rep: int = 512, lo: int = 32, hi
     return res, seeds, mult, init
 
 
+def c5_network(seed: int = MASTER_SEED):
+    """The stiff network of c5: 12 species, 24 first/second-order reactions, rates 1e-3..1e4 /s
+    (second order: the same range per voxel pair)."""
+    rng = np.random.default_rng(np.random.SeedSequence([seed, 5]))
+    return _random_network(rng, 12, 24, (1e-3, 1e4), (1e-3 * 19733.5, 1e4 * 19733.5))
+
+
+def c5_ensemble_template(seed: int = MASTER_SEED, res=(48, 48, 48)) -> Simulation:
+    """The c5 model without particles, as the template of an ensemble of sub-lattices."""
+    D = 1e-12
+    sim = Simulation(_lattice(res, 16, D))
+    sim.set_diffusion_rate("background", D)
+    sim.prepare_regions()
+    names = [f"Q{i}" for i in range(12)]
+    for n in names:
+        sim.add_particle_count(n, "background", 0, True, False)
+    sim.set_diffusion_rate("background", D)
+    for re, pr, k in c5_network(seed):
+        sim.add_reaction([names[a] for a in re], [names[p] for p in pr], k)
+    return sim
+
+
 def c5_stiff(seed: int = MASTER_SEED, res=(192, 192, 192), total_particles: int = 1_000_000) -> Workload:
     """192^3, K=16, 12 species, 24 first/second-order reactions with rates 1e-3..1e4 /s (stiff), D = 1e-12."""
-    rng = np.random.default_rng(np.random.SeedSequence([seed, 5]))
     S, R, D = 12, 24, 1e-12
     sim = Simulation(_lattice(res, 16, D))
     sim.seed_placement(seed + 5)
@@ -186,7 +207,6 @@ def c5_stiff(seed: int = MASTER_SEED, res=(192, 192, 192), total_particles: int 
     for n in names:
         sim.add_particle_count(n, "background", total_particles // S, True, False)
     sim.set_diffusion_rate("background", D)
-    rx = _random_network(rng, S, R, (1e-3, 1e4), (1e-3 * 19733.5, 1e4 * 19733.5))
-    for re, pr, k in rx:
+    for re, pr, k in c5_network(seed):
         sim.add_reaction([names[a] for a in re], [names[p] for p in pr], k)
     return Workload(f"c5_stiff_{res[0]}x{res[1]}x{res[2]}_K16", sim, 100, 16, tuple(res))

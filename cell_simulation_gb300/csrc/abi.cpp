@@ -2,8 +2,10 @@
 // Every function converts C++ exceptions into a cs_status and a thread-local
 // message; nothing throws across the ABI.
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <memory>
 #include <new>
 #include <sstream>
 #include <string>
@@ -662,3 +664,222 @@ cs_status cs_ref_frame_noalloc(const cs_ref_frame_noalloc_args* args) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ checkpoints and views
+namespace {
+
+// Little-endian binary stream of a checkpoint file.
+struct CkWriter {
+    std::FILE* f;
+    void raw(const void* p, size_t n) {
+        if (n && std::fwrite(p, 1, n, f) != n) throw Error(CS_ERR_INVALID_ARG, "checkpoint write failed");
+    }
+    template <class T>
+    void pod(const T& v) { raw(&v, sizeof(T)); }
+    void str(const std::string& s) {
+        pod<uint64_t>(s.size());
+        raw(s.data(), s.size());
+    }
+    template <class T>
+    void vec(const std::vector<T>& v) {
+        pod<uint64_t>(v.size());
+        raw(v.data(), v.size() * sizeof(T));
+    }
+};
+
+struct CkReader {
+    std::FILE* f;
+    void raw(void* p, size_t n) {
+        if (n && std::fread(p, 1, n, f) != n) throw Error(CS_ERR_INVALID_ARG, "checkpoint file is truncated");
+    }
+    template <class T>
+    T pod() {
+        T v;
+        raw(&v, sizeof(T));
+        return v;
+    }
+    uint64_t count(uint64_t limit) {
+        uint64_t n = pod<uint64_t>();
+        if (n > limit) throw Error(CS_ERR_INVALID_ARG, "checkpoint file is corrupt (array length)");
+        return n;
+    }
+    std::string str() {
+        std::string s(count(1u << 20), '\0');
+        raw(&s[0], s.size());
+        return s;
+    }
+    template <class T>
+    std::vector<T> vec(uint64_t limit) {
+        std::vector<T> v(count(limit));
+        raw(v.data(), v.size() * sizeof(T));
+        return v;
+    }
+};
+
+constexpr char kCkMagic[8] = {'C', 'S', 'I', 'M', 'C', 'K', 'P', 'T'};
+constexpr uint32_t kCkVersion = 1;
+
+}  // namespace
+
+cs_status cs_checkpoint_save(cs_sim* sim, const char* path) {
+    return guarded([&] {
+        need(sim, "sim");
+        need(path, "path");
+        const Model& m = sim->model;
+        const uint64_t V = m.V, S1 = m.S1();
+        // current lattice state: the device's when prepared, else the host model's
+        std::vector<uint32_t> slots(V * m.K), occ(V);
+        std::vector<int32_t> conc(V * S1);
+        std::vector<int64_t> counts(S1);
+        if (sim->ref) {
+            ref_get_lattice(sim->ref.get(), slots.data(), occ.data(), conc.data());
+            ref_get_counts(sim->ref.get(), counts.data());
+        } else if (sim->prod) {
+            prod_get_lattice(sim->prod.get(), m, slots.data(), occ.data(), conc.data());
+            prod_get_counts(sim->prod.get(), counts.data());
+        } else {
+            slots = m.slots;
+            occ = m.occupancy;
+            conc = m.concentrations();
+            for (uint64_t v = 0; v < V; v++)
+                for (uint64_t s = 0; s < S1; s++) counts[s] += conc[v * S1 + s];
+        }
+        std::FILE* f = std::fopen(path, "wb");
+        if (!f) throw Error(CS_ERR_INVALID_ARG, std::string("cannot open checkpoint file for writing: ") + path);
+        std::unique_ptr<std::FILE, int (*)(std::FILE*)> close(f, std::fclose);
+        CkWriter w{f};
+        w.raw(kCkMagic, sizeof(kCkMagic));
+        w.pod(kCkVersion);
+        for (int a = 0; a < 3; a++) w.pod(m.dims[a]);
+        for (int a = 0; a < 3; a++) w.pod(m.res[a]);
+        w.pod(m.tau);
+        w.pod(m.lambda);
+        w.pod(m.K);
+        w.pod(m.nr);
+        w.pod(m.np);
+        w.pod(m.n_species);
+        w.pod(m.n_reactions);
+        w.pod<uint64_t>(m.particle_names.size());
+        for (const auto& n : m.particle_names) w.str(n);
+        w.vec(m.logging);
+        w.pod<uint64_t>(m.types.size());
+        for (const RegionEntry& e : m.types) {
+            w.pod(e.type);
+            w.str(e.name);
+            w.raw(e.p0, sizeof(e.p0));
+            w.raw(e.pf, sizeof(e.pf));
+            w.raw(e.center, sizeof(e.center));
+            w.raw(e.direction, sizeof(e.direction));
+            w.pod(e.radius);
+        }
+        w.vec(m.volumes);
+        w.pod<uint8_t>(m.regions_prepared ? 1 : 0);
+        w.vec(m.regions);
+        w.vec(m.diffusion);
+        w.vec(m.stoich);
+        w.vec(m.reactants);
+        w.vec(m.rates);
+        w.vec(m.reservoir);
+        w.raw(m.rng.s, sizeof(m.rng.s));
+        w.pod(sim->mode);
+        w.pod(sim->precision);
+        w.pod(sim->frame);
+        w.vec(slots);
+        w.vec(occ);
+        w.vec(conc);
+        w.vec(counts);
+    });
+}
+
+cs_status cs_checkpoint_load(const char* path, int32_t device, cs_sim** out) {
+    return guarded([&] {
+        need(path, "path");
+        need(out, "out");
+        *out = nullptr;
+        std::FILE* f = std::fopen(path, "rb");
+        if (!f) throw Error(CS_ERR_NOT_FOUND, std::string("cannot open checkpoint file: ") + path);
+        std::unique_ptr<std::FILE, int (*)(std::FILE*)> close(f, std::fclose);
+        CkReader r{f};
+        char magic[8];
+        r.raw(magic, sizeof(magic));
+        if (std::memcmp(magic, kCkMagic, sizeof(magic)) != 0) throw Error(CS_ERR_INVALID_ARG, "not a libcellsim checkpoint");
+        if (r.pod<uint32_t>() != kCkVersion) throw Error(CS_ERR_INVALID_ARG, "unsupported checkpoint version");
+        cs_lattice_params p{};
+        for (int a = 0; a < 3; a++) p.dims[a] = r.pod<float>();
+        for (int a = 0; a < 3; a++) p.res[a] = r.pod<uint32_t>();
+        p.tau = r.pod<float>();
+        p.lambda = r.pod<float>();
+        p.max_particles_site = r.pod<uint32_t>();
+        std::unique_ptr<cs_sim> s(new_sim());
+        Model& m = s->model;
+        m.init(p);
+        const uint64_t V = m.V, lim = (1ull << 40);
+        m.nr = r.pod<uint32_t>();
+        m.np = r.pod<uint32_t>();
+        m.n_species = r.pod<uint32_t>();
+        m.n_reactions = r.pod<uint32_t>();
+        m.particle_names.resize(r.count(1u << 16));
+        for (auto& n : m.particle_names) n = r.str();
+        m.logging = r.vec<uint32_t>(1u << 16);
+        m.types.resize(r.count(1u << 16));
+        for (RegionEntry& e : m.types) {
+            e.type = r.pod<int32_t>();
+            e.name = r.str();
+            r.raw(e.p0, sizeof(e.p0));
+            r.raw(e.pf, sizeof(e.pf));
+            r.raw(e.center, sizeof(e.center));
+            r.raw(e.direction, sizeof(e.direction));
+            e.radius = r.pod<float>();
+        }
+        m.volumes = r.vec<uint32_t>(1u << 16);
+        const bool prepared = r.pod<uint8_t>() != 0;
+        m.regions = r.vec<uint32_t>(lim);
+        m.diffusion = r.vec<float>(lim);
+        m.stoich = r.vec<int32_t>(lim);
+        m.reactants = r.vec<uint32_t>(lim);
+        m.rates = r.vec<float>(lim);
+        m.reservoir = r.vec<uint32_t>(lim);
+        r.raw(m.rng.s, sizeof(m.rng.s));
+        const int32_t mode = r.pod<int32_t>();
+        s->precision = r.pod<int32_t>();
+        const uint64_t frame = r.pod<uint64_t>();
+        m.slots = r.vec<uint32_t>(lim);
+        m.occupancy = r.vec<uint32_t>(lim);
+        m.conc = r.vec<int32_t>(lim);
+        const std::vector<int64_t> counts = r.vec<int64_t>(1u << 16);
+        const uint64_t S1 = m.S1();
+        if (m.regions.size() != V || m.reservoir.size() != V || m.slots.size() != V * m.K || m.occupancy.size() != V ||
+            m.conc.size() != V * S1 || counts.size() != S1 || m.particle_names.size() != S1 ||
+            m.diffusion.size() != (size_t)m.nr * m.nr * m.np || m.rates.size() != m.n_reactions + 1u)
+            throw Error(CS_ERR_INVALID_ARG, "checkpoint file is inconsistent");
+        m.conc_explicit = true;
+        m.index_buffer.clear();
+        if (prepared) {
+            for (uint64_t v = 0; v < V; v++) m.index_buffer[m.regions[v]].push_back((uint32_t)v);
+            m.regions_prepared = true;
+        }
+        if (mode == CS_RNG_REFERENCE) {
+            s->ref.reset(ref_create(m, device));
+            ref_set_counts(s->ref.get(), counts.data());
+        } else if (mode == CS_RNG_PHILOX) {
+            s->prod.reset(prod_create(m, device));
+            prod_set_counts(s->prod.get(), counts.data());
+        }
+        s->mode = mode;
+        s->device = device;
+        s->frame = frame;
+        *out = s.release();
+    });
+}
+
+cs_status cs_render_view(cs_sim* sim, int32_t view, int32_t slice_axis, uint32_t slice, float* out_host, void* out_device) {
+    return guarded([&] {
+        need(sim, "sim");
+        if (!out_host && !out_device) throw Error(CS_ERR_INVALID_ARG, "out_host or out_device is required");
+        if (view < 0 || view > 2) throw Error(CS_ERR_INVALID_ARG, "view must be 0 (species), 1 (regions) or 2 (reservoirs)");
+        if (slice_axis < 0 || slice_axis > 2) throw Error(CS_ERR_INVALID_ARG, "slice_axis must be 0, 1 or 2");
+        if (sim->ref) ref_render_view(sim->ref.get(), view, slice_axis, slice, out_host, out_device);
+        else if (sim->prod) prod_render_view(sim->prod.get(), view, slice_axis, slice, out_host, out_device);
+        else throw Error(CS_ERR_STATE, "cs_render_view needs cs_prepare_for_gpu");
+    });
+}

@@ -36,6 +36,7 @@
 #include "brick_kernel.cuh"
 #include "prod_common.cuh"
 #include "prod_kernel.cuh"
+#include "views.cuh"
 
 namespace cellsim {
 
@@ -119,7 +120,8 @@ struct DeviceProd {
     DevBuf<unsigned long long> rmask;
     DevBuf<float> one;
     DevBuf<uint32_t> quiet;
-    DevBuf<WorkItem> spill;  // bricks handed from the brick pass to the tile pipeline
+    DevBuf<WorkItem> spill;  // bricks handed from the brick pass to the second pass
+    DevBuf<unsigned long long> sample_ring;  // species counts at the sample frames of one cs_step_philox
     std::vector<float> h_rate;
     std::vector<uint8_t> h_rre;
     std::vector<unsigned long long> h_rmask;
@@ -725,18 +727,29 @@ void prod_step(DeviceProd* d, uint32_t n_steps, uint64_t seed, int precision, ui
     if (write_freq)
         for (uint64_t f = frame0; f < frame0 + n_steps; f++)
             if (f > 0 && f % write_freq == 0) sample_frames.push_back(f);
+    // Samples are device-to-device copies of the counts into a ring, read back
+    // once at the end: the frames in between are enqueued without host waits.
     uint64_t f = frame0, end = frame0 + n_steps;
-    std::vector<unsigned long long> snap;
-    std::vector<std::vector<unsigned long long>> taken;
-    for (uint64_t sf : sample_frames) {
-        run_frames(d, (uint32_t)(sf - f), f, true);
-        f = sf;
-        std::vector<unsigned long long> h(d->S1);
-        CS_CUDA(cudaMemcpyAsync(h.data(), d->counts.p, d->S1 * 8, cudaMemcpyDeviceToHost, d->stream));
-        CS_CUDA(cudaStreamSynchronize(d->stream));
-        for (uint32_t sp : logging) samples.push_back(cs_stat_sample{sp, (int32_t)(long long)h[sp], (uint32_t)sf});
+    const uint32_t f32 = (uint32_t)frame0;
+    CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, &f32, 4, cudaMemcpyHostToDevice, d->stream));
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    if (!sample_frames.empty() && d->sample_ring.n < sample_frames.size() * d->S1)
+        d->sample_ring.alloc(sample_frames.size() * d->S1);
+    for (size_t i = 0; i < sample_frames.size(); i++) {
+        run_frames_nosync(d, (uint32_t)(sample_frames[i] - f), true);
+        f = sample_frames[i];
+        CS_CUDA(cudaMemcpyAsync(d->sample_ring.p + i * d->S1, d->counts.p, d->S1 * 8, cudaMemcpyDeviceToDevice,
+                                d->stream));
     }
-    run_frames(d, (uint32_t)(end - f), f, true);
+    run_frames_nosync(d, (uint32_t)(end - f), true);
+    if (!sample_frames.empty()) {
+        std::vector<unsigned long long> h(sample_frames.size() * d->S1);
+        CS_CUDA(cudaMemcpyAsync(h.data(), d->sample_ring.p, h.size() * 8, cudaMemcpyDeviceToHost, d->stream));
+        CS_CUDA(cudaStreamSynchronize(d->stream));
+        for (size_t i = 0; i < sample_frames.size(); i++)
+            for (uint32_t sp : logging)
+                samples.push_back(cs_stat_sample{sp, (int32_t)(long long)h[i * d->S1 + sp], (uint32_t)sample_frames[i]});
+    }
 }
 
 void prod_get_counts(DeviceProd* d, int64_t* counts) {
@@ -745,6 +758,42 @@ void prod_get_counts(DeviceProd* d, int64_t* counts) {
     CS_CUDA(cudaMemcpyAsync(h.data(), d->counts.p, h.size() * 8, cudaMemcpyDeviceToHost, d->stream));
     CS_CUDA(cudaStreamSynchronize(d->stream));
     for (size_t i = 0; i < h.size(); i++) counts[i] = (int64_t)h[i];
+}
+
+void prod_set_counts(DeviceProd* d, const int64_t* counts) {
+    DeviceGuard g(d->device);
+    std::vector<unsigned long long> h((size_t)d->n_rep * d->S1);
+    for (size_t i = 0; i < h.size(); i++) h[i] = (unsigned long long)counts[i];
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    CS_CUDA(cudaMemcpy(d->counts.p, h.data(), h.size() * 8, cudaMemcpyHostToDevice));
+}
+
+// Replicate 0's view (the single lattice of a cs_sim).
+void prod_render_view(DeviceProd* d, int32_t view, int32_t slice_axis, uint32_t slice, float* out_host, void* out_device) {
+    DeviceGuard g(d->device);
+    DevBuf<float> tmp;
+    float* out_dev = static_cast<float*>(out_device);
+    const uint64_t V = (uint64_t)d->h_reps[0].X * d->h_reps[0].Y * d->h_reps[0].Z;
+    if (!out_dev) {
+        tmp.alloc(V);
+        out_dev = tmp.p;
+    }
+    const RepDesc& r = d->h_reps[0];
+    ViewParams v{};
+    v.slots = d->slots[d->cur].p;
+    v.K = d->K;
+    v.X = r.X; v.Y = r.Y; v.Z = r.Z;
+    v.region_pad = (r.flags & 1u) ? nullptr : d->region_pad.p;
+    v.Zr = r.Zr;
+    v.reservoir = d->reservoir.n ? d->reservoir.p : nullptr;
+    v.view = view;
+    v.slice_axis = slice_axis;
+    v.slice = slice;
+    v.out = out_dev;
+    render_view_kernel<<<1024, 256, 0, d->stream>>>(v);
+    CS_LAUNCH_CHECK();
+    if (!out_device) CS_CUDA(cudaMemcpyAsync(out_host, out_dev, V * sizeof(float), cudaMemcpyDeviceToHost, d->stream));
+    CS_CUDA(cudaStreamSynchronize(d->stream));
 }
 
 void prod_get_diag(DeviceProd* d, uint32_t* diag, uint32_t n) {

@@ -32,6 +32,7 @@
 
 #include "cuda_check.h"
 #include "devmath.cuh"
+#include "views.cuh"
 #include "internal.h"
 
 namespace cellsim {
@@ -399,11 +400,6 @@ DeviceRef* ref_create(const Model& m, int device) {
     CS_CUDA(cudaMemset(d->flag.p, 0, sizeof(uint32_t)));
     std::vector<int32_t> conc = m.concentrations();
     ref_set_lattice(d.get(), m.slots.data(), m.occupancy.data(), conc.data());
-    // create_statistics, src/simulation.rs:361-388: sum of the concentrations
-    std::vector<int32_t> st(p.S1, 0);
-    for (uint64_t v = 0; v < m.V; v++)
-        for (uint32_t s = 0; s < p.S1; s++) st[s] = (int32_t)((uint32_t)st[s] + (uint32_t)conc[v * p.S1 + s]);
-    CS_CUDA(cudaMemcpy(d->stat.p, st.data(), p.S1 * sizeof(int32_t), cudaMemcpyHostToDevice));
     return d.release();
 }
 
@@ -427,6 +423,43 @@ void ref_set_lattice(DeviceRef* d, const uint32_t* slots, const uint32_t* occ, c
     CS_CUDA(cudaMemcpy(d->slots[0].p, s8.data(), VK, cudaMemcpyHostToDevice));
     CS_CUDA(cudaMemcpy(d->occ[0].p, occ, d->p.V * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CS_CUDA(cudaMemcpy(d->conc[0].p, conc, VS * sizeof(int32_t), cudaMemcpyHostToDevice));
+    // create_statistics, src/simulation.rs:361-388: the counts restart from the sum of the concentrations
+    std::vector<int32_t> st(d->p.S1, 0);
+    for (uint64_t v = 0; v < d->p.V; v++)
+        for (uint32_t s = 0; s < d->p.S1; s++) st[s] = (int32_t)((uint32_t)st[s] + (uint32_t)conc[v * d->p.S1 + s]);
+    CS_CUDA(cudaMemcpy(d->stat.p, st.data(), d->p.S1 * sizeof(int32_t), cudaMemcpyHostToDevice));
+}
+
+void ref_set_counts(DeviceRef* d, const int64_t* counts) {
+    DeviceGuard g(d->device);
+    std::vector<int32_t> st(d->p.S1);
+    for (uint32_t s = 0; s < d->p.S1; s++) st[s] = (int32_t)counts[s];
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    CS_CUDA(cudaMemcpy(d->stat.p, st.data(), d->p.S1 * sizeof(int32_t), cudaMemcpyHostToDevice));
+}
+
+void ref_render_view(DeviceRef* d, int32_t view, int32_t slice_axis, uint32_t slice, float* out_host, void* out_device) {
+    DeviceGuard g(d->device);
+    DevBuf<float> tmp;
+    float* out_dev = static_cast<float*>(out_device);
+    if (!out_dev) {
+        tmp.alloc(d->p.V);
+        out_dev = tmp.p;
+    }
+    ViewParams v{};
+    v.slots = d->slots[d->cur].p;
+    v.K = d->p.K;
+    v.X = d->p.X; v.Y = d->p.Y; v.Z = d->p.Z;
+    v.region_id = d->regions.p;
+    v.reservoir = d->reservoir.p;
+    v.view = view;
+    v.slice_axis = slice_axis;
+    v.slice = slice;
+    v.out = out_dev;
+    render_view_kernel<<<1024, 256, 0, d->stream>>>(v);
+    CS_LAUNCH_CHECK();
+    if (!out_device) CS_CUDA(cudaMemcpyAsync(out_host, out_dev, d->p.V * sizeof(float), cudaMemcpyDeviceToHost, d->stream));
+    CS_CUDA(cudaStreamSynchronize(d->stream));
 }
 
 void ref_get_lattice(DeviceRef* d, uint32_t* slots, uint32_t* occ, int32_t* conc) {

@@ -144,6 +144,8 @@ void ref_get_lattice(DeviceRef* d, uint32_t* slots, uint32_t* occ, int32_t* conc
 void ref_set_lattice(DeviceRef* d, const uint32_t* slots, const uint32_t* occ, const int32_t* conc);
 void ref_get_diag(DeviceRef* d, uint32_t* diag, uint32_t n);
 void ref_sync(DeviceRef* d);
+void ref_set_counts(DeviceRef* d, const int64_t* counts);
+void ref_render_view(DeviceRef* d, int32_t view, int32_t slice_axis, uint32_t slice, float* out_host, void* out_device);
 
 // device_prod.cu
 DeviceProd* prod_create(const Model& m, int device);
@@ -169,6 +171,9 @@ void prod_set_tiling(DeviceProd* d, int cfg_index, uint32_t seg_len);
 int prod_tiling_count();
 void prod_tiling_desc(int i, int* K, int* TY, int* TZ, int* NT);
 void prod_tiling_kind(int i, int* kind, int* BX);
+void prod_set_counts(DeviceProd* d, const int64_t* counts);
+// out_device (V floats, caller-owned device memory) or, when null, out_host
+void prod_render_view(DeviceProd* d, int32_t view, int32_t slice_axis, uint32_t slice, float* out_host, void* out_device);
 int prod_tiling_current(const DeviceProd* d);
 void prod_seed(DeviceProd* d, uint64_t seed);
 float prod_time_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched);

@@ -108,6 +108,9 @@ SIGNATURES = {
     "cs_tiling_describe": (st, [C.c_int32, i32p, i32p, i32p, i32p]),
     "cs_tiling_kind": (st, [C.c_int32, i32p, i32p]),
     "cs_autotune": (st, [P, C.c_uint32, i32p, C.POINTER(C.c_float)]),
+    "cs_checkpoint_save": (st, [P, C.c_char_p]),
+    "cs_checkpoint_load": (st, [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "cs_render_view": (st, [P, C.c_int32, C.c_int32, C.c_uint32, C.POINTER(C.c_float), C.c_void_p]),
     "cs_ensemble_autotune": (st, [P, C.c_uint32, i32p, C.POINTER(C.c_float)]),
     "cs_set_tiling": (st, [P, C.c_int32, C.c_uint32]),
     "cs_get_tiling": (st, [P, i32p]),

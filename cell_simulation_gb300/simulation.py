@@ -284,6 +284,26 @@ class Simulation:
     def set_tiling(self, index: int, segment_length: int = 0) -> None:
         N.check(self._lib.cs_set_tiling(self._h, index, segment_length))
 
+    def save_checkpoint(self, path) -> None:
+        """Full state to a file (cs_checkpoint_save)."""
+        N.check(self._lib.cs_checkpoint_save(self._h, str(path).encode()))
+
+    @classmethod
+    def load_checkpoint(cls, path, device: int = 0) -> "Simulation":
+        """A handle resumed from a checkpoint file (cs_checkpoint_load)."""
+        lib = N.load()
+        h = C.c_void_p()
+        N.check(lib.cs_checkpoint_load(str(path).encode(), device, C.byref(h)))
+        return cls(_handle=h)
+
+    def render_view(self, view: int = 0, slice_axis: int = 0, slice: int = 0) -> np.ndarray:
+        """The final_stage.wgsl views as a float32 (X, Y, Z) volume: 0 majority
+        species, 1 regions, 2 reservoirs, each / 255 (cs_render_view)."""
+        X, Y, Z = self.shape
+        out = np.zeros((X, Y, Z), np.float32)
+        N.check(self._lib.cs_render_view(self._h, view, slice_axis, slice, N.ptr(out, C.c_float), None))
+        return out
+
     def autotune(self, frames_per_trial: int = 10) -> tuple[int, float]:
         """Time every compiled variant on this lattice (state restored afterwards)
         and keep the fastest: (chosen variant index, ms per frame)."""

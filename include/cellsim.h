@@ -285,6 +285,28 @@ cs_status cs_get_tiling(const cs_sim* sim, int32_t* index);
  * the life of the process.  chosen_index / ms_per_frame may be NULL. */
 cs_status cs_autotune(cs_sim* sim, uint32_t frames_per_trial, int32_t* chosen_index, float* ms_per_frame);
 
+/* ---------------- checkpoint / resume ---------------- */
+/* Writes the full state of a handle to a file: lattice parameters, model
+ * tables, names and regions, the placement RNG, the current lattice (slots,
+ * occupancy, concentrations) and species counts, the frame number, the RNG
+ * mode and the precision.  Resuming with cs_checkpoint_load and stepping
+ * continues bit for bit as the saved handle would (the Philox seed is passed
+ * to cs_step_philox as before).  No reference counterpart (the reference keeps
+ * its state only in wgpu buffers, src/simulation.rs:29-46). */
+cs_status cs_checkpoint_save(cs_sim* sim, const char* path);
+/* Creates a handle from a checkpoint file; a handle saved after
+ * cs_prepare_for_gpu is prepared again on `device`. */
+cs_status cs_checkpoint_load(const char* path, int32_t device, cs_sim** out);
+
+/* ---------------- headless visualisation ---------------- */
+/* The views of final_stage.wgsl:35-68 (the storage texture of the reference's
+ * renderer) as V floats in lattice order: view 0 = majority species / 255,
+ * 1 = region id / 255, 2 = reservoir species / 255; voxels with
+ * res[slice_axis] - coord[slice_axis] < slice are 0.  Written to out_device
+ * (caller-owned device memory, V floats) when it is not NULL, else copied to
+ * out_host.  Needs cs_prepare_for_gpu. */
+cs_status cs_render_view(cs_sim* sim, int32_t view, int32_t slice_axis, uint32_t slice, float* out_host, void* out_device);
+
 /* ---------------- batched ensemble (production path) ---------------- */
 /* Replicates of one model on lattices of uneven sizes, all stepped by one
  * persistent launch per frame over a (replicate, tile) work queue.  The

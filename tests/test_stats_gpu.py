@@ -131,3 +131,33 @@ def test_first_passage_time():
     p, z, pv = compare("first passage C>=10", fpt_lat, fpt_ssa)
     assert reached.mean() > 0.95 and r2.mean() > 0.95
     assert p > P_MIN and abs(z) < 4
+
+
+def test_c5_precision_stress_fp32_vs_fp64():
+    """The stiff c5 network (rates 1e-3..1e4 /s, k tau up to 1.7) on 1000
+    replicates of 48^3: species counts after 150 frames with FP32 propensities
+    and selection, with FP64 selection always, and with the mixed rule (FP64
+    selection when a voxel's propensities span more than 6 decades) are one
+    distribution.  Two-sample KS per species, Bonferroni over the 12 species."""
+    sim = configs.c5_ensemble_template(res=(48, 48, 48))
+    init = [0] + [1302] * 12
+    n_steps = 150
+    runs = {}
+    for prec, seed0 in ((PREC_FP32, 50_000), (PREC_FP64, 60_000), (PREC_MIXED, 70_000)):
+        n = N_REP
+        resv = np.tile(np.array([48, 48, 48], np.uint32), (n, 1))
+        seeds = (seed0 + np.arange(n)).astype(np.uint64)
+        ens = Ensemble(sim, resv, seeds, np.ones(n, np.float32), np.asarray(init, np.uint32))
+        ens.set_precision(prec)
+        ens.step(n_steps)
+        runs[prec] = (ens.counts(), ens.diagnostics())
+        ens.close()
+    fp32, fp64, mixed = runs[PREC_FP32][0], runs[PREC_FP64][0], runs[PREC_MIXED][0]
+    assert runs[PREC_FP64][1][3] > 0  # FP64 selections counted
+    assert runs[PREC_MIXED][1][3] > 0  # the 6-decade rule engages on this network
+    worst = 1.0
+    for s in range(1, 13):
+        p1, _, _ = compare(f"c5 Q{s - 1} fp32 vs fp64", fp32[:, s].astype(float), fp64[:, s].astype(float))
+        p2, _, _ = compare(f"c5 Q{s - 1} mixed vs fp64", mixed[:, s].astype(float), fp64[:, s].astype(float))
+        worst = min(worst, p1, p2)
+    assert worst > P_MIN / 24
