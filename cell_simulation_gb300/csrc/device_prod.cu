@@ -86,11 +86,15 @@ static const std::vector<KernelCfg>& all_cfgs() {
         tile_cfg<16, 8, 32, 256, 3>(),  tile_cfg<16, 4, 64, 256, 3>(), tile_cfg<16, 16, 32, 256, 1>(),
         tile_cfg<16, 8, 64, 256, 1>(),  tile_cfg<8, 8, 32, 256, 3>(),  tile_cfg<8, 4, 64, 256, 3>(),
         tile_cfg<8, 16, 32, 256, 2>(),  tile_cfg<8, 8, 64, 256, 2>(),
-        // sparse bricks whose crowded bricks go to the dense 2-plane pass of the same K (entries 10, 11)
+        // sparse bricks whose crowded bricks go to the dense 2-plane pass of the same K (entries 10,
+        // 11).  With NT = 32 BX one warp owns each interior plane and runs its X/Y/Z sweeps without
+        // CTA barriers; otherwise every phase runs CTA-wide.
         brick_cfg<16, 8, 8, 256, 3, 768, 768, 768>(10, 4), brick_cfg<8, 8, 8, 256, 3, 768, 768, 768>(11, 4),
         dense_brick_cfg<16, 2, 8, 256, 3>(), dense_brick_cfg<8, 2, 8, 256, 3>(),
-        brick_cfg<16, 8, 8, 256, 4, 512, 512, 512>(10, 4), brick_cfg<16, 4, 8, 128, 6, 384, 384, 384>(10, 2),
-        brick_cfg<16, 8, 8, 192, 4, 544, 544, 544>(10, 4),
+        brick_cfg<16, 8, 8, 192, 4, 544, 544, 544>(10, 4), brick_cfg<16, 4, 8, 128, 5, 448, 448, 448>(10, 2),
+        brick_cfg<16, 6, 8, 192, 4, 560, 560, 560>(10, 3), brick_cfg<8, 8, 8, 192, 4, 544, 544, 544>(11, 4),
+        // small pool 1: bricks overflow after other warps have stored their planes (exercises that route)
+        brick_cfg<16, 8, 8, 256, 3, 768, 128, 768>(10, 4),
     };
     return v;
 }
