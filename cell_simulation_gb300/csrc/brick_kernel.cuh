@@ -260,6 +260,7 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
             const bool all_react = zero_order || resv != nullptr;
             const uint32_t YZ = (uint32_t)Y * (uint32_t)Z;
             const uint32_t* quiet = P.T.quiet + (size_t)rd.counts_index * S1 * P.T.QS;
+            const float* one_rep = P.T.one + (size_t)rd.counts_index * S1 * 3;
             auto lin = [&](int x, int y, int z) -> uint32_t {
                 return ((uint32_t)x * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)z;
             };
@@ -520,7 +521,8 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                     else if (!WP && (PB1[j1] & bc)) w3 = W13[rank(S1m[j1], RB1[j1], c)];
                     else if (!WP && (PB2[jj] & bc)) w3 = W23[e2];
                     else w3 = d_philox(v, frame, 0u, 0u, k0, k1).w;
-                    const bool calm = rv == 0u && !zero_order && calm_voxel<K>(r3, w3, quiet, P.T.QS);
+                    const bool calm = rv == 0u && !zero_order &&
+                                      calm_voxel<K>(r3, w3, quiet, P.T.QS, one_rep, P.T.g23 + 2 * rd.counts_index, P.T.tau);
                     if (!calm)
                         react_voxel<K>(r3, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, P.T, s_delta, s_bdiag,
                                        w3);

@@ -124,6 +124,7 @@ struct DeviceProd {
     DevBuf<unsigned long long> rmask;
     DevBuf<float> one;
     DevBuf<uint32_t> quiet;
+    DevBuf<float> g23;
     DevBuf<WorkItem> spill;  // bricks handed from the brick pass to the second pass
     DevBuf<unsigned long long> sample_ring;  // species counts at the sample frames of one cs_step_philox
     std::vector<float> h_rate;
@@ -322,6 +323,24 @@ static void build_one_table(DeviceProd* d) {
         }
     }
     d->T.QS = QS;
+    // summed second- and third-order rates per replicate (bound of fuller voxels' a0)
+    std::vector<float> g23((size_t)d->n_rep * 2, 0.0f);
+    for (uint32_t ri = 0; ri < d->n_rep; ri++) {
+        double g2 = 0.0, g3 = 0.0;
+        for (uint32_t r = 0; r < d->R; r++) {
+            int order = 0;
+            for (int j = 0; j < 3; j++) order += d->h_rre[3 * r + j] != 0;
+            const double k = (double)d->h_rate[r] * (double)d->h_reps[ri].rate_mult;
+            if (order == 2) g2 += k;
+            if (order == 3) g3 += k;
+        }
+        // rounded up to binary32 so that the device bound never falls below the exact one
+        g23[2 * ri] = std::nextafter((float)g2, INFINITY);
+        g23[2 * ri + 1] = g3 > 0.0 ? std::nextafter((float)g3, INFINITY) : 0.0f;
+    }
+    d->g23.alloc(g23.size());
+    CS_CUDA(cudaMemcpy(d->g23.p, g23.data(), g23.size() * 4, cudaMemcpyHostToDevice));
+    d->T.g23 = d->g23.p;
     d->quiet.alloc(quiet.size());
     CS_CUDA(cudaMemcpy(d->quiet.p, quiet.data(), quiet.size() * 4, cudaMemcpyHostToDevice));
     d->T.quiet = d->quiet.p;

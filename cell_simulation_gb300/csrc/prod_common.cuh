@@ -79,6 +79,8 @@ struct ProdTables {
                                       // species p (q = 0), or one of p and one of q, has no reaction event
                                       // in the frame when (B(v,0)[3] >> 8) + 1 <= quiet[p][q]
     uint32_t QS;                      // S1 when two-particle entries are tabulated, else 1
+    const float* g23;                 // [n_rep][2]: summed second- and third-order rates (times the
+                                      // replicate's multiplier), for the propensity bound of fuller voxels
 };
 
 
@@ -149,13 +151,31 @@ __device__ __forceinline__ uint32_t vox_count(const Vox<K>& c, uint32_t q) {
 }
 
 // True when the first reaction event of a voxel with content c (no
-// reservoir, no zero-order reaction) certainly falls beyond tau.
+// reservoir, no zero-order reaction) certainly falls beyond tau.  One or two
+// particles: the tabulated bound of the exact a0.  More: a0 is at most
+// sum_s a1(q_s) + n(n-1) G2 + n(n-1)(n-2) G3 (first-order propensities of the
+// particles, every second- and third-order rate times the largest possible
+// falling factorial), and a draw m <= exp(-bound tau (1 + 2^-10)) 2^24 (1 - 2^-20)
+// gives dt > tau; the margins cover the binary32 sums and the portable expf.
 template <int K>
-__device__ __forceinline__ bool calm_voxel(const Vox<K>& c, uint32_t w3, const uint32_t* quiet_rep, uint32_t QS) {
+__device__ __forceinline__ bool calm_voxel(const Vox<K>& c, uint32_t w3, const uint32_t* quiet_rep, uint32_t QS,
+                                           const float* one_rep, const float* g23, float tau) {
     const uint32_t n = vox_n<K>(c);
-    if (n == 0u || n > 2u || (n == 2u && QS == 1u)) return false;
-    const uint32_t p = vox_get<K>(c, 0), q = n == 2u ? vox_get<K>(c, 1) : 0u;
-    return (w3 >> 8) + 1u <= quiet_rep[p * QS + q];
+    if (n == 0u) return false;
+    const uint32_t m = (w3 >> 8) + 1u;
+    if (n == 1u || (n == 2u && QS != 1u)) {
+        const uint32_t p = vox_get<K>(c, 0), q = n == 2u ? vox_get<K>(c, 1) : 0u;
+        return m <= quiet_rep[p * QS + q];
+    }
+    float a = 0.0f;
+    for (uint32_t s = 0; s < n; s++) a = __fadd_rn(a, one_rep[vox_get<K>(c, s) * 3]);
+    const float nn = (float)(n * (n - 1u)), nnn = (float)(n * (n - 1u) * (n - 2u));
+    a = __fadd_rn(a, __fadd_rn(__fmul_rn(nn, g23[0]), __fmul_rn(nnn, g23[1])));
+    const float x = __fmul_rn(__fmul_rn(a, tau), 1.0009765625f);  // 1 + 2^-10
+    if (!(x >= 0.0f)) return false;
+    if (x > 20.0f) return false;
+    const float lim = __fmul_rn(__fmul_rn(d_expf(-x), 16777216.0f), 0.99999904632568359375f);  // 1 - 2^-20
+    return (float)m <= lim;
 }
 
 // Keep the c lowest set bits of m.
