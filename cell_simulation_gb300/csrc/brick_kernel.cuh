@@ -318,6 +318,25 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                 }
             };
 
+            // the next item's box masks, by the highest threads, and an L2 prefetch of the slots of
+            // its occupied voxels (called after a barrier that follows stage_item, which loads
+            // s_nwi / s_nrd)
+            auto stage_masks = [&]() {
+                if (sub != 0u || s_next >= n_items) return;
+                for (int i = NT - 1 - tid; i < NROW0; i += NT) {
+                    const uint64_t m = box_mask(s_nwi, s_nrd, i);
+                    nocc[i] = m;
+                    if (m) {
+                        const int p = i / WY, r = i - p * WY;
+                        const uint64_t vrow = s_nrd.base + ((uint64_t)((int)s_nwi.x0 - 1 + p) * s_nrd.Y +
+                                                            (uint64_t)((int)s_nwi.y0 - 1 + r)) * s_nrd.Z;
+                        for (uint64_t b = m; b; b &= b - 1ull)
+                            prefetch_l2(P.src + (vrow + (uint64_t)((int)s_nwi.z0 - 1 + __ffsll((long long)b) - 1)) * K);
+                    }
+                }
+                if (tid == 0) s_staged = s_next;
+            };
+
             // ---------------- L: box occupancy from the bitmap ----------------
             if (!uniform) {
                 for (int c = tid; c < NCH; c += NT) {
@@ -352,6 +371,24 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                 spill();
                 break;
             }
+            if (top[0] == 0u && !all_react) {
+                // Empty box: no particle can reach the interior and no reaction can fire, so the
+                // interior ends the frame empty.  Only the destination's stale voxels need zeros.
+                for (int j = w; j < NROW2; j += NW) {
+                    const int pi = j / BY + 1, r = j - (pi - 1) * BY + 1;
+                    uint32_t oldw = 0u;
+                    if (pi <= np && r <= ny && lane == 0) oldw = P.odst[orow(pi, r)];
+                    oldw = __shfl_sync(0xffffffffu, oldw, 0);
+                    if ((oldw >> lane) & 1u)
+                        st_vox_g<K>(dst + (uint64_t)lin(x0 - 1 + pi, y0 - 1 + r, z0 + lane) * K, vox_zero<K>());
+                    if (lane == 0) NEWW[j] = 0u;
+                }
+                if (sub == 0u) stage_item(s_next);
+                __syncthreads();
+                stage_masks();
+                done = true;
+                break;
+            }
 
             // ---------------- A: x-decisions of the occupied box voxels ----------------
             {
@@ -384,24 +421,6 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
             }
             if (sub == 0u) stage_item(s_next);
             __syncthreads();
-
-            // the next item's box masks, by the highest threads, and an L2 prefetch of the slots of
-            // its occupied voxels (s_nwi / s_nrd were loaded in phase A)
-            auto stage_masks = [&]() {
-                if (sub != 0u || s_next >= n_items) return;
-                for (int i = NT - 1 - tid; i < NROW0; i += NT) {
-                    const uint64_t m = box_mask(s_nwi, s_nrd, i);
-                    nocc[i] = m;
-                    if (m) {
-                        const int p = i / WY, r = i - p * WY;
-                        const uint64_t vrow = s_nrd.base + ((uint64_t)((int)s_nwi.x0 - 1 + p) * s_nrd.Y +
-                                                            (uint64_t)((int)s_nwi.y0 - 1 + r)) * s_nrd.Z;
-                        for (uint64_t b = m; b; b &= b - 1ull)
-                            prefetch_l2(P.src + (vrow + (uint64_t)((int)s_nwi.z0 - 1 + __ffsll((long long)b) - 1)) * K);
-                    }
-                }
-                if (tid == 0) s_staged = s_next;
-            };
 
             // ---------------- the item bodies of the three sweeps ----------------
             // X sweep of voxel (interior plane pi, row r, column c) into pool 1 entry e1; y-decisions
