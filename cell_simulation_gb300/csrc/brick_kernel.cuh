@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
         }
         const WorkItem nw = P.items[nx];
         const RepDesc nr = P.reps[nw.rep];
-        if (nr.flags & 1u) return;
+        if ((nr.flags & 1u) || nw.pad[0]) return;
         const int nX = (int)nr.X, nY = (int)nr.Y;
         for (int k = tid; k < B::RPX * RWY; k += NT) {
             const int rp = k / RWY, ry = k - rp * RWY;
@@ -252,7 +252,10 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
             orow0 = rd.obase + ((uint64_t)x0 * (uint64_t)Y + (uint64_t)y0) * rd.Wz + (uint64_t)(z0 >> 5);
             const uint64_t colv = ((1ull << min(32, Z - z0)) - 1ull) << 1;  // interior columns inside
             const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
-            const bool uniform = (rd.flags & 1u) != 0u;
+            // one region code over the whole region window (a one-region replicate, or a brick whose
+            // window the host found to hold one region): no region rows are staged
+            const uint32_t ucode = (rd.flags & 1u) ? 1u : wi.pad[0];
+            const bool flat = ucode != 0u;
             const uint8_t* src = P.src + rd.base * K;
             uint8_t* dst = P.dst + rd.base * K;
             const uint8_t* rpad = P.region_pad + rd.rbase;
@@ -266,9 +269,9 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
             };
             // region code of box voxel (p, r, c); p, r, c may step one outside the box
             auto code = [&](int p, int r, int c) -> uint32_t {
-                if (uniform) {
+                if (flat) {
                     const int x = x0 - 1 + p, y = y0 - 1 + r, z = z0 - 1 + c;
-                    return (x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z) ? 1u : 0u;
+                    return (x >= 0 && x < X && y >= 0 && y < Y && z >= 0 && z < Z) ? ucode : 0u;
                 }
                 return reg[((p + 1) * RWY + (r + 1)) * RWZB + c + 1];
             };
@@ -338,7 +341,7 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
             };
 
             // ---------------- L: box occupancy from the bitmap ----------------
-            if (!uniform) {
+            if (!flat) {
                 for (int c = tid; c < NCH; c += NT) {
                     const int rp = c / (RWY * 3), rem = c - rp * (RWY * 3), ry = rem / 3, cz = rem - ry * 3;
                     const int x = x0 - 2 + rp, y = y0 - 2 + ry, zp = z0 + 16 * cz;  // zp: padded column (z + 2)

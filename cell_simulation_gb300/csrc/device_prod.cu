@@ -117,6 +117,7 @@ struct DeviceProd {
     uint64_t occ_words = 0;
     bool occ_valid = false;   // the bitmaps describe the slot buffers (false after uploads and tile frames)
     DevBuf<uint8_t> region_pad, reservoir;
+    std::vector<uint8_t> h_region_pad;  // host copy of region_pad (single lattices; empty for ensembles)
     DevBuf<uint32_t> thr;
     DevBuf<uint8_t> rx_reactants, rx_ch_sp;
     DevBuf<int8_t> rx_ch_d;
@@ -353,6 +354,27 @@ static int pick_default_cfg(uint32_t K) {
     return -1;
 }
 
+// The region code shared by every lattice voxel of brick w's region window
+// (planes x0-2..x0+BX+1, rows y0-2..y0+BY+1, columns z0-2..z0+45), or 0 when
+// the window holds more than one region or the host copy is absent.
+static uint32_t window_code(const DeviceProd* d, const RepDesc& r, const WorkItem& w, const KernelCfg& cfg) {
+    if (d->h_region_pad.empty() || (r.flags & 1u)) return 0u;
+    const uint8_t* rp = d->h_region_pad.data() + r.rbase;
+    const int64_t xa = std::max<int64_t>(0, (int64_t)w.x0 - 2), xb = std::min<int64_t>(r.X, (int64_t)w.x0 + cfg.BX + 2);
+    const int64_t ya = std::max<int64_t>(0, (int64_t)w.y0 - 2), yb = std::min<int64_t>(r.Y, (int64_t)w.y0 + cfg.TY + 2);
+    const int64_t za = std::max<int64_t>(0, (int64_t)w.z0 - 2), zb = std::min<int64_t>(r.Z, (int64_t)w.z0 + 46);
+    uint32_t code = 0u;
+    for (int64_t x = xa; x < xb; x++)
+        for (int64_t y = ya; y < yb; y++) {
+            const uint8_t* row = rp + ((uint64_t)x * r.Y + (uint64_t)y) * r.Zr + 2;  // column z + 2 holds z
+            for (int64_t z = za; z < zb; z++) {
+                if (code == 0u) code = row[z];
+                else if (row[z] != code) return 0u;
+            }
+        }
+    return code;
+}
+
 // Work items for the current config: (replicate, y0, z0, x-segment).  A brick
 // configuration uses segments of BX planes, x fastest, so that bricks sharing
 // halo planes run close together in time and the halo re-reads hit L2.
@@ -382,6 +404,7 @@ static void build_items(DeviceProd* d) {
                 for (uint32_t x0 = 0; x0 < r.X; x0 += seg) {
                     WorkItem w{};
                     w.rep = ri; w.y0 = y0; w.z0 = z0; w.x0 = x0; w.x1 = std::min(r.X, x0 + seg);
+                    if (cfg.kind == KIND_BRICK) w.pad[0] = window_code(d, r, w, cfg);
                     per_rep.push_back(w);
                 }
     }
@@ -605,6 +628,8 @@ DeviceProd* prod_create(const Model& m, int device) {
         }
     d->region_pad.alloc(rc.size());
     CS_CUDA(cudaMemcpy(d->region_pad.p, rc.data(), rc.size(), cudaMemcpyHostToDevice));
+    d->h_region_pad = std::move(rc);
+    build_items(d.get());  // brick items carry their window's region code
     if (any_res) {
         std::vector<uint8_t> r8(m.V);
         for (uint64_t v = 0; v < m.V; v++) r8[v] = (uint8_t)m.reservoir[v];

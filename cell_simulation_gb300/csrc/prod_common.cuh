@@ -55,6 +55,9 @@ struct RepDesc {
 };
 static_assert(sizeof(RepDesc) == 64, "RepDesc is 64 bytes");
 
+// pad[0] of a brick item: the region code (id + 1) of every lattice voxel of
+// the brick's region window (planes x0-2..x0+BX+1, rows y0-2..y0+BY+1,
+// columns z0-2..z0+45) when they all share one, else 0.
 struct WorkItem {
     uint32_t rep, y0, z0, x0, x1, pad[3];
 };

@@ -97,6 +97,19 @@ def test_brick_pass_with_spilled_bricks_matches_oracle(orc, K):
             assert 0 < spilled < 24 * n_bricks, spilled  # some bricks spill, most do not
 
 
+@pytest.mark.parametrize("K", [8, 16])
+def test_one_region_windows_match_oracle(orc, K):
+    """A small cell in a large lattice: bricks far from it see one region in their whole region
+    window and skip the region rows, the bricks around it stage them; the frame is the same."""
+    mk = lambda: multi_region_model(res=(40, 36, 70), K=K, counts=(120, 400, 80, 40), transition=True)
+    want_s, want_c, want_d = oracle_prod(orc, mk(), 30, seed=4242)
+    for ti in brick_tilings(K):
+        got_s, got_c, got_d = gpu_prod(mk(), 30, 4242, tiling=ti, chunks=2)
+        assert np.array_equal(got_s, want_s), (ti, np.flatnonzero(got_s != want_s)[:8])
+        assert np.array_equal(got_c, want_c), ti
+        assert np.array_equal(got_d[:4], want_d[:4]), (ti, got_d, want_d)
+
+
 def test_sparse_lattice_never_spills():
     sim = multi_region_model(res=(24, 20, 40), K=16, counts=(60, 50, 40, 30))
     _, _, d = gpu_prod(sim, 10, 5)
