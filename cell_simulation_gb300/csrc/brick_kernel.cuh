@@ -19,9 +19,10 @@
 // a 64-bit mask per quantity (occupied, moving down / up along an axis, has
 // content after a sweep), and the contents of the voxels a phase produces
 // are kept in a pool where every row's voxels are contiguous: the pool index
-// of voxel (row, c) is rowbase[row] + popcount(mask[row] below c).  Warps
-// handle rows w, w + NW, ... and reserve the pool range of their rows with
-// one shared-memory atomic, so no CTA-wide scan is needed.  A phase writes
+// of voxel (row, c) is rowbase[row] + popcount(mask[row] below c).  Warp w
+// lists rows 32 w .. 32 w + 31 (one row per lane; warps past the last row
+// sit the list out) and reserves the pool range of its rows with one
+// shared-memory atomic, so no CTA-wide scan is needed.  A phase writes
 // the positions of its voxels into a list indexed like its pool, and after a
 // barrier the whole CTA runs the list with every lane busy.  The lattice is
 // mostly empty, so a brick holds a few hundred entries per pool where the
@@ -55,7 +56,6 @@ struct Brick {
     static constexpr int NROW0 = PX * WY;  // box rows (plane, row)
     static constexpr int NROW1 = BX * WY;  // X-sweep rows: interior planes, all rows
     static constexpr int NROW2 = BX * BY;  // Y/Z-sweep rows: interior planes, interior rows
-    static constexpr int RW1 = (NROW1 + NW - 1) / NW, RW2 = (NROW2 + NW - 1) / NW;
     static constexpr int RPX = BX + 4, RWY = BY + 4, RWZB = 48, RPLANE = RWY * RWZB;
     static constexpr int NCH = RPX * RWY * (RWZB / 16);  // 16-byte region chunks
     static constexpr int MAXC = CAP0 > CAP1 ? (CAP0 > CAP2 ? CAP0 : CAP2) : (CAP1 > CAP2 ? CAP1 : CAP2);
@@ -64,7 +64,7 @@ struct Brick {
     static constexpr int LCAP = WP ? 0 : (MAXC > NROW2 * 32 ? MAXC : NROW2 * 32);
     static constexpr int LDW = BY * 32;  // per-warp D list (warp-per-plane path)
     static constexpr bool DENSE = CAP0 >= NROW0 * WZ && CAP1 >= NROW1 * WZ && CAP2 >= NROW2 * WZ;  // never overflows
-    static_assert(NT % 32 == 0 && RW1 <= 32 && RW2 <= 32 && WY <= 32, "one lane per row of a warp's share");
+    static_assert(NT % 32 == 0 && WY <= 32 && BY <= 32, "one lane per row of a plane (warp-per-plane path)");
     static_assert(NROW0 * 64 <= 65536 && MAXC < 65536, "positions and pool indices fit 16 bits");
     enum : int {
         M_OCC0 = 0, M_XM = NROW0, M_XP = 2 * NROW0,
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
     using B = Brick<K, BX, BY, NT, CAP0, CAP1, CAP2>;
     constexpr bool WP = B::WP;
     constexpr int NW = B::NW, WY = B::WY, NROW0 = B::NROW0, NROW1 = B::NROW1, NROW2 = B::NROW2;
-    constexpr int RW1 = B::RW1, RW2 = B::RW2, RWY = B::RWY, RWZB = B::RWZB, NCH = B::NCH, C02 = B::C02;
+    constexpr int RWY = B::RWY, RWZB = B::RWZB, NCH = B::NCH, C02 = B::C02;
     constexpr int LCAP = B::LCAP, LDW = B::LDW;
     extern __shared__ __align__(16) uint8_t smem[];
     Vox<K>* cont0 = reinterpret_cast<Vox<K>*>(smem + B::off_c0);
@@ -642,9 +642,9 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                 stage_masks();
             } else {
                 // ---------------- B, C, D CTA-wide, each list built before a barrier ----------------
-                {
-                    const int j = w + lane * NW;
-                    const bool valid = lane < RW1 && j < NROW1;
+                if (w * 32 < NROW1) {
+                    const int j = w * 32 + lane;
+                    const bool valid = j < NROW1;
                     uint64_t s1 = 0ull;
                     if (valid) {
                         const int pi = j / WY + 1, r = j - (pi - 1) * WY;
@@ -670,9 +670,9 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                 for (uint32_t e1 = (uint32_t)tid; e1 < n1; e1 += NT) b_item(e1, L1[e1]);
                 stage_masks();
                 __syncthreads();
-                {
-                    const int j2 = w + lane * NW;
-                    const bool valid = lane < RW2 && j2 < NROW2;
+                if (w * 32 < NROW2) {
+                    const int j2 = w * 32 + lane;
+                    const bool valid = j2 < NROW2;
                     uint64_t s2 = 0ull;
                     if (valid) {
                         const int pi = j2 / BY + 1, r = j2 - (pi - 1) * BY + 1;
@@ -697,9 +697,9 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                 }
                 for (uint32_t e2 = (uint32_t)tid; e2 < n2; e2 += NT) c_item(e2, L2[e2]);
                 __syncthreads();
-                {
-                    const int j2 = w + lane * NW;
-                    const bool valid = lane < RW2 && j2 < NROW2;
+                if (w * 32 < NROW2) {
+                    const int j2 = w * 32 + lane;
+                    const bool valid = j2 < NROW2;
                     bool row_in;
                     const uint64_t s3 = d_row(j2, valid, row_in);
                     uint32_t base, total;
