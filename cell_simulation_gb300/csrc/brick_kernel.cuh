@@ -27,7 +27,7 @@
 // barrier the whole CTA runs the list with every lane busy.  The lattice is
 // mostly empty, so a brick holds a few hundred entries per pool where the
 // dense box has thousands of voxels, and the CTA footprint stays small
-// enough for three CTAs per SM.
+// enough for four CTAs per SM.
 //
 // The Philox block B(v, 0) of a voxel is evaluated once per frame, in the
 // first phase that sees the voxel non-empty, and its words (x, y, z draw of
