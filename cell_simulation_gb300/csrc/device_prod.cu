@@ -95,6 +95,9 @@ static const std::vector<KernelCfg>& all_cfgs() {
         brick_cfg<16, 6, 8, 192, 4, 560, 560, 560>(10, 3), brick_cfg<8, 8, 8, 192, 4, 544, 544, 544>(11, 4),
         // small pool 1: bricks overflow after other warps have stored their planes (exercises that route)
         brick_cfg<16, 8, 8, 256, 3, 768, 128, 768>(10, 4),
+        // 16-plane bricks, two CTAs of 12 warps per SM: the box is 1.49 times the interior (1.66 for
+        // 8 planes) and the per-brick fixed cost is spread over twice the voxels
+        brick_cfg<16, 16, 8, 384, 2, 1088, 1088, 1088>(10, 8), brick_cfg<8, 16, 8, 384, 2, 1088, 1088, 1088>(11, 8),
     };
     return v;
 }

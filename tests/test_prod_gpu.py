@@ -93,7 +93,8 @@ def test_brick_pass_with_spilled_bricks_matches_oracle(orc, K):
         if tiling_kinds()[ti][1] == 2:
             assert spilled == 0  # full-capacity pools
         else:
-            n_bricks = 3 * 3 * 3  # (19/8, 21/8, 70/32) rounded up
+            planes = tiling_kinds()[ti][1]
+            n_bricks = -(-19 // planes) * 3 * 3  # (19/planes, 21/8, 70/32) rounded up
             assert 0 < spilled < 24 * n_bricks, spilled  # some bricks spill, most do not
 
 
