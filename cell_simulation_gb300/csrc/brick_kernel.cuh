@@ -61,7 +61,10 @@ struct Brick {
     static constexpr int MAXC = CAP0 > CAP1 ? (CAP0 > CAP2 ? CAP0 : CAP2) : (CAP1 > CAP2 ? CAP1 : CAP2);
     // CTA-wide path: pool 2 shares pool 0's storage (dead after the X sweep), one list array
     static constexpr int C02 = WP ? CAP0 : (CAP0 > CAP2 ? CAP0 : CAP2);
-    static constexpr int LCAP = WP ? 0 : (MAXC > NROW2 * 32 ? MAXC : NROW2 * 32);
+    // CTA-wide lists in dead storage when it fits: the B and C lists in pool 0's position list (read
+    // only in phase A), the D list in pool 1's contents (read last in phase C); else one list array
+    static constexpr bool ALIAS = !WP && CAP1 <= CAP0 && CAP2 <= CAP0 && CAP1 * K / 2 >= NROW2 * 32;
+    static constexpr int LCAP = WP ? 0 : ALIAS ? CAP1 * K / 2 : (MAXC > NROW2 * 32 ? MAXC : NROW2 * 32);
     static constexpr int LDW = BY * 32;  // per-warp D list (warp-per-plane path)
     static constexpr bool DENSE = CAP0 >= NROW0 * WZ && CAP1 >= NROW1 * WZ && CAP2 >= NROW2 * WZ;  // never overflows
     static_assert(NT % 32 == 0 && WY <= 32 && BY <= 32, "one lane per row of a plane (warp-per-plane path)");
@@ -85,7 +88,7 @@ struct Brick {
     static constexpr size_t off_rb = off_m + (size_t)M_N * 8;            // u16 rowbases [NROW0 + NROW1 + NROW2]
     static constexpr size_t off_pos = a16(off_rb + (size_t)(NROW0 + NROW1 + NROW2) * 2);  // u16 [CAP0]
     // u16 lists: warp-per-plane L1 [CAP1], L2 [CAP2], LD [NW][LDW]; CTA-wide L [LCAP]
-    static constexpr size_t LIST_WORDS = WP ? (size_t)CAP1 + CAP2 + (size_t)NW * LDW : (size_t)LCAP;
+    static constexpr size_t LIST_WORDS = WP ? (size_t)CAP1 + CAP2 + (size_t)NW * LDW : ALIAS ? 0 : (size_t)LCAP;
     static constexpr size_t off_list = a16(off_pos + (size_t)CAP0 * 2);
     static constexpr size_t off_reg = a16(off_list + LIST_WORDS * 2);    // u8 [RPX][RWY][RWZB]
     static constexpr size_t off_nocc = a16(off_reg + (size_t)RPX * RPLANE);  // u64 [NROW0] next item's OCC0
@@ -138,9 +141,9 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
     uint16_t* RB2 = RB1 + NROW1;
     uint16_t* pos0 = reinterpret_cast<uint16_t*>(smem + B::off_pos);
     uint16_t* Lbase = reinterpret_cast<uint16_t*>(smem + B::off_list);
-    uint16_t* L1 = Lbase;                                  // positions of pool 1 entries
-    uint16_t* L2 = WP ? Lbase + CAP1 : Lbase;              // positions of pool 2 entries
-    uint16_t* LD = WP ? Lbase + CAP1 + CAP2 : Lbase;       // D lists
+    uint16_t* L1 = WP ? Lbase : B::ALIAS ? pos0 : Lbase;   // positions of pool 1 entries
+    uint16_t* L2 = WP ? Lbase + CAP1 : B::ALIAS ? pos0 : Lbase;  // positions of pool 2 entries
+    uint16_t* LD = WP ? Lbase + CAP1 + CAP2 : B::ALIAS ? reinterpret_cast<uint16_t*>(cont1) : Lbase;  // D lists
     uint8_t* reg = smem + B::off_reg;
     uint64_t* nocc = reinterpret_cast<uint64_t*>(smem + B::off_nocc);  // box masks staged for item s_staged
     uint32_t* top = reinterpret_cast<uint32_t*>(smem + B::off_tail);  // [4] pool 0, pool 1, pool 2, D list

@@ -98,6 +98,8 @@ static const std::vector<KernelCfg>& all_cfgs() {
         // 16-plane bricks, two CTAs of 12 warps per SM: the box is 1.49 times the interior (1.66 for
         // 8 planes) and the per-brick fixed cost is spread over twice the voxels
         brick_cfg<16, 16, 8, 384, 2, 1088, 1088, 1088>(10, 8), brick_cfg<8, 16, 8, 384, 2, 1088, 1088, 1088>(11, 8),
+        // 16-plane bricks, three CTAs of 8 warps per SM (smaller pools; more bricks in flight)
+        brick_cfg<16, 16, 8, 256, 3, 640, 640, 640>(10, 8), brick_cfg<8, 16, 8, 256, 3, 768, 768, 768>(11, 8),
     };
     return v;
 }
@@ -350,11 +352,18 @@ static void build_one_table(DeviceProd* d) {
     d->T.quiet = d->quiet.p;
 }
 
+// Default step before any autotuning: the 16-plane, 256-thread brick pass of the
+// model's K (the fastest variant on the sparse lattices measured), else its first
+// brick pass.
 static int pick_default_cfg(uint32_t K) {
     const auto& c = all_cfgs();
-    for (size_t i = 0; i < c.size(); i++)
-        if (c[i].K == (int)K && c[i].kind == KIND_BRICK) return (int)i;
-    return -1;
+    int first = -1;
+    for (size_t i = 0; i < c.size(); i++) {
+        if (c[i].K != (int)K || c[i].kind != KIND_BRICK) continue;
+        if (c[i].BX == 16 && c[i].NT == 256 && c[i].spill >= 0) return (int)i;
+        if (first < 0) first = (int)i;
+    }
+    return first;
 }
 
 // The region code shared by every lattice voxel of brick w's region window
