@@ -61,13 +61,18 @@ struct Brick {
     static constexpr int MAXC = CAP0 > CAP1 ? (CAP0 > CAP2 ? CAP0 : CAP2) : (CAP1 > CAP2 ? CAP1 : CAP2);
     // CTA-wide path: pool 2 shares pool 0's storage (dead after the X sweep), one list array
     static constexpr int C02 = WP ? CAP0 : (CAP0 > CAP2 ? CAP0 : CAP2);
-    // CTA-wide lists in dead storage when it fits: the B and C lists in pool 0's position list (read
-    // only in phase A), the D list in pool 1's contents (read last in phase C); else one list array
-    static constexpr bool ALIAS = !WP && CAP1 <= CAP0 && CAP2 <= CAP0 && CAP1 * K / 2 >= NROW2 * 32;
-    static constexpr int LCAP = WP ? 0 : ALIAS ? CAP1 * K / 2 : (MAXC > NROW2 * 32 ? MAXC : NROW2 * 32);
+    // CTA-wide D list: each pool-2 voxel and at most its two z-move targets (3 CAP2 entries); with
+    // reservoirs or zero-order reactions every interior voxel is stepped without a list.  The lists
+    // sit in dead storage when it fits: the B and C lists in pool 0's position list (read only in
+    // phase A), the D list in pool 1's contents (read last in phase C); else in one list array.
+    static constexpr int DCAP = 3 * CAP2;
+    static constexpr bool ALIAS = !WP && CAP1 <= CAP0 && CAP2 <= CAP0 && CAP1 * K / 2 >= DCAP;
+    static constexpr int LCAP = WP ? 0 : ALIAS ? CAP1 * K / 2 : (MAXC > DCAP ? MAXC : DCAP);
     static constexpr int LDW = BY * 32;  // per-warp D list (warp-per-plane path)
     static constexpr bool DENSE = CAP0 >= NROW0 * WZ && CAP1 >= NROW1 * WZ && CAP2 >= NROW2 * WZ;  // never overflows
     static_assert(NT % 32 == 0 && WY <= 32 && BY <= 32, "one lane per row of a plane (warp-per-plane path)");
+    // CTA-wide lists: warp w lists rows 32 w .. 32 w + 31 in one pass, so every row needs a thread
+    static_assert(NW == BX || (NT >= NROW1 && NT >= NROW2), "one thread per row of the B, C and D lists");
     static_assert(NROW0 * 64 <= 65536 && MAXC < 65536, "positions and pool indices fit 16 bits");
     enum : int {
         M_OCC0 = 0, M_XM = NROW0, M_XP = 2 * NROW0,
@@ -700,17 +705,27 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                 }
                 for (uint32_t e2 = (uint32_t)tid; e2 < n2; e2 += NT) c_item(e2, L2[e2]);
                 __syncthreads();
-                if (w * 32 < NROW2) {
-                    const int j2 = w * 32 + lane;
-                    const bool valid = j2 < NROW2;
-                    bool row_in;
-                    const uint64_t s3 = d_row(j2, valid, row_in);
-                    uint32_t base, total;
-                    append_list(s3, j2, valid && row_in, 3, (uint32_t)LCAP, LD, base, total);
+                if (all_react) {
+                    // every interior voxel inside the lattice is stepped (reservoir or zero-order
+                    // reactions), so none is left stale and no list is needed
+                    for (uint32_t t = (uint32_t)tid; t < (uint32_t)NROW2 * 32u; t += NT) {
+                        const int j2 = (int)(t >> 5), c = (int)(t & 31u) + 1;
+                        const int pi = j2 / BY + 1, r = j2 - (pi - 1) * BY + 1;
+                        if (pi <= np && r <= ny && ((colv >> c) & 1ull)) d_item((uint32_t)((j2 << 6) | c));
+                    }
+                } else {
+                    if (w * 32 < NROW2) {
+                        const int j2 = w * 32 + lane;
+                        const bool valid = j2 < NROW2;
+                        bool row_in;
+                        const uint64_t s3 = d_row(j2, valid, row_in);
+                        uint32_t base, total;
+                        append_list(s3, j2, valid && row_in, 3, (uint32_t)LCAP, LD, base, total);
+                    }
+                    __syncthreads();
+                    const uint32_t nd = top[3];
+                    for (uint32_t t = (uint32_t)tid; t < nd; t += NT) d_item(LD[t]);
                 }
-                __syncthreads();
-                const uint32_t nd = top[3];
-                for (uint32_t t = (uint32_t)tid; t < nd; t += NT) d_item(LD[t]);
             }
             done = true;
         } while (0);

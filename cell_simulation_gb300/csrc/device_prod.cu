@@ -100,6 +100,9 @@ static const std::vector<KernelCfg>& all_cfgs() {
         brick_cfg<16, 16, 8, 384, 2, 1088, 1088, 1088>(10, 8), brick_cfg<8, 16, 8, 384, 2, 1088, 1088, 1088>(11, 8),
         // 16-plane bricks, three CTAs of 8 warps per SM (smaller pools; more bricks in flight)
         brick_cfg<16, 16, 8, 256, 3, 640, 640, 640>(10, 8), brick_cfg<8, 16, 8, 256, 3, 768, 768, 768>(11, 8),
+        // four CTAs of 6 warps / six CTAs of 5 warps per SM: small pools for sparse replicates (the
+        // 512-replicate ensemble), where more bricks in flight per SM beat larger pools
+        brick_cfg<8, 16, 8, 192, 4, 432, 432, 432>(11, 8), brick_cfg<8, 16, 8, 160, 6, 176, 176, 176>(11, 8),
     };
     return v;
 }
