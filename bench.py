@@ -206,14 +206,18 @@ def describe_variant(i):
     kind, bx = tiling_kinds()[i]
     if kind == 1:
         return {"index": i, "kind": "brick", "slots": k, "brick": [bx, ty, tz], "threads": nt}
+    if kind == 2:
+        return {"index": i, "kind": "stream", "slots": k, "words_per_group": 32, "threads": nt}
     return {"index": i, "kind": "tile", "slots": k, "tile": [ty, tz], "threads": nt}
 
 
 def launches_per_frame(i):
     """Kernel launches per frame of variant i: a brick pass with bounded pools is
-    followed by the pass over its spilled bricks."""
+    followed by the pass over its spilled bricks; the sweep stream is four passes."""
     from cell_simulation_gb300 import tiling_kinds
     kind, bx = tiling_kinds()[i]
+    if kind == 2:
+        return 4
     return 2 if kind == 1 and bx > 2 else 1
 
 
@@ -295,7 +299,8 @@ def main():
     peak, peak_kind = measured_peaks()
     alg_bytes = V * (2 * K + 1)
     achieved = alg_bytes / per_launch_s / 1e9
-    kernel = "brick_step_kernel" if describe_variant(variant)["kind"] == "brick" else "prod_step_kernel"
+    kernel = {"brick": "brick_step_kernel", "stream": "sweep_pass_kernel"}.get(describe_variant(variant)["kind"],
+                                                                             "prod_step_kernel")
     traffic = profiled_traffic(kernel, w.name)
     diag = sim.diagnostics()
 

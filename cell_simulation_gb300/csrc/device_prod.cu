@@ -36,6 +36,7 @@
 #include "brick_kernel.cuh"
 #include "prod_common.cuh"
 #include "prod_kernel.cuh"
+#include "stream_kernel.cuh"
 #include "views.cuh"
 
 namespace cellsim {
@@ -48,8 +49,10 @@ typedef void (*ProdKernelFn)(ProdParams);
 // (TY x TZ tile, x-segment) items.  kind 1: the brick pass over BX x TY x 32
 // bricks; when its pools can overflow, a second brick pass `spill` with
 // pools as large as its box finishes the spilled bricks in `sub` groups of
-// its own BX planes.
-enum { KIND_TILE = 0, KIND_BRICK = 1 };
+// its own BX planes.  kind 2: the sweep stream, four barrier-free passes over
+// bitmap word groups (stream_kernel.cuh); `variant` indexes its compiled
+// launch shapes.
+enum { KIND_TILE = 0, KIND_BRICK = 1, KIND_STREAM = 2 };
 
 struct KernelCfg {
     int kind, K, TY, TZ, NT, BX;
@@ -57,7 +60,12 @@ struct KernelCfg {
     size_t (*smem)(uint32_t S1, uint32_t thr_words);
     int spill;     // kind 1 with bounded pools: index of the configuration for spilled bricks, else -1
     uint32_t sub;  // plane groups per spilled brick in that configuration
+    int variant;   // kind 2: launch shape of the passes
 };
+
+static KernelCfg stream_cfg(int K, int variant) {
+    return KernelCfg{KIND_STREAM, K, 0, 32, stream_variant_threads(variant), 0, nullptr, nullptr, -1, 0, variant};
+}
 
 template <int K, int TY, int TZ>
 static size_t tile_smem(uint32_t S1, uint32_t) { return Tile<K, TY, TZ>::smem(S1); }
@@ -103,6 +111,8 @@ static const std::vector<KernelCfg>& all_cfgs() {
         // four CTAs of 6 warps / six CTAs of 5 warps per SM: small pools for sparse replicates (the
         // 512-replicate ensemble), where more bricks in flight per SM beat larger pools
         brick_cfg<8, 16, 8, 192, 4, 432, 432, 432>(11, 8), brick_cfg<8, 16, 8, 160, 6, 176, 176, 176>(11, 8),
+        // sweep stream: 256 threads, at least two / four blocks per SM (pass 3 of variant 2: three)
+        stream_cfg(16, 0), stream_cfg(16, 1), stream_cfg(8, 0), stream_cfg(8, 1), stream_cfg(16, 2), stream_cfg(8, 2),
     };
     return v;
 }
@@ -146,6 +156,25 @@ struct DeviceProd {
     DevBuf<WorkItem> items_rep;  // grouped per replicate (plain launches)
     std::vector<uint32_t> rep_item_off;
     uint32_t n_items = 0;
+    // sweep stream: word groups (rep-major), records of two pass boundaries and per-word arrays
+    DevBuf<WordGroup> groups;
+    std::vector<uint32_t> rep_group_off;
+    uint32_t n_groups = 0;
+    DevBuf<uint4> rec[2];
+    DevBuf<uint32_t> sw[14];
+    DevBuf<uint8_t> wcode;  // per bitmap word: uniform region code of its window, or 0 (single lattices)
+    std::vector<WordGroup> h_groups;
+    bool groups_sorted = false;  // groups dealt heaviest first (sorted once per group build)
+    int stream_per_sm[4] = {0, 0, 0, 0};  // resident blocks per SM of the current stream passes
+    int stream_occ_cfg = -1;
+    // The x-decisions of frame xdec_frame (parity xdec_cur, configuration xdec_cfg, seed epoch
+    // xdec_epoch) are in the per-word arrays and rec[xdec_cur]: made by the last sweep-stream
+    // frame's pass 3.  Any other change of the lattice clears xdec_valid.
+    bool xdec_valid = false;
+    uint64_t xdec_frame = 0, xdec_epoch = 0;
+    int xdec_cur = 0, xdec_cfg = -1;
+    uint64_t seed_epoch = 0;  // advanced whenever the Philox keys change
+    uint64_t next_frame = 0;  // host copy of the frame number in stepbuf[cur]
     int cur = 0;
     ProdTables T{};
     int cfg_index = -1;
@@ -393,8 +422,14 @@ static uint32_t window_code(const DeviceProd* d, const RepDesc& r, const WorkIte
 // Work items for the current config: (replicate, y0, z0, x-segment).  A brick
 // configuration uses segments of BX planes, x fastest, so that bricks sharing
 // halo planes run close together in time and the halo re-reads hit L2.
+static void build_groups(DeviceProd* d);
+
 static void build_items(DeviceProd* d) {
     const KernelCfg& cfg = all_cfgs()[d->cfg_index];
+    if (cfg.kind == KIND_STREAM) {
+        build_groups(d);
+        return;
+    }
     std::vector<WorkItem> all, per_rep;
     d->rep_item_off.assign(d->n_rep + 1, 0);
     // target: enough items to keep every SM busy with a few in flight
@@ -440,14 +475,130 @@ static void build_items(DeviceProd* d) {
     CS_CUDA(cudaMemcpy(d->items_rep.p, per_rep.data(), per_rep.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
 }
 
+// Word groups of the sweep stream: for each replicate and x plane, runs of
+// whole rows that fill up to 32 lanes (rows of more than 32 words are cut
+// into 32-word pieces), in replicate order.  The records of group g start
+// after the capacities (32 per word) of the groups before it, so the
+// records of all groups together number 32 per bitmap word.
+static void build_groups(DeviceProd* d) {
+    std::vector<WordGroup> gs;
+    d->rep_group_off.assign(d->n_rep + 1, 0);
+    uint64_t rb = 0;
+    for (uint32_t ri = 0; ri < d->n_rep; ri++) {
+        const RepDesc& r = d->h_reps[ri];
+        d->rep_group_off[ri] = (uint32_t)gs.size();
+        for (uint32_t x = 0; x < r.X; x++) {
+            if (r.Wz <= 32) {
+                const uint32_t per = 32 / r.Wz;
+                for (uint32_t y0 = 0; y0 < r.Y; y0 += per) {
+                    const WordGroup g{ri, x, y0, std::min(per, r.Y - y0), 0u, r.Wz, rb};
+                    rb += (uint64_t)g.nrows * g.nk * 32u;
+                    gs.push_back(g);
+                }
+            } else {
+                for (uint32_t y = 0; y < r.Y; y++)
+                    for (uint32_t k0 = 0; k0 < r.Wz; k0 += 32) {
+                        const WordGroup g{ri, x, y, 1u, k0, std::min(32u, r.Wz - k0), rb};
+                        rb += (uint64_t)g.nk * 32u;
+                        gs.push_back(g);
+                    }
+            }
+        }
+    }
+    d->rep_group_off[d->n_rep] = (uint32_t)gs.size();
+    if (rb >= (1ull << 32) || gs.size() >= (1ull << 32))
+        throw Error(CS_ERR_LIMIT, "lattice too large for the sweep-stream step (at most 2^32 records)");
+    d->n_groups = (uint32_t)gs.size();
+    d->n_items = d->n_groups;
+    if (!d->h_region_pad.empty() && d->wcode.n == 0) {
+        // uniform region code of each word's window: first per row word (z from 32k-1 to
+        // 32k+32 inside the lattice), then over the 3 x 3 rows around it
+        const RepDesc& r = d->h_reps[0];
+        const uint64_t rows = (uint64_t)r.X * r.Y;
+        std::vector<uint8_t> run(rows * r.Wz, 0), wc(rows * r.Wz, 0);
+        for (uint64_t row = 0; row < rows; row++) {
+            const uint8_t* rp = d->h_region_pad.data() + row * r.Zr + 2;  // column z + 2 holds z
+            for (uint32_t k = 0; k < r.Wz; k++) {
+                const int64_t za = std::max<int64_t>(0, 32 * (int64_t)k - 1);
+                const int64_t zb = std::min<int64_t>(r.Z, 32 * (int64_t)k + 33);
+                uint8_t c = rp[za];
+                for (int64_t z = za + 1; z < zb && c; z++)
+                    if (rp[z] != c) c = 0;
+                run[row * r.Wz + k] = c;
+            }
+        }
+        for (uint32_t x = 0; x < r.X; x++)
+            for (uint32_t y = 0; y < r.Y; y++)
+                for (uint32_t k = 0; k < r.Wz; k++) {
+                    const uint64_t wi = ((uint64_t)x * r.Y + y) * r.Wz + k;
+                    uint8_t c = run[wi];
+                    for (int dx = -1; dx <= 1 && c; dx++)
+                        for (int dy = -1; dy <= 1 && c; dy++) {
+                            const int64_t xx = (int64_t)x + dx, yy = (int64_t)y + dy;
+                            if (xx < 0 || xx >= r.X || yy < 0 || yy >= r.Y) continue;
+                            if (run[((uint64_t)xx * r.Y + (uint64_t)yy) * r.Wz + k] != c) c = 0;
+                        }
+                    wc[wi] = c;
+                }
+        d->wcode.alloc(wc.size());
+        CS_CUDA(cudaMemcpy(d->wcode.p, wc.data(), wc.size(), cudaMemcpyHostToDevice));
+    }
+    d->groups.alloc(gs.size());
+    CS_CUDA(cudaMemcpy(d->groups.p, gs.data(), gs.size() * sizeof(WordGroup), cudaMemcpyHostToDevice));
+    d->h_groups = std::move(gs);
+    d->groups_sorted = false;
+    for (int b = 0; b < 2; b++)
+        if (d->rec[b].n < 2 * rb) d->rec[b].alloc(2 * rb);  // two uint4 per record
+    for (auto& a : d->sw)
+        if (a.n < d->occ_words) a.alloc(d->occ_words);
+}
+
+// Deals each replicate's word groups heaviest first (most occupied voxels in
+// the current source bitmap), so that the passes end on light groups.  The
+// order changes nothing else: records, words and results are indexed the same
+// way.  Runs once per group build, with valid bitmaps, outside any capture.
+static void sort_groups(DeviceProd* d) {
+    std::vector<uint32_t> occ(d->occ_words);
+    CS_CUDA(cudaMemcpyAsync(occ.data(), d->occ[d->cur].p, occ.size() * 4, cudaMemcpyDeviceToHost, d->stream));
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    std::vector<std::pair<uint32_t, uint32_t>> wg;  // (weight, index within the replicate's range)
+    std::vector<WordGroup> out(d->h_groups.size());
+    for (uint32_t ri = 0; ri < d->n_rep; ri++) {
+        const RepDesc& r = d->h_reps[ri];
+        const uint32_t a = d->rep_group_off[ri], b = d->rep_group_off[ri + 1];
+        wg.clear();
+        for (uint32_t gi = a; gi < b; gi++) {
+            const WordGroup& G = d->h_groups[gi];
+            uint32_t wsum = 0;
+            for (uint32_t i = 0; i < G.nrows * G.nk; i++) {
+                const uint64_t y = G.y0 + i / G.nk, k = G.k0 + i % G.nk;
+                wsum += (uint32_t)__builtin_popcount(occ[r.obase + ((uint64_t)G.x * r.Y + y) * r.Wz + k]);
+            }
+            wg.emplace_back(wsum, gi);
+        }
+        std::stable_sort(wg.begin(), wg.end(), [](const auto& u, const auto& v) { return u.first > v.first; });
+        for (uint32_t j = 0; j < wg.size(); j++) out[a + j] = d->h_groups[wg[j].second];
+    }
+    d->h_groups = std::move(out);
+    CS_CUDA(cudaMemcpy(d->groups.p, d->h_groups.data(), d->h_groups.size() * sizeof(WordGroup), cudaMemcpyHostToDevice));
+    d->groups_sorted = true;
+}
+
 static uint32_t thr_words(const DeviceProd* d) {
     const uint32_t n = d->NC * d->NC * d->S1;
     return n <= kThrSmemWords ? n : 0u;
 }
 
-static size_t cfg_smem(const DeviceProd* d, const KernelCfg& cfg) { return cfg.smem(d->S1, thr_words(d)); }
+static size_t cfg_smem(const DeviceProd* d, const KernelCfg& cfg) {
+    if (cfg.kind == KIND_STREAM) return stream_smem(cfg.NT, d->S1, thr_words(d));
+    return cfg.smem(d->S1, thr_words(d));
+}
 
 static void set_attrs(const DeviceProd* d, const KernelCfg& cfg) {
+    if (cfg.kind == KIND_STREAM) {
+        stream_set_attrs(cfg.K, cfg.variant, cfg_smem(d, cfg));
+        return;
+    }
     CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg_smem(d, cfg)));
     CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
 }
@@ -517,38 +668,88 @@ static int grid_for(DeviceProd* d, const KernelCfg& cfg, uint32_t n_items) {
 static constexpr int kCtrPerParity = 3;
 static uint32_t* group_ctr(DeviceProd* d, int g, int p) { return d->counters.p + (size_t)(2 * g + p) * kCtrPerParity; }
 
+// One pass of a sweep-stream frame of parity `parity` over all word groups
+// (rep < 0) or over replicate rep's.  Records: the x-decisions of a frame of
+// parity p are in rec[p]; pass 1 writes rec[p ^ 1], pass 2 rec[p], and pass 3
+// (fused) the next frame's x-decisions into rec[p ^ 1].  Pass 1, the first
+// pass of every frame, resets the other parity's work counters (as the brick
+// pass does, so that the kinds can alternate); pass 3 advances the frame
+// number.
+static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity, int pass) {
+    uint32_t goff = 0, ng = d->n_groups;
+    if (rep >= 0) {
+        goff = d->rep_group_off[rep];
+        ng = d->rep_group_off[rep + 1] - goff;
+    }
+    if (ng == 0) return;
+    uint32_t* w[14];
+    for (int i = 0; i < 14; i++) w[i] = d->sw[i].p;
+    // per-word arrays of the pass boundaries: {occ, movers down, movers up, work, base}; the
+    // x-decisions cover the source's occupied voxels, whose bitmap is their occ
+    const SweepWords x_dec{nullptr, w[0], w[1], w[13], w[2]};
+    const SweepWords x_in{const_cast<uint32_t*>(P.osrc), w[0], w[1], w[13], w[2]};
+    const SweepWords y_dec{w[3], w[4], w[5], w[6], w[7]};
+    const SweepWords z_dec{w[8], w[9], w[10], w[11], w[12]};
+    uint4* ra = d->rec[parity].p;
+    uint4* rb = d->rec[parity ^ 1].p;
+    const size_t smem = cfg_smem(d, cfg);
+    const uint32_t nw = (uint32_t)cfg.NT / 32u;
+    StreamParams S{};
+    S.P = P;
+    S.P.items = nullptr;
+    S.P.n_items = 0;
+    S.P.advance = pass == 3 ? 1u : 0u;
+    S.P.n_reset = pass == 1 ? P.n_reset : 0u;
+    S.groups = d->groups.p + goff;
+    S.n_groups = ng;
+    // passes 1-3 take their groups from the frame's three work counters (pass 0: round-robin)
+    if (pass > 0) S.queue = group_ctr(d, rep < 0 ? 0 : 1 + rep, parity) + (pass - 1);
+    S.wcode = d->wcode.n ? d->wcode.p : nullptr;
+    switch (pass) {
+        case 0: S.out = x_dec; S.rec_out = ra; break;
+        case 1: S.in = x_in; S.rec_in = ra; S.out = y_dec; S.rec_out = rb; break;
+        case 2: S.in = y_dec; S.rec_in = rb; S.out = z_dec; S.rec_out = ra; break;
+        default: S.in = z_dec; S.rec_in = ra; S.fuse = 1u; S.out = x_dec; S.rec_out = rb; break;
+    }
+    if (d->stream_occ_cfg != d->cfg_index) {
+        for (int q = 0; q < 4; q++) d->stream_per_sm[q] = stream_blocks_per_sm(cfg.K, cfg.variant, q, smem);
+        d->stream_occ_cfg = d->cfg_index;
+    }
+    const int per_sm = d->stream_per_sm[pass];
+    if (per_sm < 1) throw Error(CS_ERR_CUDA, "sweep-stream pass does not fit on an SM");
+    const uint64_t want = ((uint64_t)ng + nw - 1) / nw;
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)per_sm * d->num_sms, want));
+    if (!stream_launch(cfg.K, cfg.variant, pass, grid, smem, d->stream, S))
+        throw Error(CS_ERR_INVALID_ARG, "sweep-stream kernel not compiled for this K");
+    CS_LAUNCH_CHECK();
+}
+
+static void fill_params(DeviceProd* d, ProdParams& P, int parity, int rep);
+
+// Standalone pass 0 (x-decisions of every replicate) for the frame in stepbuf[cur].
+static void launch_stream_pass0(DeviceProd* d) {
+    const KernelCfg& cfg = all_cfgs()[d->cfg_index];
+    ProdParams P{};
+    fill_params(d, P, d->cur, -1);
+    launch_stream_pass(d, cfg, P, -1, d->cur, 0);
+}
+
+static void launch_stream_frame(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity) {
+    for (int pass = 1; pass < 4; pass++) launch_stream_pass(d, cfg, P, rep, parity, pass);
+}
+
 // One frame over all replicates (batched) or over replicate `rep` alone.
 static void launch_frame(DeviceProd* d, int parity, int rep) {
     const KernelCfg& cfg = all_cfgs()[d->cfg_index];
     ProdParams P{};
-    P.T = d->T;
-    P.reps = d->reps.p;
-    P.parity = (uint32_t)parity;
-    P.stepbuf = d->stepbuf.p;
-    P.src = d->slots[parity].p;
-    P.dst = d->slots[parity ^ 1].p;
-    P.osrc = d->occ[parity].p;
-    P.odst = d->occ[parity ^ 1].p;
-    P.region_pad = d->region_pad.p;
-    P.reservoir = d->reservoir.n ? d->reservoir.p : nullptr;
-    P.counts = d->counts.p;
-    P.diag = d->diag.p;
-    const int g = rep < 0 ? 0 : 1 + rep;
-    uint32_t off = 0;
-    if (rep < 0) {
-        P.items = d->items.p;
-        P.n_items = d->n_items;
-    } else {
-        off = d->rep_item_off[rep];
-        P.items = d->items_rep.p + off;
-        P.n_items = d->rep_item_off[rep + 1] - off;
+    fill_params(d, P, parity, rep);
+    if (cfg.kind == KIND_STREAM) {
+        launch_stream_frame(d, cfg, P, rep, parity);
+        return;
     }
+    const int g = rep < 0 ? 0 : 1 + rep;
+    const uint32_t off = rep < 0 ? 0u : d->rep_item_off[rep];
     uint32_t* ctr = group_ctr(d, g, parity);
-    P.queue = ctr;
-    P.reset = group_ctr(d, g, parity ^ 1);
-    P.n_reset = kCtrPerParity;
-    P.advance = 1u;
-    P.thr_smem = thr_words(d) != 0u;
     const uint32_t n = P.n_items;
     if (cfg.spill >= 0) {
         P.spill = d->spill.p + off;
@@ -574,6 +775,39 @@ static void launch_frame(DeviceProd* d, int parity, int rep) {
         sc.fn<<<grid_for(d, sc, n * cfg.sub), sc.NT, cfg_smem(d, sc), d->stream>>>(Q);
         CS_LAUNCH_CHECK();
     }
+}
+
+// Launch parameters shared by every kind for frame parity `parity`.
+static void fill_params(DeviceProd* d, ProdParams& P, int parity, int rep) {
+    P.T = d->T;
+    P.reps = d->reps.p;
+    P.parity = (uint32_t)parity;
+    P.stepbuf = d->stepbuf.p;
+    P.src = d->slots[parity].p;
+    P.dst = d->slots[parity ^ 1].p;
+    P.osrc = d->occ[parity].p;
+    P.odst = d->occ[parity ^ 1].p;
+    P.region_pad = d->region_pad.p;
+    P.reservoir = d->reservoir.n ? d->reservoir.p : nullptr;
+    P.counts = d->counts.p;
+    P.diag = d->diag.p;
+    const int g = rep < 0 ? 0 : 1 + rep;
+    if (all_cfgs()[d->cfg_index].kind != KIND_STREAM) {  // the sweep stream has word groups, no items
+        if (rep < 0) {
+            P.items = d->items.p;
+            P.n_items = d->n_items;
+        } else {
+            const uint32_t off = d->rep_item_off[rep];
+            P.items = d->items_rep.p + off;
+            P.n_items = d->rep_item_off[rep + 1] - off;
+        }
+    }
+    uint32_t* ctr = group_ctr(d, g, parity);
+    P.queue = ctr;
+    P.reset = group_ctr(d, g, parity ^ 1);
+    P.n_reset = kCtrPerParity;
+    P.advance = 1u;
+    P.thr_smem = thr_words(d) != 0u;
 }
 
 static DeviceProd* prod_alloc(const Model& m, int device, const std::vector<RepDesc>& reps, uint64_t total_voxels) {
@@ -680,6 +914,8 @@ void prod_set_lattice(DeviceProd* d, const Model& m, const uint32_t* slots) {
     }
     CS_CUDA(cudaStreamSynchronize(d->stream));
     d->cur = 0;
+    // the next frame has parity 0 whatever the last one had: its work counters start at zero
+    CS_CUDA(cudaMemset(d->counters.p, 0, d->counters.bytes()));
     CS_CUDA(cudaMemcpy(d->slots[0].p, s8.data(), s8.size(), cudaMemcpyHostToDevice));
     d->occ_valid = false;
     std::vector<unsigned long long> c(d->S1);
@@ -721,6 +957,7 @@ void prod_seed(DeviceProd* d, uint64_t seed) {
     CS_CUDA(cudaStreamSynchronize(d->stream));
     d->cur_seed = seed;
     d->seed_set = true;
+    d->seed_epoch++;
 }
 
 // Runs n frames; batched = one launch per frame over all replicates (a
@@ -732,14 +969,26 @@ static void run_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched)
     uint32_t f32 = (uint32_t)frame0;
     CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, &f32, 4, cudaMemcpyHostToDevice, d->stream));
     CS_CUDA(cudaStreamSynchronize(d->stream));
+    d->next_frame = frame0;
     run_frames_nosync(d, n, batched);
 }
 
-// Enqueues n frames; the frame number must already be in stepbuf[cur].
+// Enqueues n frames; the frame number must already be in stepbuf[cur] (and
+// its host copy in next_frame).
 static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched) {
-    const bool brick = all_cfgs()[d->cfg_index].kind == KIND_BRICK;
-    if (n && brick && !d->occ_valid) rebuild_occupancy(d);
-    if (n && !brick) d->occ_valid = false;  // the tile pipeline does not keep the bitmaps
+    if (n == 0) return;
+    // the brick pass and the sweep stream read and maintain the occupancy bitmaps
+    const int kind = all_cfgs()[d->cfg_index].kind;
+    const bool brick = kind != KIND_TILE;
+    // x-decisions made by the last frame's pass 3 hold for this frame only if nothing has changed
+    // the lattice, the seed, the frame number or the configuration since
+    const bool xdec_ok = d->occ_valid && d->xdec_valid && d->xdec_cfg == d->cfg_index && d->xdec_cur == d->cur &&
+                         d->xdec_frame == d->next_frame && d->xdec_epoch == d->seed_epoch;
+    if (brick && !d->occ_valid) rebuild_occupancy(d);
+    if (!brick) d->occ_valid = false;  // the tile pipeline does not keep the bitmaps
+    if (kind == KIND_STREAM && !d->groups_sorted) sort_groups(d);
+    d->xdec_valid = false;
+    if (kind == KIND_STREAM && !xdec_ok) launch_stream_pass0(d);
     uint32_t k = 0;
     if (batched) {
         if (d->cur == 1 && k < n) {
@@ -775,6 +1024,15 @@ static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched) {
             d->cur ^= 1;
         }
     }
+    d->next_frame += n;
+    if (kind == KIND_STREAM) {
+        // the last frame's pass 3 made the x-decisions of frame next_frame
+        d->xdec_valid = true;
+        d->xdec_cfg = d->cfg_index;
+        d->xdec_cur = d->cur;
+        d->xdec_frame = d->next_frame;
+        d->xdec_epoch = d->seed_epoch;
+    }
 }
 
 void prod_step(DeviceProd* d, uint32_t n_steps, uint64_t seed, int precision, uint64_t frame0, uint32_t write_freq,
@@ -796,6 +1054,7 @@ void prod_step(DeviceProd* d, uint32_t n_steps, uint64_t seed, int precision, ui
     const uint32_t f32 = (uint32_t)frame0;
     CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, &f32, 4, cudaMemcpyHostToDevice, d->stream));
     CS_CUDA(cudaStreamSynchronize(d->stream));
+    d->next_frame = frame0;
     if (!sample_frames.empty() && d->sample_ring.n < sample_frames.size() * d->S1)
         d->sample_ring.alloc(sample_frames.size() * d->S1);
     for (size_t i = 0; i < sample_frames.size(); i++) {
@@ -1005,6 +1264,7 @@ float prod_time_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched)
         uint32_t f32 = (uint32_t)frame0;
         CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, &f32, 4, cudaMemcpyHostToDevice, d->stream));
         CS_CUDA(cudaStreamSynchronize(d->stream));
+        d->next_frame = frame0;
         CS_CUDA(cudaEventRecord(a, d->stream));
         run_frames_nosync(d, n, batched);
         CS_CUDA(cudaEventRecord(b, d->stream));
@@ -1067,6 +1327,7 @@ int prod_autotune(DeviceProd* d, uint32_t frames, uint64_t frame0, bool batched,
         CS_CUDA(cudaMemcpyAsync(d->slots[cur0].p, keep.p, bytes, cudaMemcpyDeviceToDevice, d->stream));
         CS_CUDA(cudaMemcpyAsync(d->counts.p, keep_counts.p, d->counts.bytes(), cudaMemcpyDeviceToDevice, d->stream));
         CS_CUDA(cudaMemcpyAsync(d->diag.p, keep_diag.p, PD_N * 4, cudaMemcpyDeviceToDevice, d->stream));
+        CS_CUDA(cudaMemsetAsync(d->counters.p, 0, d->counters.bytes(), d->stream));  // parity cur0 starts afresh
         CS_CUDA(cudaStreamSynchronize(d->stream));
         d->cur = cur0;
         d->occ_valid = false;

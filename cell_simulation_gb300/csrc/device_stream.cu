@@ -1,0 +1,461 @@
+// device_stream.cu — the four passes of the sweep-stream step and their
+// launchers (see stream_kernel.cuh for the scheme).
+#include <cuda_runtime.h>
+
+#include "cuda_check.h"
+#include "stream_kernel.cuh"
+
+namespace cellsim {
+
+namespace {
+
+// Per-lane words of a warp's current group, kept in shared memory so that
+// the lane running an item can read the words of the item's lane.
+enum : int {
+    F_OCC, F_M, F_P, F_WK, F_BS,     // own word: content, movers down / up, work and base of the producing pass
+    F_LOCC, F_LP, F_LWK, F_LBS,      // lower neighbour's word (previous word of the row in the Z sweep)
+    F_HOCC, F_HM, F_HWK, F_HBS,      // upper neighbour's word (next word of the row in the Z sweep)
+    F_OLD, F_OWK, F_OBS, F_Y, F_KK,  // old destination word, this pass's work and base, the lane's row and word
+    F_VROW, F_CODE,                  // first voxel of the lane's row, the word's uniform region code (or 0)
+    NF
+};
+constexpr int LIST = 1024;  // one group holds at most 32 words x 32 bits
+
+}  // namespace
+
+// u32 words of one warp's shared-memory area: fields, three accumulators,
+// the item list (u16) and the warp's species deltas
+__host__ __device__ constexpr size_t stream_warp_words(uint32_t S1) { return (size_t)NF * 32 + 96 + LIST / 2 + S1; }
+
+size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words) {
+    return ((size_t)(NT / 32) * stream_warp_words(S1) + PD_N + thr_words) * 4;
+}
+
+template <int K>
+__device__ __forceinline__ void rec_load(const uint4* rec, uint32_t i, Vox<K>& c, uint4& t) {
+    const uint4 a = __ldg(rec + 2 * (size_t)i);
+    t = __ldg(rec + 2 * (size_t)i + 1);
+    c.w[0] = (uint64_t)a.x | ((uint64_t)a.y << 32);
+    if constexpr (K == 16) c.w[1] = (uint64_t)a.z | ((uint64_t)a.w << 32);
+}
+
+template <int K>
+__device__ __forceinline__ void rec_store(uint4* rec, uint32_t i, const Vox<K>& c, const uint4& t) {
+    uint4 a;
+    a.x = (uint32_t)c.w[0];
+    a.y = (uint32_t)(c.w[0] >> 32);
+    if constexpr (K == 16) {
+        a.z = (uint32_t)c.w[1];
+        a.w = (uint32_t)(c.w[1] >> 32);
+    } else {
+        a.z = 0u;
+        a.w = 0u;
+    }
+    rec[2 * (size_t)i] = a;
+    rec[2 * (size_t)i + 1] = t;
+}
+
+__device__ __forceinline__ uint32_t below(uint32_t m, uint32_t bit) { return (uint32_t)__popc(m & (bit - 1u)); }
+
+// PASS 0: x-decisions; 1: X sweep + y-decisions; 2: Y sweep + z-decisions;
+// 3: Z sweep + reactions + store.
+template <int K, int PASS, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams SP) {
+    constexpr int NW = NT / 32;
+    const ProdParams& P = SP.P;
+    extern __shared__ __align__(16) uint32_t sm[];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const uint32_t S1 = P.T.S1, NC = P.T.NC;
+    uint32_t* f = sm + (size_t)w * stream_warp_words(S1);  // [NF][32]
+    uint32_t* acc = f + NF * 32;                            // [3][32]: content, movers down, movers up
+    uint16_t* list = reinterpret_cast<uint16_t*>(acc + 96);
+    int32_t* s_delta = reinterpret_cast<int32_t*>(acc + 96 + LIST / 2);  // [S1] this warp's species deltas
+    uint32_t* s_diag = sm + (size_t)NW * stream_warp_words(S1);        // [PD_N]
+    uint32_t* s_thr = s_diag + PD_N;
+    const uint32_t frame = P.stepbuf[P.parity];
+    if (blockIdx.x == 0 && tid == 0) {
+        for (uint32_t i = 0; i < P.n_reset; i++) P.reset[i] = 0u;
+        if (PASS == 3 && P.advance) P.stepbuf[P.parity ^ 1u] = frame + 1u;
+    }
+    const uint32_t* thr = P.T.thr;
+    if (P.thr_smem) {
+        const uint32_t nt = NC * NC * S1;
+        for (uint32_t i = tid; i < nt; i += NT) s_thr[i] = P.T.thr[i];
+        thr = s_thr;
+    }
+    for (uint32_t s = lane; s < S1; s += 32) s_delta[s] = 0;
+    for (int i = tid; i < PD_N; i += NT) s_diag[i] = 0u;
+    __syncthreads();
+    const bool zero_order = P.T.n_zero_order != 0u;
+    const bool all_react = zero_order || P.reservoir != nullptr;
+    uint32_t cur_cidx = 0xFFFFFFFFu;
+    // this warp's species deltas into the counts of replicate cur_cidx
+    auto flush = [&]() {
+        __syncwarp();
+        if (cur_cidx != 0xFFFFFFFFu)
+            for (uint32_t s = lane; s < S1; s += 32) {
+                const int32_t dl = s_delta[s];
+                if (dl) {
+                    atomicAdd(P.counts + (size_t)cur_cidx * S1 + s, (unsigned long long)(long long)dl);
+                    s_delta[s] = 0;
+                }
+            }
+        __syncwarp();
+    };
+    auto trow = [&](uint32_t a, uint32_t b) -> const uint32_t* { return thr + ((size_t)a * NC + b) * S1; };
+
+    const uint32_t TW = gridDim.x * NW;
+    // groups from the pass's counter (one atomic per group, fetched a group ahead), else round-robin
+    auto fetch = [&]() -> uint32_t {
+        uint32_t q = 0u;
+        if (lane == 0) q = atomicAdd(SP.queue, 1u);
+        return __shfl_sync(0xffffffffu, q, 0);
+    };
+    uint32_t g = SP.queue ? fetch() : blockIdx.x * NW + (uint32_t)w;
+    while (g < SP.n_groups) {
+        const uint32_t g_next = SP.queue ? fetch() : g + TW;
+        const WordGroup G = SP.groups[g];
+        const RepDesc rd = P.reps[G.rep];
+        if constexpr (PASS == 3) {
+            if (rd.counts_index != cur_cidx) {
+                flush();
+                cur_cidx = rd.counts_index;
+            }
+        }
+        const int X = (int)rd.X, Y = (int)rd.Y, Z = (int)rd.Z;
+        const uint32_t Wz = rd.Wz;
+        const int nk = (int)G.nk;
+        const bool valid = lane < (int)(G.nrows * G.nk);
+        const int yl = valid ? lane / nk : 0;
+        const int x = (int)G.x, y = (int)G.y0 + yl, kk = (int)G.k0 + (lane - yl * nk);
+        const uint64_t wo = rd.obase + ((uint64_t)x * (uint64_t)Y + (uint64_t)y) * Wz + (uint64_t)kk;
+        const int zb = 32 * kk;
+        const uint32_t colm = !valid ? 0u : (Z - zb >= 32 ? 0xFFFFFFFFu : ((1u << (Z - zb)) - 1u));
+        uint32_t work = 0u, old = 0u, moving = 0u;  // moving: bits whose content changes along the axis
+        uint32_t own_occ = 0u, own_m = 0u, own_p = 0u, own_wk = 0u, own_bs = 0u;
+        uint32_t lo_occ = 0u, lo_p = 0u, lo_wk = 0u, lo_bs = 0u, hi_occ = 0u, hi_m = 0u, hi_wk = 0u, hi_bs = 0u;
+        if (valid) {
+            if constexpr (PASS == 0) {
+                own_occ = P.osrc[wo];
+                work = own_occ;
+            } else {
+                own_occ = SP.in.occ[wo];
+                own_m = SP.in.mv_m[wo];
+                own_p = SP.in.mv_p[wo];
+                own_wk = SP.in.work[wo];
+                own_bs = SP.in.base[wo];
+                // neighbour words: other rows for the X and Y sweeps, the row's adjacent words for Z
+                const uint64_t st = PASS == 1 ? (uint64_t)Y * Wz : PASS == 2 ? (uint64_t)Wz : 1ull;
+                const bool hl = PASS == 1 ? x > 0 : PASS == 2 ? y > 0 : kk > 0;
+                const bool hh = PASS == 1 ? x + 1 < X : PASS == 2 ? y + 1 < Y : kk + 1 < (int)Wz;
+                if (hl) {
+                    lo_occ = SP.in.occ[wo - st];
+                    lo_p = SP.in.mv_p[wo - st];
+                    lo_wk = SP.in.work[wo - st];
+                    lo_bs = SP.in.base[wo - st];
+                }
+                if (hh) {
+                    hi_occ = SP.in.occ[wo + st];
+                    hi_m = SP.in.mv_m[wo + st];
+                    hi_wk = SP.in.work[wo + st];
+                    hi_bs = SP.in.base[wo + st];
+                }
+                if constexpr (PASS == 3) {
+                    old = P.odst[wo];
+                    const uint32_t from_lo = (own_p << 1) | (lo_p >> 31), from_hi = (own_m >> 1) | (hi_m << 31);
+                    work = (own_occ | from_lo | from_hi | old | (all_react ? colm : 0u)) & colm;
+                    moving = own_m | own_p | from_lo | from_hi;
+                } else {
+                    work = (own_occ | lo_p | hi_m) & colm;
+                    moving = own_m | own_p | lo_p | hi_m;
+                }
+            }
+        }
+        f[F_OCC * 32 + lane] = own_occ;
+        f[F_M * 32 + lane] = own_m;
+        f[F_P * 32 + lane] = own_p;
+        f[F_WK * 32 + lane] = own_wk;
+        f[F_BS * 32 + lane] = own_bs;
+        f[F_LOCC * 32 + lane] = lo_occ;
+        f[F_LP * 32 + lane] = lo_p;
+        f[F_LWK * 32 + lane] = lo_wk;
+        f[F_LBS * 32 + lane] = lo_bs;
+        f[F_HOCC * 32 + lane] = hi_occ;
+        f[F_HM * 32 + lane] = hi_m;
+        f[F_HWK * 32 + lane] = hi_wk;
+        f[F_HBS * 32 + lane] = hi_bs;
+        f[F_OLD * 32 + lane] = old;
+        f[F_Y * 32 + lane] = (uint32_t)y;
+        f[F_KK * 32 + lane] = (uint32_t)kk;
+        f[F_VROW * 32 + lane] = ((uint32_t)x * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z;
+        f[F_CODE * 32 + lane] = (rd.flags & 1u) ? 1u : (SP.wcode && valid) ? (uint32_t)SP.wcode[wo] : 0u;
+        // List the work bits in three classes, so that the lanes of a warp mostly run the same
+        // path: voxels with a record of the previous pass whose content does not change along
+        // the axis, those whose content changes, and those without a record (arrivals, and in
+        // the Z sweep voxels to clear), whose Philox blocks are then evaluated by full warps.
+        // Records are indexed by the work bits alone, whatever the list order.
+        const uint32_t cls_a = PASS == 0 ? work : (work & own_occ & ~moving);
+        const uint32_t cls_b = PASS == 0 ? 0u : (work & own_occ & moving);
+        const uint32_t na = (uint32_t)__popc(cls_a), nb = (uint32_t)__popc(cls_b), nw = (uint32_t)__popc(work);
+        uint32_t incl = na | (nb << 16), inw = nw;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o), uw = __shfl_up_sync(0xffffffffu, inw, o);
+            if (lane >= o) {
+                incl += u;
+                inw += uw;
+            }
+        }
+        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31), total = __shfl_sync(0xffffffffu, inw, 31);
+        const uint32_t total_a = tot & 0xFFFFu, total_ab = total_a + (tot >> 16);
+        const uint32_t ex = incl - (na | (nb << 16)), exa = ex & 0xFFFFu, exb = ex >> 16, exw = inw - nw;
+        f[F_OWK * 32 + lane] = work;
+        f[F_OBS * 32 + lane] = (uint32_t)G.rbase + exw;
+        acc[lane] = 0u;
+        acc[32 + lane] = 0u;
+        acc[64 + lane] = 0u;
+        {
+            auto put = [&](uint32_t bits, uint32_t o) {
+                while (bits) {
+                    const int b = __ffs((int)bits) - 1;
+                    bits &= bits - 1u;
+                    list[o++] = (uint16_t)((lane << 5) | b);
+                }
+            };
+            put(cls_a, exa);
+            put(cls_b, total_a + exb);
+            put(work & ~(cls_a | cls_b), total_ab + (exw - exa - exb));
+        }
+        __syncwarp();
+
+        const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
+        const uint8_t* rpad = P.region_pad + rd.rbase;
+        const uint64_t Zr = rd.Zr;
+        // region code (id + 1) of voxel (xx, yy, zz) of the window of a word with uniform code uc
+        // (0: look it up); 0 outside the lattice
+        auto code = [&](uint32_t uc, int xx, int yy, int zz) -> uint32_t {
+            if ((unsigned)xx >= (unsigned)X || (unsigned)yy >= (unsigned)Y || (unsigned)zz >= (unsigned)Z) return 0u;
+            if (uc) return uc;
+            return __ldg(rpad + ((uint64_t)xx * (uint64_t)Y + (uint64_t)yy) * Zr + (uint64_t)zz + 2u);
+        };
+        const uint32_t YZ = (uint32_t)Y * (uint32_t)Z;
+        for (uint32_t t = (uint32_t)lane; t < total; t += 32) {
+            const uint32_t e = list[t];
+            const int i = (int)(e >> 5), b = (int)(e & 31u);
+            const uint32_t bit = 1u << b;
+            const int yy = (int)f[F_Y * 32 + i], zz = 32 * (int)f[F_KK * 32 + i] + b;
+            const uint32_t v = f[F_VROW * 32 + i] + (uint32_t)zz;
+            const uint32_t uc = f[F_CODE * 32 + i];
+            const uint32_t ri = f[F_OBS * 32 + i] + below(f[F_OWK * 32 + i], bit);  // this pass's record of the item
+            if constexpr (PASS == 0) {
+                const Vox<K> own = ld_vox_g<K>(P.src + (rd.base + v) * K);
+                const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
+                const uint32_t rs = code(uc, x, yy, zz);
+                const uint32_t d = decide_moves<K>(own, v, frame, 0u, trow(rs, code(uc, x - 1, yy, zz)),
+                                                   trow(rs, code(uc, x + 1, yy, zz)), k0, k1, b0.x);
+                rec_store<K>(SP.rec_out, ri, own, make_uint4(d, b0.y, b0.z, b0.w));
+                if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
+                if (d >> 16) atomicOr(acc + 64 + i, bit);
+            } else {
+                const uint32_t occ = f[F_OCC * 32 + i];
+                Vox<K> own = vox_zero<K>(), lo = vox_zero<K>(), hi = vox_zero<K>();
+                uint32_t dme = 0u, dlo = 0u, dhi = 0u;
+                uint4 tw = make_uint4(0u, 0u, 0u, 0u);
+                const bool own_in = (occ & bit) != 0u;
+                if (own_in) {
+                    rec_load<K>(SP.rec_in, f[F_BS * 32 + i] + below(f[F_WK * 32 + i], bit), own, tw);
+                    dme = tw.x;
+                }
+                // a neighbour's record is needed when it sends to this voxel or receives from it
+                bool need_lo, need_hi;
+                uint32_t ilo, ihi;
+                if constexpr (PASS == 3) {
+                    const uint32_t m = f[F_M * 32 + i], p = f[F_P * 32 + i];
+                    if (b > 0) {
+                        const uint32_t lb = bit >> 1;
+                        need_lo = (occ & lb) && ((m & bit) || (p & lb));
+                        ilo = f[F_BS * 32 + i] + below(f[F_WK * 32 + i], lb);
+                    } else {
+                        need_lo = (f[F_LOCC * 32 + i] >> 31) && ((m & bit) || (f[F_LP * 32 + i] >> 31));
+                        ilo = f[F_LBS * 32 + i] + below(f[F_LWK * 32 + i], 0x80000000u);
+                    }
+                    if (b < 31) {
+                        const uint32_t hb = bit << 1;
+                        need_hi = (occ & hb) && ((p & bit) || (m & hb));
+                        ihi = f[F_BS * 32 + i] + below(f[F_WK * 32 + i], hb);
+                    } else {
+                        need_hi = (f[F_HOCC * 32 + i] & 1u) && ((p & bit) || (f[F_HM * 32 + i] & 1u));
+                        ihi = f[F_HBS * 32 + i];
+                    }
+                } else {
+                    need_lo = (f[F_LOCC * 32 + i] & bit) && ((f[F_M * 32 + i] | f[F_LP * 32 + i]) & bit);
+                    need_hi = (f[F_HOCC * 32 + i] & bit) && ((f[F_P * 32 + i] | f[F_HM * 32 + i]) & bit);
+                    ilo = f[F_LBS * 32 + i] + below(f[F_LWK * 32 + i], bit);
+                    ihi = f[F_HBS * 32 + i] + below(f[F_HWK * 32 + i], bit);
+                }
+                if (need_lo) {
+                    uint4 tl;
+                    rec_load<K>(SP.rec_in, ilo, lo, tl);
+                    dlo = tl.x;
+                }
+                if (need_hi) {
+                    uint4 th;
+                    rec_load<K>(SP.rec_in, ihi, hi, th);
+                    dhi = th.x;
+                }
+                const uint32_t vs = PASS == 1 ? YZ : PASS == 2 ? (uint32_t)Z : 1u;
+                Vox<K> r = combine<K>(own, dme, lo, dlo, hi, dhi, v, v - vs, v + vs, frame, (uint32_t)(PASS - 1));
+                if constexpr (PASS == 1 || PASS == 2) {
+                    if (!vox_empty<K>(r)) {
+                        // this voxel's Philox words: carried in its record, or evaluated here
+                        uint32_t wd, wn1, wn2;
+                        if (own_in) {
+                            wd = tw.y;
+                            wn1 = tw.z;
+                            wn2 = tw.w;
+                        } else {
+                            const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
+                            wd = PASS == 1 ? b0.y : b0.z;
+                            wn1 = PASS == 1 ? b0.z : b0.w;
+                            wn2 = PASS == 1 ? b0.w : 0u;
+                        }
+                        const uint32_t rs = code(uc, x, yy, zz);
+                        const uint32_t clo = PASS == 1 ? code(uc, x, yy - 1, zz) : code(uc, x, yy, zz - 1);
+                        const uint32_t chi = PASS == 1 ? code(uc, x, yy + 1, zz) : code(uc, x, yy, zz + 1);
+                        const uint32_t d =
+                            decide_moves<K>(r, v, frame, (uint32_t)PASS, trow(rs, clo), trow(rs, chi), k0, k1, wd);
+                        rec_store<K>(SP.rec_out, ri, r, make_uint4(d, wn1, wn2, 0u));
+                        atomicOr(acc + i, bit);
+                        if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
+                        if (d >> 16) atomicOr(acc + 64 + i, bit);
+                    }
+                } else {
+                    const uint32_t rv = P.reservoir ? (uint32_t)P.reservoir[rd.base + v] : 0u;
+                    if (rv != 0u || zero_order || !vox_empty<K>(r)) {
+                        const uint32_t w3 = own_in ? tw.y : d_philox(v, frame, 0u, 0u, k0, k1).w;
+                        const bool calm =
+                            rv == 0u && !zero_order &&
+                            calm_voxel<K>(r, w3, P.T.quiet + (size_t)rd.counts_index * S1 * P.T.QS, P.T.QS,
+                                          P.T.one + (size_t)rd.counts_index * S1 * 3, P.T.g23 + 2 * rd.counts_index,
+                                          P.T.tau);
+                        if (!calm)
+                            react_voxel<K>(r, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, P.T, s_delta,
+                                           s_diag, w3);
+                    }
+                    if (!vox_empty<K>(r)) {
+                        st_vox_g<K>(P.dst + (rd.base + v) * K, r);
+                        atomicOr(acc + i, bit);
+                        if (SP.fuse) {
+                            // pass 0 of the next frame for this voxel
+                            const uint32_t nf = frame + 1u;
+                            const U4 b0 = d_philox(v, nf, 0u, 0u, k0, k1);
+                            const uint32_t rs = code(uc, x, yy, zz);
+                            const uint32_t d = decide_moves<K>(r, v, nf, 0u, trow(rs, code(uc, x - 1, yy, zz)),
+                                                               trow(rs, code(uc, x + 1, yy, zz)), k0, k1, b0.x);
+                            rec_store<K>(SP.rec_out, ri, r, make_uint4(d, b0.y, b0.z, b0.w));
+                            if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
+                            if (d >> 16) atomicOr(acc + 64 + i, bit);
+                        }
+                    } else if (f[F_OLD * 32 + i] & bit) {
+                        st_vox_g<K>(P.dst + (rd.base + v) * K, vox_zero<K>());
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (valid) {
+            if constexpr (PASS == 0) {
+                SP.out.mv_m[wo] = acc[32 + lane];
+                SP.out.mv_p[wo] = acc[64 + lane];
+                SP.out.work[wo] = work;
+                SP.out.base[wo] = f[F_OBS * 32 + lane];
+            } else if constexpr (PASS == 3) {
+                P.odst[wo] = acc[lane];
+                if (SP.fuse) {
+                    SP.out.mv_m[wo] = acc[32 + lane];
+                    SP.out.mv_p[wo] = acc[64 + lane];
+                    SP.out.work[wo] = work;
+                    SP.out.base[wo] = f[F_OBS * 32 + lane];
+                }
+            } else {
+                SP.out.occ[wo] = acc[lane];
+                SP.out.mv_m[wo] = acc[32 + lane];
+                SP.out.mv_p[wo] = acc[64 + lane];
+                SP.out.work[wo] = work;
+                SP.out.base[wo] = f[F_OBS * 32 + lane];
+            }
+        }
+        __syncwarp();
+        g = g_next;
+    }
+    if constexpr (PASS == 3) flush();
+    __syncthreads();
+    for (int i = tid; i < PD_N; i += NT)
+        if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
+}
+
+// ------------------------------------------------------------------ launchers
+
+namespace {
+struct Variant {
+    int NT, MINB, MINB3;  // threads per block, minimum resident blocks per SM of passes 0-2 and of pass 3
+};
+// compiled launch shapes; pass 3 (reactions) needs more registers than the sweeps
+constexpr Variant kVariants[] = {{256, 2, 2}, {256, 4, 4}, {256, 4, 3}};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+template <int K, int NT, int MINB, int MINB3>
+void* pass_fn(int pass) {
+    switch (pass) {
+        case 0: return reinterpret_cast<void*>(&sweep_pass_kernel<K, 0, NT, MINB>);
+        case 1: return reinterpret_cast<void*>(&sweep_pass_kernel<K, 1, NT, MINB>);
+        case 2: return reinterpret_cast<void*>(&sweep_pass_kernel<K, 2, NT, MINB>);
+        default: return reinterpret_cast<void*>(&sweep_pass_kernel<K, 3, NT, MINB3>);
+    }
+}
+
+template <int K>
+void* fn_of(int variant, int pass) {
+    switch (variant) {
+        case 0: return pass_fn<K, 256, 2, 2>(pass);
+        case 1: return pass_fn<K, 256, 4, 4>(pass);
+        case 2: return pass_fn<K, 256, 4, 3>(pass);
+        default: return nullptr;
+    }
+}
+
+void* kernel_of(int K, int variant, int pass) {
+    if (pass < 0 || pass > 3) return nullptr;
+    return K == 16 ? fn_of<16>(variant, pass) : K == 8 ? fn_of<8>(variant, pass) : nullptr;
+}
+}  // namespace
+
+int stream_variant_count() { return kNumVariants; }
+int stream_variant_threads(int variant) { return variant >= 0 && variant < kNumVariants ? kVariants[variant].NT : 0; }
+
+bool stream_launch(int K, int variant, int pass, int grid, size_t smem, cudaStream_t s, const StreamParams& SP) {
+    void* fn = kernel_of(K, variant, pass);
+    if (!fn) return false;
+    void* args[] = {const_cast<StreamParams*>(&SP)};
+    CS_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3((unsigned)kVariants[variant].NT), args, smem, s));
+    return true;
+}
+
+int stream_blocks_per_sm(int K, int variant, int pass, size_t smem) {
+    void* fn = kernel_of(K, variant, pass);
+    if (!fn) return 0;
+    int n = 0;
+    CS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kVariants[variant].NT, smem));
+    return n;
+}
+
+void stream_set_attrs(int K, int variant, size_t smem) {
+    for (int pass = 0; pass < 4; pass++) {
+        void* fn = kernel_of(K, variant, pass);
+        if (!fn) continue;
+        CS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    }
+}
+
+}  // namespace cellsim

@@ -1,0 +1,93 @@
+// stream_kernel.cuh — the sweep-stream form of the production step.
+//
+// One frame is four barrier-free passes over the occupancy bitmaps:
+//
+//   pass 0  x-move decisions of every occupied voxel of the source lattice
+//   pass 1  X sweep (new content along x), y-move decisions
+//   pass 2  Y sweep, z-move decisions
+//   pass 3  Z sweep, reactions, store into the destination lattice and its
+//           occupancy bitmap; voxels that became empty get zeros
+//
+// Pass 0 of frame f + 1 needs only the final contents of frame f, so pass 3
+// also makes the next frame's x-decisions while the contents are in
+// registers, and consecutive frames run passes 1-3 only.  The host runs a
+// standalone pass 0 when those decisions are absent or stale (the first
+// frame, a new lattice, seed, frame number or step configuration).
+//
+// A warp takes a word group: up to 32 bitmap words of one replicate, one per
+// lane (rows of one x plane, z fastest).  Each lane builds the word's work
+// mask from its own words and those of the neighbouring rows (or, for the
+// Z sweep, the neighbouring bits), the warp lists the set bits in shared
+// memory and runs the list with every lane busy.  Nothing synchronises
+// beyond the warp, so every SM keeps as many warps in flight as its
+// registers allow.
+//
+// Between passes a voxel's state is a 32-byte record (content, move
+// decisions, and the words of its Philox block B(v, 0) that later passes
+// still need).  Records are packed per group: the record of work bit b of a
+// word is base[word] + popcount(work[word] below b), where work and base are
+// the producing pass's per-word arrays.  The records a pass writes are
+// therefore contiguous, so L2 holds whole lines of them between passes.
+//
+// The per-voxel operations (decide_moves, combine, calm_voxel,
+// react_voxel) are those of the brick pass and the tile pipeline, so all
+// three forms compute the same lattice bit for bit.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "prod_common.cuh"
+#include "prod_kernel.cuh"
+
+namespace cellsim {
+
+// Lane i of a group holds word k0 + i % nk of row (x, y0 + i / nk).
+struct WordGroup {
+    uint32_t rep, x, y0, nrows, k0, nk;
+    uint64_t rbase;  // first record index of the group (capacity nrows * nk * 32 records)
+};
+static_assert(sizeof(WordGroup) == 32, "WordGroup is 32 bytes");
+
+// Per-word arrays of one pass boundary (indexed like the occupancy bitmaps).
+struct SweepWords {
+    uint32_t* occ;   // voxels with content after the sweep
+    uint32_t* mv_m;  // voxels whose next-axis decision moves something to the lower neighbour
+    uint32_t* mv_p;  // ... to the upper neighbour
+    uint32_t* work;  // work mask of the producing pass (record index)
+    uint32_t* base;  // first record index of the word
+};
+
+struct StreamParams {
+    ProdParams P;
+    const WordGroup* groups;
+    uint32_t n_groups;
+    uint32_t* queue;  // group counter of this pass (zero at launch); null: groups dealt round-robin
+    // per bitmap word: the region code shared by every lattice voxel of the word's window
+    // (rows x-1..x+1, y-1..y+1, z from 32k-1 to 32k+32), or 0; null for one-region replicates
+    const uint8_t* wcode;
+    // pass 3: nonzero when it also makes the next frame's x-decisions (the
+    // work of pass 0 for frame + 1) from the final contents, so that the next
+    // frame starts at pass 1
+    uint32_t fuse;
+    SweepWords in;   // produced by the previous pass (pass 0: unused)
+    SweepWords out;  // produced by this pass (pass 3: the next frame's x-decisions when fused)
+    const uint4* rec_in;
+    uint4* rec_out;
+};
+
+// Compiled launch shapes ("variants": threads per block and minimum resident
+// blocks per SM) of the four passes.
+int stream_variant_count();
+int stream_variant_threads(int variant);
+// Launches pass `pass` (0..3) of variant `variant` for slot count K.
+// Returns false when no such kernel is compiled.
+bool stream_launch(int K, int variant, int pass, int grid, size_t smem, cudaStream_t s, const StreamParams& SP);
+// Resident blocks per SM of that kernel with `smem` dynamic shared memory.
+int stream_blocks_per_sm(int K, int variant, int pass, size_t smem);
+// Dynamic shared memory of one block of NT threads.
+size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words);
+// Sets the kernel attributes (shared-memory size and carveout) of every pass.
+void stream_set_attrs(int K, int variant, size_t smem);
+
+}  // namespace cellsim

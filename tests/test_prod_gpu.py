@@ -111,6 +111,49 @@ def test_one_region_windows_match_oracle(orc, K):
         assert np.array_equal(got_d[:4], want_d[:4]), (ti, got_d, want_d)
 
 
+def stream_tilings(K):
+    return [i for i, (t, (kind, _)) in enumerate(zip(tiling_variants(), tiling_kinds())) if t[0] == K and kind == 2]
+
+
+@pytest.mark.parametrize("K", [8, 16])
+def test_sweep_stream_matches_oracle(orc, K):
+    """The sweep stream on the crowded patchy lattice and on a multi-region lattice with
+    reservoirs, in runs split over several step calls: each call after the first starts from the
+    x-decisions that the previous call's last pass made.  The frames are the oracle's."""
+    models = (lambda: patchy_model(K=K),
+              lambda: multi_region_model(res=(9, 8, 40), K=K, counts=(70, 60, 50, 40), reservoir=True))
+    assert stream_tilings(K)
+    for mk in models:
+        want_s, want_c, want_d = oracle_prod(orc, mk(), 24, seed=77)
+        for ti in stream_tilings(K):
+            got_s, got_c, got_d = gpu_prod(mk(), 24, 77, tiling=ti, chunks=5)
+            assert np.array_equal(got_s, want_s), (ti, np.flatnonzero(got_s != want_s)[:8])
+            assert np.array_equal(got_c, want_c), ti
+            assert np.array_equal(got_d[:4], want_d[:4]), (ti, got_d, want_d)
+
+
+def test_sweep_stream_recomputes_stale_decisions(orc):
+    """A seed change and a lattice upload between step calls make the next frame's x-decisions
+    (made by the last pass of the previous call) stale: the lattice still follows the oracle.
+    The upload comes after an odd number of frames, so the frame parity restarts at 0 while the
+    parity-0 work counters were used last (the brick pass is checked on that too)."""
+    mk = lambda: multi_region_model(res=(11, 13, 37), K=16, counts=(60, 50, 40, 30))
+    ref = mk()
+    want_s, want_c, _ = oracle_prod(orc, ref, 6, seed=11)
+    res, K, NR, S, R, tau, lam, tab = oracle_args(ref)
+    orc.prod_run(res, K, NR, S, R, tau, lam, tab, want_s, want_c, 12, 6, 9)
+    for ti in stream_tilings(16) + brick_tilings(16)[-1:]:
+        sim = mk()
+        sim.prepare_for_gpu(RNG_PHILOX, 0)
+        sim.set_tiling(ti)
+        sim.step_philox(6, 11)
+        sim.step_philox(5, 12)  # new seed
+        sim.set_lattice(sim.get_lattice()[0])  # same content, fresh upload
+        sim.step_philox(4, 12)
+        assert np.array_equal(sim.get_lattice()[0].astype(np.uint8), want_s), ti
+        assert np.array_equal(sim.counts(), want_c), ti
+
+
 def test_sparse_lattice_never_spills():
     sim = multi_region_model(res=(24, 20, 40), K=16, counts=(60, 50, 40, 30))
     _, _, d = gpu_prod(sim, 10, 5)
