@@ -355,7 +355,7 @@ def main():
         "gpu_launches": args.steps * launches_per_frame(variant),
         "clocks": clk,
         "diagnostics": {"events": int(diag[0]), "rejected_capacity": int(diag[1]), "event_cap": int(diag[2]),
-                        "fp64_selections": int(diag[3])},
+                        "fp64_selections": int(diag[3]), "ssa_voxels": int(diag[6])},
     }
     line.update(extras)
     print(json.dumps(line), flush=True)

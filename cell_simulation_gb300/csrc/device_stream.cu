@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                 if constexpr (PASS == 3) {
                     old = P.odst[wo];
                     const uint32_t from_lo = (own_p << 1) | (lo_p >> 31), from_hi = (own_m >> 1) | (hi_m << 31);
-                    work = (own_occ | from_lo | from_hi | old | (all_react ? colm : 0u)) & colm;
+                    work = (own_occ | from_lo | from_hi | (all_react ? colm : 0u)) & colm;
                     moving = own_m | own_p | from_lo | from_hi;
                 } else {
                     work = (own_occ | lo_p | hi_m) & colm;
@@ -191,8 +191,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         f[F_CODE * 32 + lane] = (rd.flags & 1u) ? 1u : (SP.wcode && valid) ? (uint32_t)SP.wcode[wo] : 0u;
         // List the work bits in three classes, so that the lanes of a warp mostly run the same
         // path: voxels with a record of the previous pass whose content does not change along
-        // the axis, those whose content changes, and those without a record (arrivals, and in
-        // the Z sweep voxels to clear), whose Philox blocks are then evaluated by full warps.
+        // the axis, those whose content changes, and those without a record (arrivals), whose
+        // Philox blocks are then evaluated by full warps.
         // Records are indexed by the work bits alone, whatever the list order.
         const uint32_t cls_a = PASS == 0 ? work : (work & own_occ & ~moving);
         const uint32_t cls_b = PASS == 0 ? 0u : (work & own_occ & moving);
@@ -356,8 +356,6 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                             if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
                             if (d >> 16) atomicOr(acc + 64 + i, bit);
                         }
-                    } else if (f[F_OLD * 32 + i] & bit) {
-                        st_vox_g<K>(P.dst + (rd.base + v) * K, vox_zero<K>());
                     }
                 }
             }
@@ -371,6 +369,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                 SP.out.base[wo] = f[F_OBS * 32 + lane];
             } else if constexpr (PASS == 3) {
                 P.odst[wo] = acc[lane];
+                // voxels the destination held that end the frame empty get zeros
+                for (uint32_t bits = old & ~acc[lane]; bits; bits &= bits - 1u)
+                    st_vox_g<K>(P.dst + (rd.base + f[F_VROW * 32 + lane] + (uint32_t)zb + (uint32_t)(__ffs((int)bits) - 1)) * K,
+                                vox_zero<K>());
                 if (SP.fuse) {
                     SP.out.mv_m[wo] = acc[32 + lane];
                     SP.out.mv_p[wo] = acc[64 + lane];

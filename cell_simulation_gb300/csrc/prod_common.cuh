@@ -39,7 +39,12 @@
 
 namespace cellsim {
 
-enum { PD_EVENTS = 0, PD_REJECT_CAP = 1, PD_EVENT_CAP = 2, PD_FP64_SEL = 3, PD_DENSE_BRICKS = 4, PD_LOST_BRICKS = 5, PD_N = 8 };
+// Diagnostic counters: events fired, events rejected for capacity, voxels that hit the event cap,
+// FP64 selections, bricks spilled to the second pass, bricks lost (never), voxels that ran the SSA.
+enum {
+    PD_EVENTS = 0, PD_REJECT_CAP = 1, PD_EVENT_CAP = 2, PD_FP64_SEL = 3, PD_DENSE_BRICKS = 4, PD_LOST_BRICKS = 5,
+    PD_SSA_VOXELS = 6, PD_N = 8
+};
 
 struct RepDesc {
     uint64_t base;   // first voxel of this replicate in the packed slot/reservoir arrays
@@ -319,6 +324,7 @@ __device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, u
                                          float mult, uint32_t rep, const ProdTables& T, int32_t* s_delta,
                                          uint32_t* s_diag, uint32_t w3) {
     if (T.R == 0) return false;
+    atomicAdd(s_diag + PD_SSA_VOXELS, 1u);
     uint32_t n = vox_n<K>(c);
     double td = 0.0;
     float tf = 0.0f;
