@@ -552,7 +552,8 @@ __global__ void __launch_bounds__(NT, MINB) brick_step_kernel(ProdParams P) {
                     else if (!WP && (PB2[jj] & bc)) w3 = W23[e2];
                     else w3 = d_philox(v, frame, 0u, 0u, k0, k1).w;
                     const bool calm = rv == 0u && !zero_order &&
-                                      calm_voxel<K>(r3, w3, quiet, P.T.QS, one_rep, P.T.g23 + 2 * rd.counts_index, P.T.tau);
+                                      calm_voxel<K>(r3, w3, quiet, P.T.QS, one_rep, P.T.g23 + 2 * rd.counts_index,
+                                                P.T.a2 ? P.T.a2 + (size_t)rd.counts_index * S1 * S1 : nullptr, P.T.tau);
                     if (!calm)
                         react_voxel<K>(r3, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, P.T, s_delta, s_bdiag,
                                        w3);

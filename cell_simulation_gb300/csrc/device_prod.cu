@@ -111,8 +111,9 @@ static const std::vector<KernelCfg>& all_cfgs() {
         // four CTAs of 6 warps / six CTAs of 5 warps per SM: small pools for sparse replicates (the
         // 512-replicate ensemble), where more bricks in flight per SM beat larger pools
         brick_cfg<8, 16, 8, 192, 4, 432, 432, 432>(11, 8), brick_cfg<8, 16, 8, 160, 6, 176, 176, 176>(11, 8),
-        // sweep stream: 256 threads, at least two / four blocks per SM (pass 3 of variant 2: three)
+        // sweep stream: 256 threads, at least two / four blocks per SM (pass 3 of variants 2, 3: three, two)
         stream_cfg(16, 0), stream_cfg(16, 1), stream_cfg(8, 0), stream_cfg(8, 1), stream_cfg(16, 2), stream_cfg(8, 2),
+        stream_cfg(16, 3), stream_cfg(8, 3),
     };
     return v;
 }
@@ -144,6 +145,7 @@ struct DeviceProd {
     DevBuf<float> one;
     DevBuf<uint32_t> quiet;
     DevBuf<float> g23;
+    DevBuf<float> a2;  // pair propensities (ProdTables::a2)
     DevBuf<WorkItem> spill;  // bricks handed from the brick pass to the second pass
     DevBuf<unsigned long long> sample_ring;  // species counts at the sample frames of one cs_step_philox
     std::vector<float> h_rate;
@@ -163,6 +165,7 @@ struct DeviceProd {
     DevBuf<uint4> rec[2];
     DevBuf<uint32_t> sw[14];
     DevBuf<uint8_t> wcode;  // per bitmap word: uniform region code of its window, or 0 (single lattices)
+    DevBuf<uint32_t> ssa_list;  // pass 3: output record indices of the voxels whose SSA runs in pass 4
     std::vector<WordGroup> h_groups;
     bool groups_sorted = false;  // groups dealt heaviest first (sorted once per group build)
     int stream_per_sm[4] = {0, 0, 0, 0};  // resident blocks per SM of the current stream passes
@@ -379,6 +382,35 @@ static void build_one_table(DeviceProd* d) {
     d->g23.alloc(g23.size());
     CS_CUDA(cudaMemcpy(d->g23.p, g23.data(), g23.size() * 4, cudaMemcpyHostToDevice));
     d->T.g23 = d->g23.p;
+    // second-order propensity of one particle pair (p, q) per replicate: the rates of the
+    // reactions whose reactants are exactly p and q, twice for p == q (n(n-1) counts each
+    // unordered pair of p twice), rounded up; tabulated beside the two-particle thresholds
+    d->T.a2 = nullptr;
+    if (QS == S1) {
+        std::vector<float> a2((size_t)d->n_rep * S1 * S1, 0.0f);
+        for (uint32_t ri = 0; ri < d->n_rep; ri++) {
+            std::vector<double> acc2((size_t)S1 * S1, 0.0);
+            for (uint32_t r = 0; r < d->R; r++) {
+                const uint32_t sp[3] = {d->h_rre[3 * r], d->h_rre[3 * r + 1], d->h_rre[3 * r + 2]};
+                uint32_t nz = 0, a = 0, b = 0;
+                for (int j = 0; j < 3; j++)
+                    if (sp[j]) {
+                        if (nz == 0) a = sp[j];
+                        else b = sp[j];
+                        nz++;
+                    }
+                if (nz != 2) continue;
+                const double k = (double)d->h_rate[r] * (double)d->h_reps[ri].rate_mult * (a == b ? 2.0 : 1.0);
+                acc2[(size_t)a * S1 + b] += k;
+                if (a != b) acc2[(size_t)b * S1 + a] += k;
+            }
+            for (size_t i = 0; i < acc2.size(); i++)
+                a2[(size_t)ri * S1 * S1 + i] = acc2[i] > 0.0 ? std::nextafter((float)acc2[i], INFINITY) : 0.0f;
+        }
+        d->a2.alloc(a2.size());
+        CS_CUDA(cudaMemcpy(d->a2.p, a2.data(), a2.size() * 4, cudaMemcpyHostToDevice));
+        d->T.a2 = d->a2.p;
+    }
     d->quiet.alloc(quiet.size());
     CS_CUDA(cudaMemcpy(d->quiet.p, quiet.data(), quiet.size() * 4, cudaMemcpyHostToDevice));
     d->T.quiet = d->quiet.p;
@@ -551,6 +583,7 @@ static void build_groups(DeviceProd* d) {
         if (d->rec[b].n < 2 * rb) d->rec[b].alloc(2 * rb);  // two uint4 per record
     for (auto& a : d->sw)
         if (a.n < d->occ_words) a.alloc(d->occ_words);
+    if (d->ssa_list.n < rb) d->ssa_list.alloc(rb);  // at most one entry per record
 }
 
 // Deals each replicate's word groups heaviest first (most occupied voxels in
@@ -596,7 +629,7 @@ static size_t cfg_smem(const DeviceProd* d, const KernelCfg& cfg) {
 
 static void set_attrs(const DeviceProd* d, const KernelCfg& cfg) {
     if (cfg.kind == KIND_STREAM) {
-        stream_set_attrs(cfg.K, cfg.variant, cfg_smem(d, cfg));
+        stream_set_attrs(cfg.K, cfg.variant, cfg_smem(d, cfg), stream_ssa_smem(d->S1, d->R));
         return;
     }
     CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg_smem(d, cfg)));
@@ -663,9 +696,10 @@ static int grid_for(DeviceProd* d, const KernelCfg& cfg, uint32_t n_items) {
 }
 
 // Counters of launch group g (0 = all replicates, 1 + r = replicate r alone)
-// for frame parity p: [0] work queue of the first launch, [1] spilled bricks,
-// [2] work queue of the spill pass.
-static constexpr int kCtrPerParity = 3;
+// for frame parity p.  Brick pass: [0] work queue of the first launch, [1]
+// spilled bricks, [2] work queue of the spill pass.  Sweep stream: [0..2] group
+// queues of passes 1-3, [3] voxels listed for the SSA pass.
+static constexpr int kCtrPerParity = 4;
 static uint32_t* group_ctr(DeviceProd* d, int g, int p) { return d->counters.p + (size_t)(2 * g + p) * kCtrPerParity; }
 
 // One pass of a sweep-stream frame of parity `parity` over all word groups
@@ -705,14 +739,28 @@ static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdPa
     // passes 1-3 take their groups from the frame's three work counters (pass 0: round-robin)
     if (pass > 0) S.queue = group_ctr(d, rep < 0 ? 0 : 1 + rep, parity) + (pass - 1);
     S.wcode = d->wcode.n ? d->wcode.p : nullptr;
+    S.ssa_list = d->ssa_list.p;
+    S.ssa_count = group_ctr(d, rep < 0 ? 0 : 1 + rep, parity) + 3;
     switch (pass) {
         case 0: S.out = x_dec; S.rec_out = ra; break;
         case 1: S.in = x_in; S.rec_in = ra; S.out = y_dec; S.rec_out = rb; break;
         case 2: S.in = y_dec; S.rec_in = rb; S.out = z_dec; S.rec_out = ra; break;
         default: S.in = z_dec; S.rec_in = ra; S.fuse = 1u; S.out = x_dec; S.rec_out = rb; break;
     }
+    if (pass == 4) {
+        // the SSA pass over the voxels pass 3 listed: a fixed grid that reads the count on the device
+        S.in = SweepWords{};
+        S.rec_in = nullptr;
+        S.fuse = 1u;
+        S.out = x_dec;
+        S.rec_out = rb;
+        if (!stream_ssa_launch(cfg.K, 2 * d->num_sms, stream_ssa_smem(d->S1, d->R), d->stream, S))
+            throw Error(CS_ERR_INVALID_ARG, "sweep-stream kernel not compiled for this K");
+        CS_LAUNCH_CHECK();
+        return;
+    }
     if (d->stream_occ_cfg != d->cfg_index) {
-        for (int q = 0; q < 4; q++) d->stream_per_sm[q] = stream_blocks_per_sm(cfg.K, cfg.variant, q, smem);
+        for (int q = 0; q < 4; q++) d->stream_per_sm[q] = stream_blocks_per_sm(cfg.K, cfg.variant, q, cfg_smem(d, cfg));
         d->stream_occ_cfg = d->cfg_index;
     }
     const int per_sm = d->stream_per_sm[pass];
@@ -735,7 +783,7 @@ static void launch_stream_pass0(DeviceProd* d) {
 }
 
 static void launch_stream_frame(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity) {
-    for (int pass = 1; pass < 4; pass++) launch_stream_pass(d, cfg, P, rep, parity, pass);
+    for (int pass = 1; pass <= 4; pass++) launch_stream_pass(d, cfg, P, rep, parity, pass);
 }
 
 // One frame over all replicates (batched) or over replicate `rep` alone.

@@ -331,18 +331,22 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                     }
                 } else {
                     const uint32_t rv = P.reservoir ? (uint32_t)P.reservoir[rd.base + v] : 0u;
+                    bool listed = false;
                     if (rv != 0u || zero_order || !vox_empty<K>(r)) {
                         const uint32_t w3 = own_in ? tw.y : d_philox(v, frame, 0u, 0u, k0, k1).w;
                         const bool calm =
                             rv == 0u && !zero_order &&
                             calm_voxel<K>(r, w3, P.T.quiet + (size_t)rd.counts_index * S1 * P.T.QS, P.T.QS,
                                           P.T.one + (size_t)rd.counts_index * S1 * 3, P.T.g23 + 2 * rd.counts_index,
-                                          P.T.tau);
-                        if (!calm)
-                            react_voxel<K>(r, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, P.T, s_delta,
-                                           s_diag, w3);
+                                          P.T.a2 ? P.T.a2 + (size_t)rd.counts_index * S1 * S1 : nullptr, P.T.tau);
+                        if (!calm) {
+                            // pass 4 runs this voxel's SSA: its content waits in its output record
+                            rec_store<K>(SP.rec_out, ri, r, make_uint4(v, w3, rv, G.rep));
+                            SP.ssa_list[atomicAdd(SP.ssa_count, 1u)] = ri;
+                            listed = true;
+                        }
                     }
-                    if (!vox_empty<K>(r)) {
+                    if (!listed && !vox_empty<K>(r)) {
                         st_vox_g<K>(P.dst + (rd.base + v) * K, r);
                         atomicOr(acc + i, bit);
                         if (SP.fuse) {
@@ -396,6 +400,107 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
 }
 
+// Pass 4: the SSA of the voxels pass 3 listed, one thread per voxel, then
+// their store, occupancy bit and next-frame x-decisions (as pass 3 does for
+// the quiet voxels).  Each thread keeps its own species deltas in shared
+// memory (replicates may differ from voxel to voxel).
+template <int K>
+__global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
+    const ProdParams& P = SP.P;
+    extern __shared__ __align__(16) uint32_t sm[];
+    const uint32_t S1 = P.T.S1, NC = P.T.NC;
+    const int tid = threadIdx.x;
+    int32_t* my = reinterpret_cast<int32_t*>(sm) + (size_t)tid * S1;
+    uint32_t* s_diag = sm + (size_t)128 * S1;
+    for (uint32_t s = 0; s < S1; s++) my[s] = 0;
+    for (int i = tid; i < PD_N; i += 128) s_diag[i] = 0u;
+    // the reaction tables in shared memory: each SSA walks them in long dependent chains
+    const uint32_t R = P.T.R;
+    uint8_t* rx = reinterpret_cast<uint8_t*>(sm + ((size_t)128 * S1 + PD_N + 3) / 4 * 4);
+    unsigned long long* rm = reinterpret_cast<unsigned long long*>(rx);
+    float* rate = reinterpret_cast<float*>(rx + 16 * S1);
+    uint8_t* rre = rx + 16 * S1 + 4 * R;
+    uint8_t* csp = rre + 3 * R;
+    int8_t* cdl = reinterpret_cast<int8_t*>(csp + 8 * R);
+    for (uint32_t i = tid; i < 2 * S1; i += 128) rm[i] = P.T.rmask[i];
+    for (uint32_t i = tid; i < R; i += 128) rate[i] = P.T.rx_rate[i];
+    for (uint32_t i = tid; i < 3 * R; i += 128) rre[i] = P.T.rx_reactants[i];
+    for (uint32_t i = tid; i < 8 * R; i += 128) {
+        csp[i] = P.T.rx_ch_sp[i];
+        cdl[i] = P.T.rx_ch_d[i];
+    }
+    ProdTables TS = P.T;
+    TS.rmask = rm;
+    TS.rx_rate = rate;
+    TS.rx_reactants = rre;
+    TS.rx_ch_sp = csp;
+    TS.rx_ch_d = cdl;
+    __syncthreads();
+    const uint32_t frame = P.stepbuf[P.parity];
+    const uint32_t n = *SP.ssa_count;
+    // Few voxels (the usual case): one per warp, on lane 0, spread over every SM, so that no
+    // warp runs several divergent SSAs; many: one per thread.
+    const uint32_t warps = gridDim.x * 4u, gw = blockIdx.x * 4u + ((uint32_t)tid >> 5);
+    const bool per_warp = n <= warps;
+    if (per_warp && (tid & 31) != 0) goto done;
+    for (uint32_t j = per_warp ? gw : blockIdx.x * 128u + (uint32_t)tid; j < n; j += per_warp ? warps : gridDim.x * 128u) {
+        const uint32_t ri = SP.ssa_list[j];
+        Vox<K> r;
+        uint4 t;
+        rec_load<K>(SP.rec_out, ri, r, t);
+        const uint32_t v = t.x, w3 = t.y, rv = t.z;
+        const RepDesc rd = P.reps[t.w];
+        const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
+        react_voxel_inline<K>(r, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, TS, my, s_diag, w3);
+        for (uint32_t s = 0; s < S1; s++)
+            if (my[s]) {
+                atomicAdd(P.counts + (size_t)rd.counts_index * S1 + s, (unsigned long long)(long long)my[s]);
+                my[s] = 0;
+            }
+        if (vox_empty<K>(r)) continue;
+        const uint32_t Y = rd.Y, Z = rd.Z, X = rd.X;
+        const uint32_t x = v / (Y * Z), rem = v - x * (Y * Z), y = rem / Z, z = rem - y * Z;
+        const uint64_t wo = rd.obase + ((uint64_t)x * Y + y) * rd.Wz + (z >> 5);
+        const uint32_t bit = 1u << (z & 31u);
+        st_vox_g<K>(P.dst + (rd.base + v) * K, r);
+        atomicOr(P.odst + wo, bit);
+        if (SP.fuse) {
+            const uint32_t uc = (rd.flags & 1u) ? 1u : SP.wcode ? (uint32_t)SP.wcode[wo] : 0u;
+            const uint8_t* rpad = P.region_pad + rd.rbase;
+            auto code = [&](int xx, int yy, int zz) -> uint32_t {
+                if ((unsigned)xx >= X || (unsigned)yy >= Y || (unsigned)zz >= Z) return 0u;
+                if (uc) return uc;
+                return rpad[((uint64_t)xx * Y + (uint64_t)yy) * rd.Zr + (uint64_t)zz + 2u];
+            };
+            const uint32_t nf = frame + 1u;
+            const U4 b0 = d_philox(v, nf, 0u, 0u, k0, k1);
+            const uint32_t rs = code((int)x, (int)y, (int)z);
+            const uint32_t* tlo = P.T.thr + ((size_t)rs * NC + code((int)x - 1, (int)y, (int)z)) * S1;
+            const uint32_t* thi = P.T.thr + ((size_t)rs * NC + code((int)x + 1, (int)y, (int)z)) * S1;
+            const uint32_t d = decide_moves<K>(r, v, nf, 0u, tlo, thi, k0, k1, b0.x);
+            rec_store<K>(SP.rec_out, ri, r, make_uint4(d, b0.y, b0.z, b0.w));
+            if (d & 0xFFFFu) atomicOr(SP.out.mv_m + wo, bit);
+            if (d >> 16) atomicOr(SP.out.mv_p + wo, bit);
+        }
+    }
+done:
+    __syncthreads();
+    for (int i = tid; i < PD_N; i += 128)
+        if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
+}
+
+// per-thread deltas, diagnostics, then the staged tables (16 S1 + 23 R bytes)
+size_t stream_ssa_smem(uint32_t S1, uint32_t R) {
+    return ((size_t)128 * S1 + PD_N + 3) / 4 * 16 + (size_t)16 * S1 + (size_t)23 * R;
+}
+
+bool stream_ssa_launch(int K, int grid, size_t smem, cudaStream_t s, const StreamParams& SP) {
+    if (K == 16) sweep_ssa_kernel<16><<<grid, 128, smem, s>>>(SP);
+    else if (K == 8) sweep_ssa_kernel<8><<<grid, 128, smem, s>>>(SP);
+    else return false;
+    return true;
+}
+
 // ------------------------------------------------------------------ launchers
 
 namespace {
@@ -403,7 +508,7 @@ struct Variant {
     int NT, MINB, MINB3;  // threads per block, minimum resident blocks per SM of passes 0-2 and of pass 3
 };
 // compiled launch shapes; pass 3 (reactions) needs more registers than the sweeps
-constexpr Variant kVariants[] = {{256, 2, 2}, {256, 4, 4}, {256, 4, 3}};
+constexpr Variant kVariants[] = {{256, 2, 2}, {256, 4, 4}, {256, 4, 3}, {256, 4, 2}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 template <int K, int NT, int MINB, int MINB3>
@@ -422,6 +527,7 @@ void* fn_of(int variant, int pass) {
         case 0: return pass_fn<K, 256, 2, 2>(pass);
         case 1: return pass_fn<K, 256, 4, 4>(pass);
         case 2: return pass_fn<K, 256, 4, 3>(pass);
+        case 3: return pass_fn<K, 256, 4, 2>(pass);
         default: return nullptr;
     }
 }
@@ -451,13 +557,15 @@ int stream_blocks_per_sm(int K, int variant, int pass, size_t smem) {
     return n;
 }
 
-void stream_set_attrs(int K, int variant, size_t smem) {
+void stream_set_attrs(int K, int variant, size_t smem, size_t ssa_smem) {
     for (int pass = 0; pass < 4; pass++) {
         void* fn = kernel_of(K, variant, pass);
         if (!fn) continue;
         CS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         CS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     }
+    void* ssa = K == 16 ? reinterpret_cast<void*>(&sweep_ssa_kernel<16>) : reinterpret_cast<void*>(&sweep_ssa_kernel<8>);
+    CS_CUDA(cudaFuncSetAttribute(ssa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssa_smem));
 }
 
 }  // namespace cellsim

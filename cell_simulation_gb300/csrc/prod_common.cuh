@@ -89,6 +89,8 @@ struct ProdTables {
     uint32_t QS;                      // S1 when two-particle entries are tabulated, else 1
     const float* g23;                 // [n_rep][2]: summed second- and third-order rates (times the
                                       // replicate's multiplier), for the propensity bound of fuller voxels
+    const float* a2;                  // [n_rep][S1][S1] when QS == S1, else null: second-order propensity of
+                                      // one particle pair (p, q), rounded up (the pair terms of that bound)
 };
 
 
@@ -106,19 +108,13 @@ __device__ __forceinline__ Vox<K> vox_zero() {
     return c;
 }
 
-__device__ __forceinline__ uint32_t nz64(uint64_t x) {
-    x |= x >> 4;
-    x |= x >> 2;
-    x |= x >> 1;
-    return (uint32_t)__popcll(x & 0x0101010101010101ull);
-}
-
+// Particles in a voxel.  Contents on this path are always compacted (no empty
+// slot before an occupied one), so the count is the index of the highest
+// non-zero byte plus one.
 template <int K>
 __device__ __forceinline__ uint32_t vox_n(const Vox<K>& c) {
-    uint32_t n = 0;
-#pragma unroll
-    for (int i = 0; i < K / 8; i++) n += nz64(c.w[i]);
-    return n;
+    if (K == 16 && c.w[K / 8 - 1]) return 8u + ((71u - (uint32_t)__clzll((long long)c.w[K / 8 - 1])) >> 3);
+    return c.w[0] ? (71u - (uint32_t)__clzll((long long)c.w[0])) >> 3 : 0u;
 }
 
 template <int K>
@@ -161,13 +157,17 @@ __device__ __forceinline__ uint32_t vox_count(const Vox<K>& c, uint32_t q) {
 // True when the first reaction event of a voxel with content c (no
 // reservoir, no zero-order reaction) certainly falls beyond tau.  One or two
 // particles: the tabulated bound of the exact a0.  More: a0 is at most
-// sum_s a1(q_s) + n(n-1) G2 + n(n-1)(n-2) G3 (first-order propensities of the
-// particles, every second- and third-order rate times the largest possible
-// falling factorial), and a draw m <= exp(-bound tau (1 + 2^-10)) 2^24 (1 - 2^-20)
-// gives dt > tau; the margins cover the binary32 sums and the portable expf.
+// sum_s a1(q_s) + sum_{i<j} a2(q_i, q_j) + n(n-1)(n-2) G3: the first-order
+// propensities of the particles, the second-order propensity of every pair of
+// particles (a2, tabulated per species pair and rounded up: the falling
+// factorials of second-order reactions split exactly into pairs), and every
+// third-order rate times the largest possible falling factorial.  Without the
+// pair table (very many replicates and species) n(n-1) G2 bounds the pairs.
+// A draw m <= exp(-bound tau (1 + 2^-10)) 2^24 (1 - 2^-20) gives dt > tau; the
+// margins cover the binary32 sums and the portable expf.
 template <int K>
 __device__ __forceinline__ bool calm_voxel(const Vox<K>& c, uint32_t w3, const uint32_t* quiet_rep, uint32_t QS,
-                                           const float* one_rep, const float* g23, float tau) {
+                                           const float* one_rep, const float* g23, const float* a2_rep, float tau) {
     const uint32_t n = vox_n<K>(c);
     if (n == 0u) return false;
     const uint32_t m = (w3 >> 8) + 1u;
@@ -177,8 +177,17 @@ __device__ __forceinline__ bool calm_voxel(const Vox<K>& c, uint32_t w3, const u
     }
     float a = 0.0f;
     for (uint32_t s = 0; s < n; s++) a = __fadd_rn(a, one_rep[vox_get<K>(c, s) * 3]);
-    const float nn = (float)(n * (n - 1u)), nnn = (float)(n * (n - 1u) * (n - 2u));
-    a = __fadd_rn(a, __fadd_rn(__fmul_rn(nn, g23[0]), __fmul_rn(nnn, g23[1])));
+    const float nnn = (float)(n * (n - 1u) * (n - 2u));
+    if (a2_rep) {
+        for (uint32_t i = 0; i + 1u < n; i++) {
+            const float* row = a2_rep + vox_get<K>(c, i) * QS;
+            for (uint32_t j = i + 1u; j < n; j++) a = __fadd_rn(a, row[vox_get<K>(c, j)]);
+        }
+        a = __fadd_rn(a, __fmul_rn(nnn, g23[1]));
+    } else {
+        const float nn = (float)(n * (n - 1u));
+        a = __fadd_rn(a, __fadd_rn(__fmul_rn(nn, g23[0]), __fmul_rn(nnn, g23[1])));
+    }
     const float x = __fmul_rn(__fmul_rn(a, tau), 1.0009765625f);  // 1 + 2^-10
     if (!(x >= 0.0f)) return false;
     if (x > 20.0f) return false;
@@ -260,11 +269,18 @@ __device__ __forceinline__ Vox<K> combine(const Vox<K>& own, uint32_t down, cons
     return r;
 }
 
+// Reads of the reaction tables.  Plain (generic) loads, because a kernel may
+// hand react_voxel tables staged in shared memory as well as global ones.
+template <typename T>
+__device__ __forceinline__ T tab_ld(const T* p) {
+    return *p;
+}
+
 // Propensity of reaction r (0-based) for the voxel content c.
 template <int K>
 __device__ __forceinline__ float propensity(const ProdTables& T, uint32_t r, const Vox<K>& c, uint32_t resv, float mult) {
     const uint8_t* re = T.rx_reactants + 3 * r;
-    uint32_t s0 = __ldg(re), s1 = __ldg(re + 1), s2 = __ldg(re + 2);
+    uint32_t s0 = tab_ld(re), s1 = tab_ld(re + 1), s2 = tab_ld(re + 2);
     uint32_t ff = 1;
     uint32_t sp[3] = {s0, s1, s2};
 #pragma unroll
@@ -278,7 +294,7 @@ __device__ __forceinline__ float propensity(const ProdTables& T, uint32_t r, con
         if (cnt <= m) return 0.0f;
         ff *= cnt - m;
     }
-    return __fmul_rn(__fmul_rn(__ldg(T.rx_rate + r), mult), (float)ff);
+    return __fmul_rn(__fmul_rn(tab_ld(T.rx_rate + r), mult), (float)ff);
 }
 
 // Reactions whose propensity can be non-zero in the voxel: those with a
@@ -292,12 +308,12 @@ __device__ __forceinline__ void candidates(const ProdTables& T, const Vox<K>& c,
     m1 = T.zmask[1];
     for (uint32_t i = 0; i < n; i++) {
         uint32_t q = vox_get<K>(c, i);
-        m0 |= __ldg(T.rmask + 2 * q);
-        m1 |= __ldg(T.rmask + 2 * q + 1);
+        m0 |= tab_ld(T.rmask + 2 * q);
+        m1 |= tab_ld(T.rmask + 2 * q + 1);
     }
     if (resv) {
-        m0 |= __ldg(T.rmask + 2 * resv);
-        m1 |= __ldg(T.rmask + 2 * resv + 1);
+        m0 |= tab_ld(T.rmask + 2 * resv);
+        m1 |= tab_ld(T.rmask + 2 * resv + 1);
     }
 }
 
@@ -318,11 +334,13 @@ __device__ __forceinline__ int next_bit(unsigned long long& m0, unsigned long lo
 // SSA within tau for one voxel.  Returns true when any reaction fired (the
 // content is then rewritten species-major).  s_delta[S1] and s_diag[PD_N]
 // are block-shared accumulators.
-// w3 is B(v, 0)[3], evaluated by the caller.
+// w3 is B(v, 0)[3], evaluated by the caller.  react_voxel_inline is the body,
+// for kernels that run the SSA in a loop of their own; react_voxel is the
+// out-of-line call for kernels whose register budget must not grow for it.
 template <int K>
-__device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0, uint32_t k1,
-                                         float mult, uint32_t rep, const ProdTables& T, int32_t* s_delta,
-                                         uint32_t* s_diag, uint32_t w3) {
+__device__ __forceinline__ bool react_voxel_inline(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0,
+                                                   uint32_t k1, float mult, uint32_t rep, const ProdTables& T,
+                                                   int32_t* s_delta, uint32_t* s_diag, uint32_t w3) {
     if (T.R == 0) return false;
     atomicAdd(s_diag + PD_SSA_VOXELS, 1u);
     uint32_t n = vox_n<K>(c);
@@ -337,9 +355,9 @@ __device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, u
         if (resv == 0u && n <= 1u) {
             // one particle or none: the candidate sum is tabulated (same binary32 sum)
             const float* o = T.one + ((size_t)rep * T.S1 + (n ? vox_get<K>(c, 0) : 0u)) * 3;
-            a0 = __ldg(o);
-            amax = __ldg(o + 1);
-            amin = __ldg(o + 2);
+            a0 = tab_ld(o);
+            amax = tab_ld(o + 1);
+            amin = tab_ld(o + 2);
         } else {
             unsigned long long m0 = c0, m1 = c1;
             for (int r = next_bit(m0, m1); r >= 0; r = next_bit(m0, m1)) {
@@ -404,10 +422,10 @@ __device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, u
         int total = (int)n;
         bool ok = true;
         for (int j = 0; j < 8; j++) {
-            uint32_t s = __ldg(csp + j);
+            uint32_t s = tab_ld(csp + j);
             if (s == 0) break;
             if (s == resv) continue;
-            int d = __ldg(cd + j);
+            int d = tab_ld(cd + j);
             int have = (int)vox_count<K>(c, s);
             if (have + d < 0) ok = false;
             total += d;
@@ -419,10 +437,10 @@ __device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, u
         // removals first, so that the content never exceeds K slots in between
         for (int pass = 0; pass < 2; pass++) {
             for (int j = 0; j < 8; j++) {
-                uint32_t s = __ldg(csp + j);
+                uint32_t s = tab_ld(csp + j);
                 if (s == 0) break;
                 if (s == resv) continue;
-                int d = __ldg(cd + j);
+                int d = tab_ld(cd + j);
                 if (pass == 0) {
                     for (; d < 0; d++) {  // remove one occurrence: move the last particle into its slot
                         uint32_t idx = 0;
@@ -434,7 +452,7 @@ __device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, u
                     }
                 } else {
                     for (; d > 0; d--) vox_set<K>(c, n++, s);
-                    atomicAdd(s_delta + s, __ldg(cd + j));
+                    atomicAdd(s_delta + s, tab_ld(cd + j));
                 }
             }
         }
@@ -460,6 +478,13 @@ __device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, u
         c = out;
     }
     return fired;
+}
+
+template <int K>
+__device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0, uint32_t k1,
+                                         float mult, uint32_t rep, const ProdTables& T, int32_t* s_delta,
+                                         uint32_t* s_diag, uint32_t w3) {
+    return react_voxel_inline<K>(c, resv, v, frame, k0, k1, mult, rep, T, s_delta, s_diag, w3);
 }
 
 }  // namespace cellsim

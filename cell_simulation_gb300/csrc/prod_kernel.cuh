@@ -361,7 +361,9 @@ __global__ void __launch_bounds__(NT, MINB) prod_step_kernel(ProdParams P) {
                                 rv == 0u && !always_react &&
                                 calm_voxel<K>(r, w3, P.T.quiet + (size_t)rd.counts_index * P.T.S1 * P.T.QS, P.T.QS,
                                               P.T.one + (size_t)rd.counts_index * P.T.S1 * 3,
-                                              P.T.g23 + 2 * rd.counts_index, P.T.tau);
+                                              P.T.g23 + 2 * rd.counts_index,
+                                              P.T.a2 ? P.T.a2 + (size_t)rd.counts_index * P.T.S1 * P.T.S1 : nullptr,
+                                              P.T.tau);
                             if (!quiet)
                                 react_voxel<K>(r, rv, v, frame, k0, k1, mult, rd.counts_index, P.T, s_delta, s_diag, w3);
                         }

@@ -7,6 +7,14 @@
 //   pass 2  Y sweep, z-move decisions
 //   pass 3  Z sweep, reactions, store into the destination lattice and its
 //           occupancy bitmap; voxels that became empty get zeros
+//   pass 4  the SSA of the few voxels whose first reaction event may fall
+//           within the frame (pass 3 lists them instead of running it)
+//
+// Pass 3 decides for every occupied voxel whether an event can fire at all
+// (the exact quiet-voxel bound); the rest are parked in their output record
+// and listed, and pass 4 runs their SSA one thread per voxel, stores them and
+// makes their next-frame decisions.  Keeping the SSA out of pass 3 keeps its
+// registers and its warps free of rare, long single-lane calls.
 //
 // Pass 0 of frame f + 1 needs only the final contents of frame f, so pass 3
 // also makes the next frame's x-decisions while the contents are in
@@ -74,6 +82,8 @@ struct StreamParams {
     SweepWords out;  // produced by this pass (pass 3: the next frame's x-decisions when fused)
     const uint4* rec_in;
     uint4* rec_out;
+    uint32_t* ssa_list;   // output record indices of the voxels listed for pass 4
+    uint32_t* ssa_count;  // their number (zero at the start of the frame)
 };
 
 // Compiled launch shapes ("variants": threads per block and minimum resident
@@ -87,7 +97,11 @@ bool stream_launch(int K, int variant, int pass, int grid, size_t smem, cudaStre
 int stream_blocks_per_sm(int K, int variant, int pass, size_t smem);
 // Dynamic shared memory of one block of NT threads.
 size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words);
-// Sets the kernel attributes (shared-memory size and carveout) of every pass.
-void stream_set_attrs(int K, int variant, size_t smem);
+// Sets the kernel attributes (shared-memory size and carveout) of every pass;
+// ssa_smem is the SSA pass's.
+void stream_set_attrs(int K, int variant, size_t smem, size_t ssa_smem);
+// The SSA pass (pass 4): `grid` blocks over the listed voxels.
+bool stream_ssa_launch(int K, int grid, size_t smem, cudaStream_t s, const StreamParams& SP);
+size_t stream_ssa_smem(uint32_t S1, uint32_t R);
 
 }  // namespace cellsim
