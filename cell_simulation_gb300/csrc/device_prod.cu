@@ -416,16 +416,17 @@ static void build_one_table(DeviceProd* d) {
     d->T.quiet = d->quiet.p;
 }
 
-// Default step before any autotuning: the 16-plane, 256-thread brick pass of the
-// model's K (the fastest variant on the sparse lattices measured), else its first
-// brick pass.
+// Default step before any autotuning: the sweep stream of the model's K with
+// four-block sweep passes and a three-block pass 3 (the fastest variant on the
+// sparse lattices and the replicate ensemble measured), else its first brick
+// pass.
 static int pick_default_cfg(uint32_t K) {
     const auto& c = all_cfgs();
     int first = -1;
     for (size_t i = 0; i < c.size(); i++) {
-        if (c[i].K != (int)K || c[i].kind != KIND_BRICK) continue;
-        if (c[i].BX == 16 && c[i].NT == 256 && c[i].spill >= 0) return (int)i;
-        if (first < 0) first = (int)i;
+        if (c[i].K != (int)K) continue;
+        if (c[i].kind == KIND_STREAM && c[i].variant == 2) return (int)i;
+        if (first < 0 && c[i].kind == KIND_BRICK) first = (int)i;
     }
     return first;
 }
