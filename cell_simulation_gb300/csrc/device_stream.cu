@@ -188,7 +188,13 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         f[F_Y * 32 + lane] = (uint32_t)y;
         f[F_KK * 32 + lane] = (uint32_t)kk;
         f[F_VROW * 32 + lane] = ((uint32_t)x * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z;
-        f[F_CODE * 32 + lane] = (rd.flags & 1u) ? 1u : (SP.wcode && valid) ? (uint32_t)SP.wcode[wo] : 0u;
+        {
+            // the word's uniform region code; bit 8: its whole window lies inside the lattice, so
+            // every neighbour of its voxels has that code too
+            const uint32_t uc = (rd.flags & 1u) ? 1u : (SP.wcode && valid) ? (uint32_t)SP.wcode[wo] : 0u;
+            const bool inner = x > 0 && x + 1 < X && y > 0 && y + 1 < Y && kk > 0 && kk + 1 < (int)Wz;
+            f[F_CODE * 32 + lane] = uc | (uc && inner ? 0x100u : 0u);
+        }
         // List the work bits in three classes, so that the lanes of a warp mostly run the same
         // path: voxels with a record of the previous pass whose content does not change along
         // the axis, those whose content changes, and those without a record (arrivals), whose
@@ -232,8 +238,9 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         const uint8_t* rpad = P.region_pad + rd.rbase;
         const uint64_t Zr = rd.Zr;
         // region code (id + 1) of voxel (xx, yy, zz) of the window of a word with uniform code uc
-        // (0: look it up); 0 outside the lattice
+        // (0: look it up; bit 8: the whole window is inside the lattice); 0 outside the lattice
         auto code = [&](uint32_t uc, int xx, int yy, int zz) -> uint32_t {
+            if (uc & 0x100u) return uc & 0xFFu;
             if ((unsigned)xx >= (unsigned)X || (unsigned)yy >= (unsigned)Y || (unsigned)zz >= (unsigned)Z) return 0u;
             if (uc) return uc;
             return __ldg(rpad + ((uint64_t)xx * (uint64_t)Y + (uint64_t)yy) * Zr + (uint64_t)zz + 2u);
@@ -400,10 +407,11 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
 }
 
-// Pass 4: the SSA of the voxels pass 3 listed, one thread per voxel, then
-// their store, occupancy bit and next-frame x-decisions (as pass 3 does for
-// the quiet voxels).  Each thread keeps its own species deltas in shared
-// memory (replicates may differ from voxel to voxel).
+// Pass 4: the SSA of the voxels pass 3 listed, one warp per voxel (the lanes
+// evaluate its candidate reactions together, react_voxel_warp), then its store,
+// occupancy bit and next-frame x-decisions by lane 0 (as pass 3 does for the
+// quiet voxels).  Species deltas are flushed per voxel (replicates may differ
+// from voxel to voxel); the reaction tables are staged in shared memory.
 template <int K>
 __global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
     const ProdParams& P = SP.P;
@@ -438,12 +446,10 @@ __global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
     __syncthreads();
     const uint32_t frame = P.stepbuf[P.parity];
     const uint32_t n = *SP.ssa_count;
-    // Few voxels (the usual case): one per warp, on lane 0, spread over every SM, so that no
-    // warp runs several divergent SSAs; many: one per thread.
-    const uint32_t warps = gridDim.x * 4u, gw = blockIdx.x * 4u + ((uint32_t)tid >> 5);
-    const bool per_warp = n <= warps;
-    if (per_warp && (tid & 31) != 0) goto done;
-    for (uint32_t j = per_warp ? gw : blockIdx.x * 128u + (uint32_t)tid; j < n; j += per_warp ? warps : gridDim.x * 128u) {
+    // One warp per listed voxel: the lanes share its SSA (react_voxel_warp), lane 0 stores it.
+    const uint32_t warps = gridDim.x * 4u, gw = blockIdx.x * 4u + ((uint32_t)tid >> 5), lane = (uint32_t)tid & 31u;
+    int32_t* my0 = reinterpret_cast<int32_t*>(sm) + (size_t)(tid - (int)lane) * S1;  // lane 0's deltas
+    for (uint32_t j = gw; j < n; j += warps) {
         const uint32_t ri = SP.ssa_list[j];
         Vox<K> r;
         uint4 t;
@@ -451,39 +457,43 @@ __global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
         const uint32_t v = t.x, w3 = t.y, rv = t.z;
         const RepDesc rd = P.reps[t.w];
         const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
-        react_voxel_inline<K>(r, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, TS, my, s_diag, w3);
-        for (uint32_t s = 0; s < S1; s++)
-            if (my[s]) {
-                atomicAdd(P.counts + (size_t)rd.counts_index * S1 + s, (unsigned long long)(long long)my[s]);
-                my[s] = 0;
+        react_voxel_warp<K>(r, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, TS, my0, s_diag, w3);
+        __syncwarp();
+        if (lane == 0u) {
+            for (uint32_t s = 0; s < S1; s++)
+                if (my0[s]) {
+                    atomicAdd(P.counts + (size_t)rd.counts_index * S1 + s, (unsigned long long)(long long)my0[s]);
+                    my0[s] = 0;
+                }
+            if (!vox_empty<K>(r)) {
+                const uint32_t Y = rd.Y, Z = rd.Z, X = rd.X;
+                const uint32_t x = v / (Y * Z), rem = v - x * (Y * Z), y = rem / Z, z = rem - y * Z;
+                const uint64_t wo = rd.obase + ((uint64_t)x * Y + y) * rd.Wz + (z >> 5);
+                const uint32_t bit = 1u << (z & 31u);
+                st_vox_g<K>(P.dst + (rd.base + v) * K, r);
+                atomicOr(P.odst + wo, bit);
+                if (SP.fuse) {
+                    const uint32_t uc = (rd.flags & 1u) ? 1u : SP.wcode ? (uint32_t)SP.wcode[wo] : 0u;
+                    const uint8_t* rpad = P.region_pad + rd.rbase;
+                    auto code = [&](int xx, int yy, int zz) -> uint32_t {
+                        if ((unsigned)xx >= X || (unsigned)yy >= Y || (unsigned)zz >= Z) return 0u;
+                        if (uc) return uc;
+                        return rpad[((uint64_t)xx * Y + (uint64_t)yy) * rd.Zr + (uint64_t)zz + 2u];
+                    };
+                    const uint32_t nf = frame + 1u;
+                    const U4 b0 = d_philox(v, nf, 0u, 0u, k0, k1);
+                    const uint32_t rs = code((int)x, (int)y, (int)z);
+                    const uint32_t* tlo = P.T.thr + ((size_t)rs * NC + code((int)x - 1, (int)y, (int)z)) * S1;
+                    const uint32_t* thi = P.T.thr + ((size_t)rs * NC + code((int)x + 1, (int)y, (int)z)) * S1;
+                    const uint32_t d = decide_moves<K>(r, v, nf, 0u, tlo, thi, k0, k1, b0.x);
+                    rec_store<K>(SP.rec_out, ri, r, make_uint4(d, b0.y, b0.z, b0.w));
+                    if (d & 0xFFFFu) atomicOr(SP.out.mv_m + wo, bit);
+                    if (d >> 16) atomicOr(SP.out.mv_p + wo, bit);
+                }
             }
-        if (vox_empty<K>(r)) continue;
-        const uint32_t Y = rd.Y, Z = rd.Z, X = rd.X;
-        const uint32_t x = v / (Y * Z), rem = v - x * (Y * Z), y = rem / Z, z = rem - y * Z;
-        const uint64_t wo = rd.obase + ((uint64_t)x * Y + y) * rd.Wz + (z >> 5);
-        const uint32_t bit = 1u << (z & 31u);
-        st_vox_g<K>(P.dst + (rd.base + v) * K, r);
-        atomicOr(P.odst + wo, bit);
-        if (SP.fuse) {
-            const uint32_t uc = (rd.flags & 1u) ? 1u : SP.wcode ? (uint32_t)SP.wcode[wo] : 0u;
-            const uint8_t* rpad = P.region_pad + rd.rbase;
-            auto code = [&](int xx, int yy, int zz) -> uint32_t {
-                if ((unsigned)xx >= X || (unsigned)yy >= Y || (unsigned)zz >= Z) return 0u;
-                if (uc) return uc;
-                return rpad[((uint64_t)xx * Y + (uint64_t)yy) * rd.Zr + (uint64_t)zz + 2u];
-            };
-            const uint32_t nf = frame + 1u;
-            const U4 b0 = d_philox(v, nf, 0u, 0u, k0, k1);
-            const uint32_t rs = code((int)x, (int)y, (int)z);
-            const uint32_t* tlo = P.T.thr + ((size_t)rs * NC + code((int)x - 1, (int)y, (int)z)) * S1;
-            const uint32_t* thi = P.T.thr + ((size_t)rs * NC + code((int)x + 1, (int)y, (int)z)) * S1;
-            const uint32_t d = decide_moves<K>(r, v, nf, 0u, tlo, thi, k0, k1, b0.x);
-            rec_store<K>(SP.rec_out, ri, r, make_uint4(d, b0.y, b0.z, b0.w));
-            if (d & 0xFFFFu) atomicOr(SP.out.mv_m + wo, bit);
-            if (d >> 16) atomicOr(SP.out.mv_p + wo, bit);
         }
+        __syncwarp();
     }
-done:
     __syncthreads();
     for (int i = tid; i < PD_N; i += 128)
         if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);

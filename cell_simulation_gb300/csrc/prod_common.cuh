@@ -480,6 +480,194 @@ __device__ __forceinline__ bool react_voxel_inline(Vox<K>& c, uint32_t resv, uin
     return fired;
 }
 
+// Element q (0..3) of a four-element register array, by selects (no local memory).
+template <typename T>
+__device__ __forceinline__ T pick4(const T (&a)[4], uint32_t q) {
+    return q == 0u ? a[0] : q == 1u ? a[1] : q == 2u ? a[2] : a[3];
+}
+
+// Index of set bit k (0-based) of the 128-bit mask (m0, m1); k < popcount.
+__device__ __forceinline__ int nth_bit(unsigned long long m0, unsigned long long m1, uint32_t k) {
+    uint32_t off = 0u;
+    uint32_t p0 = (uint32_t)__popcll(m0);
+    unsigned long long m = m0;
+    if (k >= p0) {
+        k -= p0;
+        m = m1;
+        off = 64u;
+    }
+    uint32_t w = (uint32_t)m, pl = (uint32_t)__popc(w);
+    if (k >= pl) {
+        k -= pl;
+        w = (uint32_t)(m >> 32);
+        off += 32u;
+    }
+#pragma unroll
+    for (uint32_t sh = 16u; sh; sh >>= 1) {
+        const uint32_t c = (uint32_t)__popc(w & ((1u << sh) - 1u));
+        if (k >= c) {
+            k -= c;
+            w >>= sh;
+            off += sh;
+        }
+    }
+    return (int)off;
+}
+
+// The SSA of react_voxel_inline run by a whole warp: every lane calls it with
+// the same voxel and gets the same result.  Lanes evaluate the candidate
+// reactions' propensities in parallel (lane l takes candidates l, l + 32, ...
+// in index order); every sum and running sum is then formed in candidate
+// order with one value shuffled in at a time, so every binary32 and binary64
+// result, and so the lattice, equals react_voxel_inline's.  Counters and
+// species deltas are updated by lane 0.
+template <int K>
+__device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0,
+                                                 uint32_t k1, float mult, uint32_t rep, const ProdTables& T,
+                                                 int32_t* s_delta, uint32_t* s_diag, uint32_t w3) {
+    const uint32_t lane = threadIdx.x & 31u;
+    if (T.R == 0) return false;
+    if (lane == 0u) atomicAdd(s_diag + PD_SSA_VOXELS, 1u);
+    uint32_t n = vox_n<K>(c);
+    double td = 0.0;
+    float tf = 0.0f;
+    bool fired = false;
+    uint32_t ev = 0;
+    for (; ev < T.max_events; ev++) {
+        unsigned long long c0, c1;
+        candidates<K>(T, c, n, resv, c0, c1);
+        const uint32_t nc = (uint32_t)(__popcll(c0) + __popcll(c1));
+        // this lane's candidates (at most 128 reactions: four rounds) and their propensities
+        float ach[4];
+        int rch[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t k = (uint32_t)q * 32u + lane;
+            rch[q] = k < nc ? nth_bit(c0, c1, k) : -1;
+            ach[q] = rch[q] >= 0 ? propensity<K>(T, (uint32_t)rch[q], c, resv, mult) : 0.0f;
+        }
+        float a0 = 0.0f, amax = 0.0f, amin = __int_as_float(0x7f800000);
+        if (resv == 0u && n <= 1u) {
+            const float* o = T.one + ((size_t)rep * T.S1 + (n ? vox_get<K>(c, 0) : 0u)) * 3;
+            a0 = tab_ld(o);
+            amax = tab_ld(o + 1);
+            amin = tab_ld(o + 2);
+        } else {
+            for (uint32_t k = 0; k < nc; k++) {
+                const float a = __shfl_sync(0xffffffffu, pick4(ach, k >> 5), k & 31u);
+                a0 = __fadd_rn(a0, a);
+                if (a > 0.0f) { amax = fmaxf(amax, a); amin = fminf(amin, a); }
+            }
+        }
+        if (!(a0 > 0.0f)) break;
+        U4 ph{0u, 0u, 0u, 0u};
+        uint32_t w1 = w3;
+        if (ev != 0u) {
+            ph = d_philox(v, frame, 0x80000000u | ev, 0u, k0, k1);
+            w1 = ph.x;
+        }
+        float u1 = __fmul_rn((float)((w1 >> 8) + 1u), 0x1p-24f);
+        float dt = __fdiv_rn(-d_logf(u1), a0);
+        if (T.precision == 1) {
+            tf = __fadd_rn(tf, dt);
+            if (tf > T.tau) break;
+        } else {
+            td = __dadd_rn(td, (double)dt);
+            if (td > T.tau_d) break;
+        }
+        if (ev == 0u) ph = d_philox(v, frame, 0x80000000u, 0u, k0, k1);
+        const uint32_t w2 = ph.y;
+        float u2 = __fmul_rn((float)(w2 >> 8), 0x1p-24f);
+        bool use64 = (T.precision == 2) || (T.precision == 0 && amax > __fmul_rn(1e6f, amin));
+        int sel = -1;
+        int last_pos = -1;
+        if (!use64) {
+            float target = __fmul_rn(u2, a0), run = 0.0f;
+            for (uint32_t k = 0; k < nc; k++) {
+                const float a = __shfl_sync(0xffffffffu, pick4(ach, k >> 5), k & 31u);
+                const int r = __shfl_sync(0xffffffffu, pick4(rch, k >> 5), k & 31u);
+                if (a > 0.0f) last_pos = r;
+                run = __fadd_rn(run, a);
+                if (target < run) { sel = r; break; }
+            }
+        } else {
+            if (lane == 0u) atomicAdd(s_diag + PD_FP64_SEL, 1u);
+            double a0d = 0.0;
+            for (uint32_t k = 0; k < nc; k++)
+                a0d = __dadd_rn(a0d, (double)__shfl_sync(0xffffffffu, pick4(ach, k >> 5), k & 31u));
+            double target = __dmul_rn((double)u2, a0d), run = 0.0;
+            for (uint32_t k = 0; k < nc; k++) {
+                const float a = __shfl_sync(0xffffffffu, pick4(ach, k >> 5), k & 31u);
+                const int r = __shfl_sync(0xffffffffu, pick4(rch, k >> 5), k & 31u);
+                if (a > 0.0f) last_pos = r;
+                run = __dadd_rn(run, (double)a);
+                if (target < run) { sel = r; break; }
+            }
+        }
+        if (sel < 0) sel = last_pos;
+        if (sel < 0) break;
+        // apply the change list, skipping the voxel's reservoir species (every lane, same result)
+        const uint8_t* csp = T.rx_ch_sp + 8 * sel;
+        const int8_t* cd = T.rx_ch_d + 8 * sel;
+        int total = (int)n;
+        bool ok = true;
+        for (int j = 0; j < 8; j++) {
+            uint32_t s = tab_ld(csp + j);
+            if (s == 0) break;
+            if (s == resv) continue;
+            int d = tab_ld(cd + j);
+            int have = (int)vox_count<K>(c, s);
+            if (have + d < 0) ok = false;
+            total += d;
+        }
+        if (!ok || total > (int)K) {
+            if (lane == 0u) atomicAdd(s_diag + PD_REJECT_CAP, 1u);
+            continue;
+        }
+        for (int pass = 0; pass < 2; pass++) {
+            for (int j = 0; j < 8; j++) {
+                uint32_t s = tab_ld(csp + j);
+                if (s == 0) break;
+                if (s == resv) continue;
+                int d = tab_ld(cd + j);
+                if (pass == 0) {
+                    for (; d < 0; d++) {
+                        uint32_t idx = 0;
+                        for (uint32_t i = 0; i < n; i++)
+                            if (vox_get<K>(c, i) == s) idx = i;
+                        vox_set<K>(c, idx, vox_get<K>(c, n - 1));
+                        vox_set<K>(c, n - 1, 0u);
+                        n--;
+                    }
+                } else {
+                    for (; d > 0; d--) vox_set<K>(c, n++, s);
+                    if (lane == 0u) atomicAdd(s_delta + s, tab_ld(cd + j));
+                }
+            }
+        }
+        if (lane == 0u) atomicAdd(s_diag + PD_EVENTS, 1u);
+        fired = true;
+    }
+    if (ev == T.max_events && lane == 0u) atomicAdd(s_diag + PD_EVENT_CAP, 1u);
+    if (fired) {
+        Vox<K> out = vox_zero<K>();
+        uint32_t j = 0, prev = 0;
+        for (;;) {
+            uint32_t best = 256;
+            for (uint32_t i = 0; i < n; i++) {
+                uint32_t b = vox_get<K>(c, i);
+                if (b > prev && b < best) best = b;
+            }
+            if (best == 256) break;
+            uint32_t cnt = vox_count<K>(c, best);
+            for (uint32_t k = 0; k < cnt; k++) vox_or<K>(out, j++, best);
+            prev = best;
+        }
+        c = out;
+    }
+    return fired;
+}
+
 template <int K>
 __device__ __noinline__ bool react_voxel(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0, uint32_t k1,
                                          float mult, uint32_t rep, const ProdTables& T, int32_t* s_delta,

@@ -268,6 +268,27 @@ def test_switching_step_kinds_mid_run_matches_oracle(orc):
     assert np.array_equal(sim.counts(), want_c)
 
 
+def test_switching_to_and_from_the_sweep_stream_matches_oracle(orc):
+    """Brick, sweep-stream and tile frames in one run: frames of another kind (and an upload)
+    make the x-decisions the last stream frame left for the next frame stale, so the stream
+    recomputes them.  Odd frame counts change the parity the kinds hand over."""
+    mk = lambda: multi_region_model(res=(13, 17, 40), K=16, counts=(90, 70, 50, 40))
+    want_s, want_c, _ = oracle_prod(orc, mk(), 21, seed=777)
+    sim = mk()
+    sim.prepare_for_gpu(RNG_PHILOX, 0)
+    kinds = tiling_kinds()
+    tile = next(i for i, (t, k) in enumerate(zip(tiling_variants(), kinds)) if t[0] == 16 and k[0] == 0)
+    brick = next(i for i, (t, k) in enumerate(zip(tiling_variants(), kinds)) if t[0] == 16 and k == (1, 8))
+    stream = stream_tilings(16)[-1]
+    for ti, n in ((stream, 3), (brick, 4), (stream, 5), (tile, 3), (stream, 2)):
+        sim.set_tiling(ti)
+        sim.step_philox(n, 777)
+    sim.set_lattice(sim.get_lattice()[0])
+    sim.step_philox(4, 777)
+    assert np.array_equal(sim.get_lattice()[0].astype(np.uint8), want_s)
+    assert np.array_equal(sim.counts(), want_c)
+
+
 def test_autotune_keeps_state_and_results(orc):
     """The autotuner times every variant on a copy of the live state: the
     simulation does not advance and the following frames equal the oracle."""
