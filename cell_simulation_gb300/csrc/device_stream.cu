@@ -57,6 +57,15 @@ __device__ __forceinline__ void rec_store(uint4* rec, uint32_t i, const Vox<K>& 
 
 __device__ __forceinline__ uint32_t below(uint32_t m, uint32_t bit) { return (uint32_t)__popc(m & (bit - 1u)); }
 
+// Programmatic dependent launch: the passes are launched so that a launch's
+// blocks may start while the previous launch drains.  Each kernel lets the
+// next one launch at once, stages its constant tables, and waits for the
+// previous launch to complete (and its memory to be visible) before it reads
+// or writes anything the previous launches produced or read.  Without a
+// programmatic dependency the wait returns at once.
+__device__ __forceinline__ void allow_next_launch() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+__device__ __forceinline__ void wait_previous_launch() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
 // PASS 0: x-decisions; 1: X sweep + y-decisions; 2: Y sweep + z-decisions;
 // 3: Z sweep + reactions + store.
 template <int K, int PASS, int NT, int MINB>
@@ -72,11 +81,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     int32_t* s_delta = reinterpret_cast<int32_t*>(acc + 96 + LIST / 2);  // [S1] this warp's species deltas
     uint32_t* s_diag = sm + (size_t)NW * stream_warp_words(S1);        // [PD_N]
     uint32_t* s_thr = s_diag + PD_N;
-    const uint32_t frame = P.stepbuf[P.parity];
-    if (blockIdx.x == 0 && tid == 0) {
-        for (uint32_t i = 0; i < P.n_reset; i++) P.reset[i] = 0u;
-        if (PASS == 3 && P.advance) P.stepbuf[P.parity ^ 1u] = frame + 1u;
-    }
+    allow_next_launch();
     const uint32_t* thr = P.T.thr;
     if (P.thr_smem) {
         const uint32_t nt = NC * NC * S1;
@@ -85,6 +90,12 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     }
     for (uint32_t s = lane; s < S1; s += 32) s_delta[s] = 0;
     for (int i = tid; i < PD_N; i += NT) s_diag[i] = 0u;
+    wait_previous_launch();
+    const uint32_t frame = P.stepbuf[P.parity];
+    if (blockIdx.x == 0 && tid == 0) {
+        for (uint32_t i = 0; i < P.n_reset; i++) P.reset[i] = 0u;
+        if (PASS == 3 && P.advance) P.stepbuf[P.parity ^ 1u] = frame + 1u;
+    }
     __syncthreads();
     const bool zero_order = P.T.n_zero_order != 0u;
     const bool all_react = zero_order || P.reservoir != nullptr;
@@ -418,6 +429,7 @@ __global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
     extern __shared__ __align__(16) uint32_t sm[];
     const uint32_t S1 = P.T.S1, NC = P.T.NC;
     const int tid = threadIdx.x;
+    allow_next_launch();
     int32_t* my = reinterpret_cast<int32_t*>(sm) + (size_t)tid * S1;
     uint32_t* s_diag = sm + (size_t)128 * S1;
     for (uint32_t s = 0; s < S1; s++) my[s] = 0;
@@ -444,6 +456,7 @@ __global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
     TS.rx_ch_sp = csp;
     TS.rx_ch_d = cdl;
     __syncthreads();
+    wait_previous_launch();
     const uint32_t frame = P.stepbuf[P.parity];
     const uint32_t n = *SP.ssa_count;
     // One warp per listed voxel: the lanes share its SSA (react_voxel_warp), lane 0 stores it.
@@ -504,10 +517,14 @@ size_t stream_ssa_smem(uint32_t S1, uint32_t R) {
     return ((size_t)128 * S1 + PD_N + 3) / 4 * 16 + (size_t)16 * S1 + (size_t)23 * R;
 }
 
+static void launch_pdl(void* fn, int grid, int threads, size_t smem, cudaStream_t s, const StreamParams& SP);
+
 bool stream_ssa_launch(int K, int grid, size_t smem, cudaStream_t s, const StreamParams& SP) {
-    if (K == 16) sweep_ssa_kernel<16><<<grid, 128, smem, s>>>(SP);
-    else if (K == 8) sweep_ssa_kernel<8><<<grid, 128, smem, s>>>(SP);
-    else return false;
+    void* fn = K == 16 ? reinterpret_cast<void*>(&sweep_ssa_kernel<16>)
+             : K == 8  ? reinterpret_cast<void*>(&sweep_ssa_kernel<8>)
+                       : nullptr;
+    if (!fn) return false;
+    launch_pdl(fn, grid, 128, smem, s, SP);
     return true;
 }
 
@@ -551,11 +568,26 @@ void* kernel_of(int K, int variant, int pass) {
 int stream_variant_count() { return kNumVariants; }
 int stream_variant_threads(int variant) { return variant >= 0 && variant < kNumVariants ? kVariants[variant].NT : 0; }
 
+// Launch with programmatic stream serialization (see wait_previous_launch).
+static void launch_pdl(void* fn, int grid, int threads, size_t smem, cudaStream_t s, const StreamParams& SP) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void* args[] = {const_cast<StreamParams*>(&SP)};
+    CS_CUDA(cudaLaunchKernelExC(&cfg, fn, args));
+}
+
 bool stream_launch(int K, int variant, int pass, int grid, size_t smem, cudaStream_t s, const StreamParams& SP) {
     void* fn = kernel_of(K, variant, pass);
     if (!fn) return false;
-    void* args[] = {const_cast<StreamParams*>(&SP)};
-    CS_CUDA(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3((unsigned)kVariants[variant].NT), args, smem, s));
+    launch_pdl(fn, grid, kVariants[variant].NT, smem, s, SP);
     return true;
 }
 
