@@ -271,8 +271,11 @@ cs_status cs_step_philox_timed(cs_sim* sim, uint32_t n_steps, uint64_t seed, flo
  * length of a work item (0 = automatic; tile pipeline only); used by the
  * autotuner.  cs_tiling_kind: kind 0 = tile pipeline over (TY x TZ tile,
  * x-segment) items; kind 1 = sparse brick pass over brick_planes x TY x TZ
- * bricks, crowded bricks finished by the tile pipeline.  No reference
- * counterpart (the reference has one fixed dispatch shape per shader). */
+ * bricks, crowded bricks finished by a full-capacity second brick pass;
+ * kind 2 = sweep stream (the default): barrier-free passes over groups of 32
+ * occupancy-bitmap words (TY = 0, TZ = 32, brick_planes = 0).  Every variant
+ * computes the same lattice.  No reference counterpart (the reference has one
+ * fixed dispatch shape per shader). */
 cs_status cs_tiling_count(int32_t* n);
 cs_status cs_tiling_describe(int32_t index, int32_t* K, int32_t* TY, int32_t* TZ, int32_t* threads);
 cs_status cs_tiling_kind(int32_t index, int32_t* kind, int32_t* brick_planes);
