@@ -1,0 +1,59 @@
+"""bench.py's multi-rank path on the CPU.  Under torchrun every rank times its
+own replica and rank 0 reports the maximum over ranks after a barrier; two
+gloo ranks here check that the barrier completes and that both ranks agree
+on that maximum.  The reference arm does its work on rank 0 only: another
+rank exits at once without output."""
+import os
+import socket
+import subprocess
+import sys
+from pathlib import Path
+
+import torch.multiprocessing as mp
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _free_port() -> int:
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank: int, world: int, port: int, out: str) -> None:
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    d = bench.Dist(world)
+    d.barrier()
+    m = d.max(1.0 + 2.5 * rank)  # each rank's own frame time
+    d.barrier()
+    d.close()
+    Path(f"{out}.{rank}").write_text(repr(m))
+
+
+def test_max_over_two_gloo_ranks(tmp_path):
+    out = str(tmp_path / "max")
+    mp.spawn(_rank_main, args=(2, _free_port(), out), nprocs=2, join=True)
+    for r in range(2):
+        assert float(Path(f"{out}.{r}").read_text()) == 3.5
+
+
+def test_single_rank_needs_no_process_group():
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    d = bench.Dist(1)
+    d.barrier()
+    assert d.max(2.0) == 2.0
+    d.close()
+
+
+def test_reference_arm_runs_on_rank_zero_only():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1", MASTER_ADDR="127.0.0.1")
+    res = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3"],
+                         cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert res.stdout.strip() == ""
