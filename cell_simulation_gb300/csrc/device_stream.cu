@@ -23,12 +23,13 @@ constexpr int LIST = 1024;  // one group holds at most 32 words x 32 bits
 
 }  // namespace
 
-// u32 words of one warp's shared-memory area: fields, three accumulators,
-// the item list (u16) and the warp's species deltas
-__host__ __device__ constexpr size_t stream_warp_words(uint32_t S1) { return (size_t)NF * 32 + 96 + LIST / 2 + S1; }
+// u32 words of one warp's shared-memory area: fields, three accumulators and
+// the item list (u16)
+__host__ __device__ constexpr size_t stream_warp_words() { return (size_t)NF * 32 + 96 + LIST / 2; }
 
 size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words) {
-    return ((size_t)(NT / 32) * stream_warp_words(S1) + PD_N + thr_words) * 4;
+    (void)S1;
+    return ((size_t)(NT / 32) * stream_warp_words() + PD_N + thr_words) * 4;
 }
 
 template <int K>
@@ -75,11 +76,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     extern __shared__ __align__(16) uint32_t sm[];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const uint32_t S1 = P.T.S1, NC = P.T.NC;
-    uint32_t* f = sm + (size_t)w * stream_warp_words(S1);  // [NF][32]
+    uint32_t* f = sm + (size_t)w * stream_warp_words();  // [NF][32]
     uint32_t* acc = f + NF * 32;                            // [3][32]: content, movers down, movers up
     uint16_t* list = reinterpret_cast<uint16_t*>(acc + 96);
-    int32_t* s_delta = reinterpret_cast<int32_t*>(acc + 96 + LIST / 2);  // [S1] this warp's species deltas
-    uint32_t* s_diag = sm + (size_t)NW * stream_warp_words(S1);        // [PD_N]
+    uint32_t* s_diag = sm + (size_t)NW * stream_warp_words();  // [PD_N]
     uint32_t* s_thr = s_diag + PD_N;
     allow_next_launch();
     const uint32_t* thr = P.T.thr;
@@ -88,7 +88,6 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         for (uint32_t i = tid; i < nt; i += NT) s_thr[i] = P.T.thr[i];
         thr = s_thr;
     }
-    for (uint32_t s = lane; s < S1; s += 32) s_delta[s] = 0;
     for (int i = tid; i < PD_N; i += NT) s_diag[i] = 0u;
     wait_previous_launch();
     const uint32_t frame = P.stepbuf[P.parity];
@@ -99,20 +98,6 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     __syncthreads();
     const bool zero_order = P.T.n_zero_order != 0u;
     const bool all_react = zero_order || P.reservoir != nullptr;
-    uint32_t cur_cidx = 0xFFFFFFFFu;
-    // this warp's species deltas into the counts of replicate cur_cidx
-    auto flush = [&]() {
-        __syncwarp();
-        if (cur_cidx != 0xFFFFFFFFu)
-            for (uint32_t s = lane; s < S1; s += 32) {
-                const int32_t dl = s_delta[s];
-                if (dl) {
-                    atomicAdd(P.counts + (size_t)cur_cidx * S1 + s, (unsigned long long)(long long)dl);
-                    s_delta[s] = 0;
-                }
-            }
-        __syncwarp();
-    };
     auto trow = [&](uint32_t a, uint32_t b) -> const uint32_t* { return thr + ((size_t)a * NC + b) * S1; };
 
     const uint32_t TW = gridDim.x * NW;
@@ -127,12 +112,6 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         const uint32_t g_next = SP.queue ? fetch() : g + TW;
         const WordGroup G = SP.groups[g];
         const RepDesc rd = P.reps[G.rep];
-        if constexpr (PASS == 3) {
-            if (rd.counts_index != cur_cidx) {
-                flush();
-                cur_cidx = rd.counts_index;
-            }
-        }
         const int X = (int)rd.X, Y = (int)rd.Y, Z = (int)rd.Z;
         const uint32_t Wz = rd.Wz;
         const int nk = (int)G.nk;
@@ -412,7 +391,6 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         __syncwarp();
         g = g_next;
     }
-    if constexpr (PASS == 3) flush();
     __syncthreads();
     for (int i = tid; i < PD_N; i += NT)
         if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
