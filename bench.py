@@ -207,18 +207,18 @@ def describe_variant(i):
     if kind == 1:
         return {"index": i, "kind": "brick", "slots": k, "brick": [bx, ty, tz], "threads": nt}
     if kind == 2:
-        return {"index": i, "kind": "stream", "slots": k, "words_per_group": 32, "threads": nt}
+        from cell_simulation_gb300 import tiling_launches
+        return {"index": i, "kind": "stream", "slots": k, "words_per_group": 32, "threads": nt,
+                "passes_per_frame": tiling_launches()[i]}
     return {"index": i, "kind": "tile", "slots": k, "tile": [ty, tz], "threads": nt}
 
 
 def launches_per_frame(i):
     """Kernel launches per frame of variant i: a brick pass with bounded pools is
-    followed by the pass over its spilled bricks; the sweep stream is four passes."""
-    from cell_simulation_gb300 import tiling_kinds
-    kind, bx = tiling_kinds()[i]
-    if kind == 2:
-        return 4
-    return 2 if kind == 1 and bx > 2 else 1
+    followed by the pass over its spilled bricks; the sweep stream is four passes,
+    or three where the Y and Z sweeps are one launch."""
+    from cell_simulation_gb300 import tiling_launches
+    return tiling_launches()[i]
 
 
 def ensemble_numbers(device, steps_batched=200, steps_plain=20):

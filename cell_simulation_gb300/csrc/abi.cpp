@@ -520,6 +520,13 @@ cs_status cs_tiling_kind(int32_t index, int32_t* kind, int32_t* brick_planes) {
     });
 }
 
+cs_status cs_tiling_launches(int32_t index, int32_t* launches) {
+    return guarded([&] {
+        need(launches, "launches");
+        *launches = prod_tiling_launches(index);
+    });
+}
+
 cs_status cs_set_tiling(cs_sim* sim, int32_t index, uint32_t segment_length) {
     return guarded([&] {
         need(sim, "sim");

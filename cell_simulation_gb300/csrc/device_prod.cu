@@ -114,6 +114,9 @@ static const std::vector<KernelCfg>& all_cfgs() {
         // sweep stream: 256 threads, at least two / four blocks per SM (pass 3 of variants 2, 3: three, two)
         stream_cfg(16, 0), stream_cfg(16, 1), stream_cfg(8, 0), stream_cfg(8, 1), stream_cfg(16, 2), stream_cfg(8, 2),
         stream_cfg(16, 3), stream_cfg(8, 3),
+        // sweep stream with the Y and Z sweeps fused into one launch (rows of at most 32 words), at
+        // three / four blocks per SM
+        stream_cfg(16, 4), stream_cfg(8, 4), stream_cfg(16, 5), stream_cfg(8, 5),
     };
     return v;
 }
@@ -162,7 +165,7 @@ struct DeviceProd {
     DevBuf<WordGroup> groups;
     std::vector<uint32_t> rep_group_off;
     uint32_t n_groups = 0;
-    DevBuf<uint4> rec[2];
+    DevBuf<uint4> rec[3];  // two parities; fused variants: x-, y- and z-decision records in 0, 1, 2
     DevBuf<uint32_t> sw[14];
     DevBuf<uint8_t> wcode;  // per bitmap word: uniform region code of its window, or 0 (single lattices)
     DevBuf<uint32_t> ssa_list;  // pass 3: output record indices of the voxels whose SSA runs in pass 4
@@ -417,18 +420,20 @@ static void build_one_table(DeviceProd* d) {
 }
 
 // Default step before any autotuning: the sweep stream of the model's K with
-// four-block sweep passes and a three-block pass 3 (the fastest variant on the
-// sparse lattices and the replicate ensemble measured), else its first brick
-// pass.
-static int pick_default_cfg(uint32_t K) {
+// four-block X sweeps and the Y and Z sweeps fused at three blocks per SM
+// (the fastest on the sparse 256^3 lattice measured) where rows have at most
+// 32 words, else four-block sweep passes and a three-block pass 3, else its
+// first brick pass.
+static int pick_default_cfg(uint32_t K, bool fused_ok) {
     const auto& c = all_cfgs();
-    int first = -1;
+    int first = -1, plain = -1;
     for (size_t i = 0; i < c.size(); i++) {
         if (c[i].K != (int)K) continue;
-        if (c[i].kind == KIND_STREAM && c[i].variant == 2) return (int)i;
+        if (c[i].kind == KIND_STREAM && c[i].variant == 4 && fused_ok) return (int)i;
+        if (c[i].kind == KIND_STREAM && c[i].variant == 2) plain = (int)i;
         if (first < 0 && c[i].kind == KIND_BRICK) first = (int)i;
     }
-    return first;
+    return plain >= 0 ? plain : first;
 }
 
 // The region code shared by every lattice voxel of brick w's region window
@@ -456,6 +461,13 @@ static uint32_t window_code(const DeviceProd* d, const RepDesc& r, const WorkIte
 // configuration uses segments of BX planes, x fastest, so that bricks sharing
 // halo planes run close together in time and the halo re-reads hit L2.
 static void build_groups(DeviceProd* d);
+
+// The fused Y and Z sweeps need every group to hold whole rows.
+static bool fused_fits(const DeviceProd* d) {
+    for (const RepDesc& r : d->h_reps)
+        if (r.Wz > 32) return false;
+    return true;
+}
 
 static void build_items(DeviceProd* d) {
     const KernelCfg& cfg = all_cfgs()[d->cfg_index];
@@ -539,6 +551,9 @@ static void build_groups(DeviceProd* d) {
         }
     }
     d->rep_group_off[d->n_rep] = (uint32_t)gs.size();
+    const bool fused = stream_variant_fused(all_cfgs()[d->cfg_index].variant);
+    if (fused && !fused_fits(d))
+        throw Error(CS_ERR_INVALID_ARG, "fused sweep-stream variant needs rows of at most 32 bitmap words (Z <= 1024)");
     if (rb >= (1ull << 32) || gs.size() >= (1ull << 32))
         throw Error(CS_ERR_LIMIT, "lattice too large for the sweep-stream step (at most 2^32 records)");
     d->n_groups = (uint32_t)gs.size();
@@ -580,7 +595,7 @@ static void build_groups(DeviceProd* d) {
     CS_CUDA(cudaMemcpy(d->groups.p, gs.data(), gs.size() * sizeof(WordGroup), cudaMemcpyHostToDevice));
     d->h_groups = std::move(gs);
     d->groups_sorted = false;
-    for (int b = 0; b < 2; b++)
+    for (int b = 0; b < (fused ? 3 : 2); b++)
         if (d->rec[b].n < 2 * rb) d->rec[b].alloc(2 * rb);  // two uint4 per record
     for (auto& a : d->sw)
         if (a.n < d->occ_words) a.alloc(d->occ_words);
@@ -639,6 +654,8 @@ static void set_attrs(const DeviceProd* d, const KernelCfg& cfg) {
 
 static void set_cfg(DeviceProd* d, int idx) {
     const KernelCfg& cfg = all_cfgs()[idx];
+    if (cfg.kind == KIND_STREAM && stream_variant_fused(cfg.variant) && !fused_fits(d))
+        throw Error(CS_ERR_INVALID_ARG, "fused sweep-stream variant needs rows of at most 32 bitmap words (Z <= 1024)");
     set_attrs(d, cfg);
     if (cfg.spill >= 0) set_attrs(d, all_cfgs()[cfg.spill]);
     d->cfg_index = idx;
@@ -706,7 +723,9 @@ static uint32_t* group_ctr(DeviceProd* d, int g, int p) { return d->counters.p +
 // One pass of a sweep-stream frame of parity `parity` over all word groups
 // (rep < 0) or over replicate rep's.  Records: the x-decisions of a frame of
 // parity p are in rec[p]; pass 1 writes rec[p ^ 1], pass 2 rec[p], and pass 3
-// (fused) the next frame's x-decisions into rec[p ^ 1].  Pass 1, the first
+// (fused) the next frame's x-decisions into rec[p ^ 1].  Fused variants keep
+// x-, y- and z-decisions in rec[0], rec[1] and rec[2]: their pass 2 sweeps
+// along y and z and writes the next frame's x-decisions back into rec[0].  Pass 1, the first
 // pass of every frame, resets the other parity's work counters (as the brick
 // pass does, so that the kinds can alternate); pass 3 advances the frame
 // number.
@@ -725,15 +744,18 @@ static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdPa
     const SweepWords x_in{const_cast<uint32_t*>(P.osrc), w[0], w[1], w[13], w[2]};
     const SweepWords y_dec{w[3], w[4], w[5], w[6], w[7]};
     const SweepWords z_dec{w[8], w[9], w[10], w[11], w[12]};
-    uint4* ra = d->rec[parity].p;
-    uint4* rb = d->rec[parity ^ 1].p;
+    const bool fused = stream_variant_fused(cfg.variant);
+    uint4* const rx = d->rec[fused ? 0 : parity].p;       // this frame's x-decisions
+    uint4* const ry = d->rec[fused ? 1 : parity ^ 1].p;   // y-decisions
+    uint4* const rz = d->rec[fused ? 2 : parity].p;       // z-decisions
+    uint4* const rnx = d->rec[fused ? 0 : parity ^ 1].p;  // the next frame's x-decisions
     const size_t smem = cfg_smem(d, cfg);
     const uint32_t nw = (uint32_t)cfg.NT / 32u;
     StreamParams S{};
     S.P = P;
     S.P.items = nullptr;
     S.P.n_items = 0;
-    S.P.advance = pass == 3 ? 1u : 0u;
+    S.P.advance = (pass == 3 || (fused && pass == 2)) ? 1u : 0u;
     S.P.n_reset = pass == 1 ? P.n_reset : 0u;
     S.groups = d->groups.p + goff;
     S.n_groups = ng;
@@ -743,10 +765,22 @@ static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdPa
     S.ssa_list = d->ssa_list.p;
     S.ssa_count = group_ctr(d, rep < 0 ? 0 : 1 + rep, parity) + 3;
     switch (pass) {
-        case 0: S.out = x_dec; S.rec_out = ra; break;
-        case 1: S.in = x_in; S.rec_in = ra; S.out = y_dec; S.rec_out = rb; break;
-        case 2: S.in = y_dec; S.rec_in = rb; S.out = z_dec; S.rec_out = ra; break;
-        default: S.in = z_dec; S.rec_in = ra; S.fuse = 1u; S.out = x_dec; S.rec_out = rb; break;
+        case 0: S.out = x_dec; S.rec_out = rx; break;
+        case 1: S.in = x_in; S.rec_in = rx; S.out = y_dec; S.rec_out = ry; break;
+        case 2:
+            S.in = y_dec;
+            S.rec_in = ry;
+            if (fused) {  // the Y and Z sweeps: z-decisions in rec_mid, the next frame's x-decisions out
+                S.rec_mid = rz;
+                S.fuse = 1u;
+                S.out = x_dec;
+                S.rec_out = rnx;
+            } else {
+                S.out = z_dec;
+                S.rec_out = rz;
+            }
+            break;
+        default: S.in = z_dec; S.rec_in = rz; S.fuse = 1u; S.out = x_dec; S.rec_out = rnx; break;
     }
     if (pass == 4) {
         // the SSA pass over the voxels pass 3 listed: a fixed grid that reads the count on the device
@@ -754,7 +788,7 @@ static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdPa
         S.rec_in = nullptr;
         S.fuse = 1u;
         S.out = x_dec;
-        S.rec_out = rb;
+        S.rec_out = rnx;
         if (!stream_ssa_launch(cfg.K, 2 * d->num_sms, stream_ssa_smem(d->S1, d->R), d->stream, S))
             throw Error(CS_ERR_INVALID_ARG, "sweep-stream kernel not compiled for this K");
         CS_LAUNCH_CHECK();
@@ -784,7 +818,9 @@ static void launch_stream_pass0(DeviceProd* d) {
 }
 
 static void launch_stream_frame(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity) {
-    for (int pass = 1; pass <= 4; pass++) launch_stream_pass(d, cfg, P, rep, parity, pass);
+    const bool fused = stream_variant_fused(cfg.variant);
+    for (int pass = 1; pass <= 4; pass++)
+        if (!(fused && pass == 3)) launch_stream_pass(d, cfg, P, rep, parity, pass);
 }
 
 // One frame over all replicates (batched) or over replicate `rep` alone.
@@ -894,7 +930,7 @@ static DeviceProd* prod_alloc(const Model& m, int device, const std::vector<RepD
     CS_CUDA(cudaMemset(d->counters.p, 0, d->counters.bytes()));
     CS_CUDA(cudaMemset(d->stepbuf.p, 0, 8));
     CS_CUDA(cudaMemset(d->counts.p, 0, d->counts.bytes()));
-    int ci = pick_default_cfg(d->K);
+    int ci = pick_default_cfg(d->K, fused_fits(d.get()));
     if (ci < 0) throw Error(CS_ERR_LIMIT, "no kernel configuration for this K");
     set_cfg(d.get(), ci);
     return d.release();
@@ -1294,6 +1330,12 @@ void prod_tiling_kind(int i, int* kind, int* BX) {
     if (i < 0 || i >= (int)c.size()) throw Error(CS_ERR_INVALID_ARG, "tile configuration index out of range");
     *kind = c[i].kind; *BX = c[i].BX;
 }
+int prod_tiling_launches(int i) {
+    const auto& c = all_cfgs();
+    if (i < 0 || i >= (int)c.size()) throw Error(CS_ERR_INVALID_ARG, "tile configuration index out of range");
+    if (c[i].kind == KIND_STREAM) return stream_variant_fused(c[i].variant) ? 3 : 4;
+    return c[i].spill >= 0 ? 2 : 1;
+}
 int prod_tiling_current(const DeviceProd* d) { return d->cfg_index; }
 cudaStream_t prod_stream(const DeviceProd* d) { return d->stream; }
 
@@ -1386,6 +1428,7 @@ int prod_autotune(DeviceProd* d, uint32_t frames, uint64_t frame0, bool batched,
     float best_t = 0.0f;
     for (int i = 0; i < (int)c.size(); i++) {
         if (c[i].K != (int)d->K) continue;
+        if (c[i].kind == KIND_STREAM && stream_variant_fused(c[i].variant) && !fused_fits(d)) continue;
         d->seg_len = 0;
         set_cfg(d, i);
         prod_time_frames(d, 2, frame0, batched);  // warm-up: graph, bitmaps, caches

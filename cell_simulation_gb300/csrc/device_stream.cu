@@ -2,6 +2,8 @@
 // launchers (see stream_kernel.cuh for the scheme).
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "cuda_check.h"
 #include "stream_kernel.cuh"
 
@@ -32,10 +34,18 @@ size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words) {
     return ((size_t)(NT / 32) * stream_warp_words() + PD_N + thr_words) * 4;
 }
 
-template <int K>
+// NC: the records were written by an earlier launch (read-only path); else
+// by this launch (the fused Y and Z sweeps), read coherently through L2.
+template <int K, bool NC = true>
 __device__ __forceinline__ void rec_load(const uint4* rec, uint32_t i, Vox<K>& c, uint4& t) {
-    const uint4 a = __ldg(rec + 2 * (size_t)i);
-    t = __ldg(rec + 2 * (size_t)i + 1);
+    uint4 a;
+    if constexpr (NC) {
+        a = __ldg(rec + 2 * (size_t)i);
+        t = __ldg(rec + 2 * (size_t)i + 1);
+    } else {
+        a = __ldcg(rec + 2 * (size_t)i);
+        t = __ldcg(rec + 2 * (size_t)i + 1);
+    }
     c.w[0] = (uint64_t)a.x | ((uint64_t)a.y << 32);
     if constexpr (K == 16) c.w[1] = (uint64_t)a.z | ((uint64_t)a.w << 32);
 }
@@ -68,7 +78,7 @@ __device__ __forceinline__ void allow_next_launch() { asm volatile("griddepcontr
 __device__ __forceinline__ void wait_previous_launch() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 
 // PASS 0: x-decisions; 1: X sweep + y-decisions; 2: Y sweep + z-decisions;
-// 3: Z sweep + reactions + store.
+// 3: Z sweep + reactions + store; PASS_YZ: 2 and then 3 on each group.
 template <int K, int PASS, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams SP) {
     constexpr int NW = NT / 32;
@@ -93,7 +103,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     const uint32_t frame = P.stepbuf[P.parity];
     if (blockIdx.x == 0 && tid == 0) {
         for (uint32_t i = 0; i < P.n_reset; i++) P.reset[i] = 0u;
-        if (PASS == 3 && P.advance) P.stepbuf[P.parity ^ 1u] = frame + 1u;
+        if ((PASS == 3 || PASS == PASS_YZ) && P.advance) P.stepbuf[P.parity ^ 1u] = frame + 1u;
     }
     __syncthreads();
     const bool zero_order = P.T.n_zero_order != 0u;
@@ -121,274 +131,318 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         const uint64_t wo = rd.obase + ((uint64_t)x * (uint64_t)Y + (uint64_t)y) * Wz + (uint64_t)kk;
         const int zb = 32 * kk;
         const uint32_t colm = !valid ? 0u : (Z - zb >= 32 ? 0xFFFFFFFFu : ((1u << (Z - zb)) - 1u));
-        uint32_t work = 0u, old = 0u, moving = 0u;  // moving: bits whose content changes along the axis
-        uint32_t own_occ = 0u, own_m = 0u, own_p = 0u, own_wk = 0u, own_bs = 0u;
-        uint32_t lo_occ = 0u, lo_p = 0u, lo_wk = 0u, lo_bs = 0u, hi_occ = 0u, hi_m = 0u, hi_wk = 0u, hi_bs = 0u;
-        if (valid) {
-            if constexpr (PASS == 0) {
-                own_occ = P.osrc[wo];
-                work = own_occ;
-            } else {
-                own_occ = SP.in.occ[wo];
-                own_m = SP.in.mv_m[wo];
-                own_p = SP.in.mv_p[wo];
-                own_wk = SP.in.work[wo];
-                own_bs = SP.in.base[wo];
-                // neighbour words: other rows for the X and Y sweeps, the row's adjacent words for Z
-                const uint64_t st = PASS == 1 ? (uint64_t)Y * Wz : PASS == 2 ? (uint64_t)Wz : 1ull;
-                const bool hl = PASS == 1 ? x > 0 : PASS == 2 ? y > 0 : kk > 0;
-                const bool hh = PASS == 1 ? x + 1 < X : PASS == 2 ? y + 1 < Y : kk + 1 < (int)Wz;
-                if (hl) {
-                    lo_occ = SP.in.occ[wo - st];
-                    lo_p = SP.in.mv_p[wo - st];
-                    lo_wk = SP.in.work[wo - st];
-                    lo_bs = SP.in.base[wo - st];
-                }
-                if (hh) {
-                    hi_occ = SP.in.occ[wo + st];
-                    hi_m = SP.in.mv_m[wo + st];
-                    hi_wk = SP.in.work[wo + st];
-                    hi_bs = SP.in.base[wo + st];
-                }
-                if constexpr (PASS == 3) {
+        // One sweep PP of the group.  CH (PASS_YZ): the Y sweep leaves its output words in this
+        // warp's shared memory and its records in rec_mid, and the Z sweep starts from them.
+        auto sweep = [&](auto pass_c, auto chain_c) {
+            constexpr int PP = decltype(pass_c)::value;
+            constexpr bool CH = decltype(chain_c)::value;
+            const uint4* const rin = (CH && PP == 3) ? SP.rec_mid : SP.rec_in;
+            uint4* const rout = (CH && PP == 2) ? SP.rec_mid : SP.rec_out;
+            uint32_t work = 0u, old = 0u, moving = 0u;  // moving: bits whose content changes along the axis
+            uint32_t own_occ = 0u, own_m = 0u, own_p = 0u, own_wk = 0u, own_bs = 0u;
+            uint32_t lo_occ = 0u, lo_p = 0u, lo_wk = 0u, lo_bs = 0u, hi_occ = 0u, hi_m = 0u, hi_wk = 0u, hi_bs = 0u;
+            if constexpr (CH && PP == 3) {
+                // the Y sweep's words of this lane; the row's previous and next words are the
+                // neighbouring lanes' (a group holds whole rows)
+                own_occ = acc[lane];
+                own_m = acc[32 + lane];
+                own_p = acc[64 + lane];
+                own_wk = f[F_OWK * 32 + lane];
+                own_bs = f[F_OBS * 32 + lane];
+                const uint32_t u_occ = __shfl_up_sync(0xffffffffu, own_occ, 1), u_p = __shfl_up_sync(0xffffffffu, own_p, 1),
+                               u_wk = __shfl_up_sync(0xffffffffu, own_wk, 1), u_bs = __shfl_up_sync(0xffffffffu, own_bs, 1);
+                const uint32_t d_occ = __shfl_down_sync(0xffffffffu, own_occ, 1), d_m = __shfl_down_sync(0xffffffffu, own_m, 1),
+                               d_wk = __shfl_down_sync(0xffffffffu, own_wk, 1), d_bs = __shfl_down_sync(0xffffffffu, own_bs, 1);
+                if (valid) {
+                    if (kk > 0) {
+                        lo_occ = u_occ;
+                        lo_p = u_p;
+                        lo_wk = u_wk;
+                        lo_bs = u_bs;
+                    }
+                    if (kk + 1 < (int)Wz) {
+                        hi_occ = d_occ;
+                        hi_m = d_m;
+                        hi_wk = d_wk;
+                        hi_bs = d_bs;
+                    }
                     old = P.odst[wo];
                     const uint32_t from_lo = (own_p << 1) | (lo_p >> 31), from_hi = (own_m >> 1) | (hi_m << 31);
                     work = (own_occ | from_lo | from_hi | (all_react ? colm : 0u)) & colm;
                     moving = own_m | own_p | from_lo | from_hi;
+                }
+            } else if (valid) {
+                if constexpr (PP == 0) {
+                    own_occ = P.osrc[wo];
+                    work = own_occ;
                 } else {
-                    work = (own_occ | lo_p | hi_m) & colm;
-                    moving = own_m | own_p | lo_p | hi_m;
+                    own_occ = SP.in.occ[wo];
+                    own_m = SP.in.mv_m[wo];
+                    own_p = SP.in.mv_p[wo];
+                    own_wk = SP.in.work[wo];
+                    own_bs = SP.in.base[wo];
+                    // neighbour words: other rows for the X and Y sweeps, the row's adjacent words for Z
+                    const uint64_t st = PP == 1 ? (uint64_t)Y * Wz : PP == 2 ? (uint64_t)Wz : 1ull;
+                    const bool hl = PP == 1 ? x > 0 : PP == 2 ? y > 0 : kk > 0;
+                    const bool hh = PP == 1 ? x + 1 < X : PP == 2 ? y + 1 < Y : kk + 1 < (int)Wz;
+                    if (hl) {
+                        lo_occ = SP.in.occ[wo - st];
+                        lo_p = SP.in.mv_p[wo - st];
+                        lo_wk = SP.in.work[wo - st];
+                        lo_bs = SP.in.base[wo - st];
+                    }
+                    if (hh) {
+                        hi_occ = SP.in.occ[wo + st];
+                        hi_m = SP.in.mv_m[wo + st];
+                        hi_wk = SP.in.work[wo + st];
+                        hi_bs = SP.in.base[wo + st];
+                    }
+                    if constexpr (PP == 3) {
+                        old = P.odst[wo];
+                        const uint32_t from_lo = (own_p << 1) | (lo_p >> 31), from_hi = (own_m >> 1) | (hi_m << 31);
+                        work = (own_occ | from_lo | from_hi | (all_react ? colm : 0u)) & colm;
+                        moving = own_m | own_p | from_lo | from_hi;
+                    } else {
+                        work = (own_occ | lo_p | hi_m) & colm;
+                        moving = own_m | own_p | lo_p | hi_m;
+                    }
                 }
             }
-        }
-        f[F_OCC * 32 + lane] = own_occ;
-        f[F_M * 32 + lane] = own_m;
-        f[F_P * 32 + lane] = own_p;
-        f[F_WK * 32 + lane] = own_wk;
-        f[F_BS * 32 + lane] = own_bs;
-        f[F_LOCC * 32 + lane] = lo_occ;
-        f[F_LP * 32 + lane] = lo_p;
-        f[F_LWK * 32 + lane] = lo_wk;
-        f[F_LBS * 32 + lane] = lo_bs;
-        f[F_HOCC * 32 + lane] = hi_occ;
-        f[F_HM * 32 + lane] = hi_m;
-        f[F_HWK * 32 + lane] = hi_wk;
-        f[F_HBS * 32 + lane] = hi_bs;
-        f[F_OLD * 32 + lane] = old;
-        f[F_Y * 32 + lane] = (uint32_t)y;
-        f[F_KK * 32 + lane] = (uint32_t)kk;
-        f[F_VROW * 32 + lane] = ((uint32_t)x * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z;
-        {
-            // the word's uniform region code; bit 8: its whole window lies inside the lattice, so
-            // every neighbour of its voxels has that code too
-            const uint32_t uc = (rd.flags & 1u) ? 1u : (SP.wcode && valid) ? (uint32_t)SP.wcode[wo] : 0u;
-            const bool inner = x > 0 && x + 1 < X && y > 0 && y + 1 < Y && kk > 0 && kk + 1 < (int)Wz;
-            f[F_CODE * 32 + lane] = uc | (uc && inner ? 0x100u : 0u);
-        }
-        // List the work bits in three classes, so that the lanes of a warp mostly run the same
-        // path: voxels with a record of the previous pass whose content does not change along
-        // the axis, those whose content changes, and those without a record (arrivals), whose
-        // Philox blocks are then evaluated by full warps.
-        // Records are indexed by the work bits alone, whatever the list order.
-        const uint32_t cls_a = PASS == 0 ? work : (work & own_occ & ~moving);
-        const uint32_t cls_b = PASS == 0 ? 0u : (work & own_occ & moving);
-        const uint32_t na = (uint32_t)__popc(cls_a), nb = (uint32_t)__popc(cls_b), nw = (uint32_t)__popc(work);
-        uint32_t incl = na | (nb << 16), inw = nw;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o), uw = __shfl_up_sync(0xffffffffu, inw, o);
-            if (lane >= o) {
-                incl += u;
-                inw += uw;
+            f[F_OCC * 32 + lane] = own_occ;
+            f[F_M * 32 + lane] = own_m;
+            f[F_P * 32 + lane] = own_p;
+            f[F_WK * 32 + lane] = own_wk;
+            f[F_BS * 32 + lane] = own_bs;
+            f[F_LOCC * 32 + lane] = lo_occ;
+            f[F_LP * 32 + lane] = lo_p;
+            f[F_LWK * 32 + lane] = lo_wk;
+            f[F_LBS * 32 + lane] = lo_bs;
+            f[F_HOCC * 32 + lane] = hi_occ;
+            f[F_HM * 32 + lane] = hi_m;
+            f[F_HWK * 32 + lane] = hi_wk;
+            f[F_HBS * 32 + lane] = hi_bs;
+            f[F_OLD * 32 + lane] = old;
+            f[F_Y * 32 + lane] = (uint32_t)y;
+            f[F_KK * 32 + lane] = (uint32_t)kk;
+            f[F_VROW * 32 + lane] = ((uint32_t)x * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z;
+            {
+                // the word's uniform region code; bit 8: its whole window lies inside the lattice, so
+                // every neighbour of its voxels has that code too
+                const uint32_t uc = (rd.flags & 1u) ? 1u : (SP.wcode && valid) ? (uint32_t)SP.wcode[wo] : 0u;
+                const bool inner = x > 0 && x + 1 < X && y > 0 && y + 1 < Y && kk > 0 && kk + 1 < (int)Wz;
+                f[F_CODE * 32 + lane] = uc | (uc && inner ? 0x100u : 0u);
             }
-        }
-        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31), total = __shfl_sync(0xffffffffu, inw, 31);
-        const uint32_t total_a = tot & 0xFFFFu, total_ab = total_a + (tot >> 16);
-        const uint32_t ex = incl - (na | (nb << 16)), exa = ex & 0xFFFFu, exb = ex >> 16, exw = inw - nw;
-        f[F_OWK * 32 + lane] = work;
-        f[F_OBS * 32 + lane] = (uint32_t)G.rbase + exw;
-        acc[lane] = 0u;
-        acc[32 + lane] = 0u;
-        acc[64 + lane] = 0u;
-        {
-            auto put = [&](uint32_t bits, uint32_t o) {
-                while (bits) {
-                    const int b = __ffs((int)bits) - 1;
-                    bits &= bits - 1u;
-                    list[o++] = (uint16_t)((lane << 5) | b);
+            // List the work bits in three classes, so that the lanes of a warp mostly run the same
+            // path: voxels with a record of the previous pass whose content does not change along
+            // the axis, those whose content changes, and those without a record (arrivals), whose
+            // Philox blocks are then evaluated by full warps.
+            // Records are indexed by the work bits alone, whatever the list order.
+            const uint32_t cls_a = PP == 0 ? work : (work & own_occ & ~moving);
+            const uint32_t cls_b = PP == 0 ? 0u : (work & own_occ & moving);
+            const uint32_t na = (uint32_t)__popc(cls_a), nb = (uint32_t)__popc(cls_b), nw = (uint32_t)__popc(work);
+            uint32_t incl = na | (nb << 16), inw = nw;
+    #pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o), uw = __shfl_up_sync(0xffffffffu, inw, o);
+                if (lane >= o) {
+                    incl += u;
+                    inw += uw;
                 }
-            };
-            put(cls_a, exa);
-            put(cls_b, total_a + exb);
-            put(work & ~(cls_a | cls_b), total_ab + (exw - exa - exb));
-        }
-        __syncwarp();
+            }
+            const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31), total = __shfl_sync(0xffffffffu, inw, 31);
+            const uint32_t total_a = tot & 0xFFFFu, total_ab = total_a + (tot >> 16);
+            const uint32_t ex = incl - (na | (nb << 16)), exa = ex & 0xFFFFu, exb = ex >> 16, exw = inw - nw;
+            f[F_OWK * 32 + lane] = work;
+            f[F_OBS * 32 + lane] = (uint32_t)G.rbase + exw;
+            acc[lane] = 0u;
+            acc[32 + lane] = 0u;
+            acc[64 + lane] = 0u;
+            {
+                auto put = [&](uint32_t bits, uint32_t o) {
+                    while (bits) {
+                        const int b = __ffs((int)bits) - 1;
+                        bits &= bits - 1u;
+                        list[o++] = (uint16_t)((lane << 5) | b);
+                    }
+                };
+                put(cls_a, exa);
+                put(cls_b, total_a + exb);
+                put(work & ~(cls_a | cls_b), total_ab + (exw - exa - exb));
+            }
+            __syncwarp();
 
-        const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
-        const uint8_t* rpad = P.region_pad + rd.rbase;
-        const uint64_t Zr = rd.Zr;
-        // region code (id + 1) of voxel (xx, yy, zz) of the window of a word with uniform code uc
-        // (0: look it up; bit 8: the whole window is inside the lattice); 0 outside the lattice
-        auto code = [&](uint32_t uc, int xx, int yy, int zz) -> uint32_t {
-            if (uc & 0x100u) return uc & 0xFFu;
-            if ((unsigned)xx >= (unsigned)X || (unsigned)yy >= (unsigned)Y || (unsigned)zz >= (unsigned)Z) return 0u;
-            if (uc) return uc;
-            return __ldg(rpad + ((uint64_t)xx * (uint64_t)Y + (uint64_t)yy) * Zr + (uint64_t)zz + 2u);
-        };
-        const uint32_t YZ = (uint32_t)Y * (uint32_t)Z;
-        for (uint32_t t = (uint32_t)lane; t < total; t += 32) {
-            const uint32_t e = list[t];
-            const int i = (int)(e >> 5), b = (int)(e & 31u);
-            const uint32_t bit = 1u << b;
-            const int yy = (int)f[F_Y * 32 + i], zz = 32 * (int)f[F_KK * 32 + i] + b;
-            const uint32_t v = f[F_VROW * 32 + i] + (uint32_t)zz;
-            const uint32_t uc = f[F_CODE * 32 + i];
-            const uint32_t ri = f[F_OBS * 32 + i] + below(f[F_OWK * 32 + i], bit);  // this pass's record of the item
-            if constexpr (PASS == 0) {
-                const Vox<K> own = ld_vox_g<K>(P.src + (rd.base + v) * K);
-                const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
-                const uint32_t rs = code(uc, x, yy, zz);
-                const uint32_t d = decide_moves<K>(own, v, frame, 0u, trow(rs, code(uc, x - 1, yy, zz)),
-                                                   trow(rs, code(uc, x + 1, yy, zz)), k0, k1, b0.x);
-                rec_store<K>(SP.rec_out, ri, own, make_uint4(d, b0.y, b0.z, b0.w));
-                if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
-                if (d >> 16) atomicOr(acc + 64 + i, bit);
-            } else {
-                const uint32_t occ = f[F_OCC * 32 + i];
-                Vox<K> own = vox_zero<K>(), lo = vox_zero<K>(), hi = vox_zero<K>();
-                uint32_t dme = 0u, dlo = 0u, dhi = 0u;
-                uint4 tw = make_uint4(0u, 0u, 0u, 0u);
-                const bool own_in = (occ & bit) != 0u;
-                if (own_in) {
-                    rec_load<K>(SP.rec_in, f[F_BS * 32 + i] + below(f[F_WK * 32 + i], bit), own, tw);
-                    dme = tw.x;
-                }
-                // a neighbour's record is needed when it sends to this voxel or receives from it
-                bool need_lo, need_hi;
-                uint32_t ilo, ihi;
-                if constexpr (PASS == 3) {
-                    const uint32_t m = f[F_M * 32 + i], p = f[F_P * 32 + i];
-                    if (b > 0) {
-                        const uint32_t lb = bit >> 1;
-                        need_lo = (occ & lb) && ((m & bit) || (p & lb));
-                        ilo = f[F_BS * 32 + i] + below(f[F_WK * 32 + i], lb);
-                    } else {
-                        need_lo = (f[F_LOCC * 32 + i] >> 31) && ((m & bit) || (f[F_LP * 32 + i] >> 31));
-                        ilo = f[F_LBS * 32 + i] + below(f[F_LWK * 32 + i], 0x80000000u);
-                    }
-                    if (b < 31) {
-                        const uint32_t hb = bit << 1;
-                        need_hi = (occ & hb) && ((p & bit) || (m & hb));
-                        ihi = f[F_BS * 32 + i] + below(f[F_WK * 32 + i], hb);
-                    } else {
-                        need_hi = (f[F_HOCC * 32 + i] & 1u) && ((p & bit) || (f[F_HM * 32 + i] & 1u));
-                        ihi = f[F_HBS * 32 + i];
-                    }
+            const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
+            const uint8_t* rpad = P.region_pad + rd.rbase;
+            const uint64_t Zr = rd.Zr;
+            // region code (id + 1) of voxel (xx, yy, zz) of the window of a word with uniform code uc
+            // (0: look it up; bit 8: the whole window is inside the lattice); 0 outside the lattice
+            auto code = [&](uint32_t uc, int xx, int yy, int zz) -> uint32_t {
+                if (uc & 0x100u) return uc & 0xFFu;
+                if ((unsigned)xx >= (unsigned)X || (unsigned)yy >= (unsigned)Y || (unsigned)zz >= (unsigned)Z) return 0u;
+                if (uc) return uc;
+                return __ldg(rpad + ((uint64_t)xx * (uint64_t)Y + (uint64_t)yy) * Zr + (uint64_t)zz + 2u);
+            };
+            const uint32_t YZ = (uint32_t)Y * (uint32_t)Z;
+            for (uint32_t t = (uint32_t)lane; t < total; t += 32) {
+                const uint32_t e = list[t];
+                const int i = (int)(e >> 5), b = (int)(e & 31u);
+                const uint32_t bit = 1u << b;
+                const int yy = (int)f[F_Y * 32 + i], zz = 32 * (int)f[F_KK * 32 + i] + b;
+                const uint32_t v = f[F_VROW * 32 + i] + (uint32_t)zz;
+                const uint32_t uc = f[F_CODE * 32 + i];
+                const uint32_t ri = f[F_OBS * 32 + i] + below(f[F_OWK * 32 + i], bit);  // this pass's record of the item
+                if constexpr (PP == 0) {
+                    const Vox<K> own = ld_vox_g<K>(P.src + (rd.base + v) * K);
+                    const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
+                    const uint32_t rs = code(uc, x, yy, zz);
+                    const uint32_t d = decide_moves<K>(own, v, frame, 0u, trow(rs, code(uc, x - 1, yy, zz)),
+                                                       trow(rs, code(uc, x + 1, yy, zz)), k0, k1, b0.x);
+                    rec_store<K>(rout, ri, own, make_uint4(d, b0.y, b0.z, b0.w));
+                    if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
+                    if (d >> 16) atomicOr(acc + 64 + i, bit);
                 } else {
-                    need_lo = (f[F_LOCC * 32 + i] & bit) && ((f[F_M * 32 + i] | f[F_LP * 32 + i]) & bit);
-                    need_hi = (f[F_HOCC * 32 + i] & bit) && ((f[F_P * 32 + i] | f[F_HM * 32 + i]) & bit);
-                    ilo = f[F_LBS * 32 + i] + below(f[F_LWK * 32 + i], bit);
-                    ihi = f[F_HBS * 32 + i] + below(f[F_HWK * 32 + i], bit);
-                }
-                if (need_lo) {
-                    uint4 tl;
-                    rec_load<K>(SP.rec_in, ilo, lo, tl);
-                    dlo = tl.x;
-                }
-                if (need_hi) {
-                    uint4 th;
-                    rec_load<K>(SP.rec_in, ihi, hi, th);
-                    dhi = th.x;
-                }
-                const uint32_t vs = PASS == 1 ? YZ : PASS == 2 ? (uint32_t)Z : 1u;
-                Vox<K> r = combine<K>(own, dme, lo, dlo, hi, dhi, v, v - vs, v + vs, frame, (uint32_t)(PASS - 1));
-                if constexpr (PASS == 1 || PASS == 2) {
-                    if (!vox_empty<K>(r)) {
-                        // this voxel's Philox words: carried in its record, or evaluated here
-                        uint32_t wd, wn1, wn2;
-                        if (own_in) {
-                            wd = tw.y;
-                            wn1 = tw.z;
-                            wn2 = tw.w;
+                    const uint32_t occ = f[F_OCC * 32 + i];
+                    Vox<K> own = vox_zero<K>(), lo = vox_zero<K>(), hi = vox_zero<K>();
+                    uint32_t dme = 0u, dlo = 0u, dhi = 0u;
+                    uint4 tw = make_uint4(0u, 0u, 0u, 0u);
+                    const bool own_in = (occ & bit) != 0u;
+                    if (own_in) {
+                        rec_load<K, !(CH && PP == 3)>(rin, f[F_BS * 32 + i] + below(f[F_WK * 32 + i], bit), own, tw);
+                        dme = tw.x;
+                    }
+                    // a neighbour's record is needed when it sends to this voxel or receives from it
+                    bool need_lo, need_hi;
+                    uint32_t ilo, ihi;
+                    if constexpr (PP == 3) {
+                        const uint32_t m = f[F_M * 32 + i], p = f[F_P * 32 + i];
+                        if (b > 0) {
+                            const uint32_t lb = bit >> 1;
+                            need_lo = (occ & lb) && ((m & bit) || (p & lb));
+                            ilo = f[F_BS * 32 + i] + below(f[F_WK * 32 + i], lb);
                         } else {
-                            const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
-                            wd = PASS == 1 ? b0.y : b0.z;
-                            wn1 = PASS == 1 ? b0.z : b0.w;
-                            wn2 = PASS == 1 ? b0.w : 0u;
+                            need_lo = (f[F_LOCC * 32 + i] >> 31) && ((m & bit) || (f[F_LP * 32 + i] >> 31));
+                            ilo = f[F_LBS * 32 + i] + below(f[F_LWK * 32 + i], 0x80000000u);
                         }
-                        const uint32_t rs = code(uc, x, yy, zz);
-                        const uint32_t clo = PASS == 1 ? code(uc, x, yy - 1, zz) : code(uc, x, yy, zz - 1);
-                        const uint32_t chi = PASS == 1 ? code(uc, x, yy + 1, zz) : code(uc, x, yy, zz + 1);
-                        const uint32_t d =
-                            decide_moves<K>(r, v, frame, (uint32_t)PASS, trow(rs, clo), trow(rs, chi), k0, k1, wd);
-                        rec_store<K>(SP.rec_out, ri, r, make_uint4(d, wn1, wn2, 0u));
-                        atomicOr(acc + i, bit);
-                        if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
-                        if (d >> 16) atomicOr(acc + 64 + i, bit);
-                    }
-                } else {
-                    const uint32_t rv = P.reservoir ? (uint32_t)P.reservoir[rd.base + v] : 0u;
-                    bool listed = false;
-                    if (rv != 0u || zero_order || !vox_empty<K>(r)) {
-                        const uint32_t w3 = own_in ? tw.y : d_philox(v, frame, 0u, 0u, k0, k1).w;
-                        const bool calm =
-                            rv == 0u && !zero_order &&
-                            calm_voxel<K>(r, w3, P.T.quiet + (size_t)rd.counts_index * S1 * P.T.QS, P.T.QS,
-                                          P.T.one + (size_t)rd.counts_index * S1 * 3, P.T.g23 + 2 * rd.counts_index,
-                                          P.T.a2 ? P.T.a2 + (size_t)rd.counts_index * S1 * S1 : nullptr, P.T.tau);
-                        if (!calm) {
-                            // pass 4 runs this voxel's SSA: its content waits in its output record
-                            rec_store<K>(SP.rec_out, ri, r, make_uint4(v, w3, rv, G.rep));
-                            SP.ssa_list[atomicAdd(SP.ssa_count, 1u)] = ri;
-                            listed = true;
+                        if (b < 31) {
+                            const uint32_t hb = bit << 1;
+                            need_hi = (occ & hb) && ((p & bit) || (m & hb));
+                            ihi = f[F_BS * 32 + i] + below(f[F_WK * 32 + i], hb);
+                        } else {
+                            need_hi = (f[F_HOCC * 32 + i] & 1u) && ((p & bit) || (f[F_HM * 32 + i] & 1u));
+                            ihi = f[F_HBS * 32 + i];
                         }
+                    } else {
+                        need_lo = (f[F_LOCC * 32 + i] & bit) && ((f[F_M * 32 + i] | f[F_LP * 32 + i]) & bit);
+                        need_hi = (f[F_HOCC * 32 + i] & bit) && ((f[F_P * 32 + i] | f[F_HM * 32 + i]) & bit);
+                        ilo = f[F_LBS * 32 + i] + below(f[F_LWK * 32 + i], bit);
+                        ihi = f[F_HBS * 32 + i] + below(f[F_HWK * 32 + i], bit);
                     }
-                    if (!listed && !vox_empty<K>(r)) {
-                        st_vox_g<K>(P.dst + (rd.base + v) * K, r);
-                        atomicOr(acc + i, bit);
-                        if (SP.fuse) {
-                            // pass 0 of the next frame for this voxel
-                            const uint32_t nf = frame + 1u;
-                            const U4 b0 = d_philox(v, nf, 0u, 0u, k0, k1);
+                    if (need_lo) {
+                        uint4 tl;
+                        rec_load<K, !(CH && PP == 3)>(rin, ilo, lo, tl);
+                        dlo = tl.x;
+                    }
+                    if (need_hi) {
+                        uint4 th;
+                        rec_load<K, !(CH && PP == 3)>(rin, ihi, hi, th);
+                        dhi = th.x;
+                    }
+                    const uint32_t vs = PP == 1 ? YZ : PP == 2 ? (uint32_t)Z : 1u;
+                    Vox<K> r = combine<K>(own, dme, lo, dlo, hi, dhi, v, v - vs, v + vs, frame, (uint32_t)(PP - 1));
+                    if constexpr (PP == 1 || PP == 2) {
+                        if (!vox_empty<K>(r)) {
+                            // this voxel's Philox words: carried in its record, or evaluated here
+                            uint32_t wd, wn1, wn2;
+                            if (own_in) {
+                                wd = tw.y;
+                                wn1 = tw.z;
+                                wn2 = tw.w;
+                            } else {
+                                const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
+                                wd = PP == 1 ? b0.y : b0.z;
+                                wn1 = PP == 1 ? b0.z : b0.w;
+                                wn2 = PP == 1 ? b0.w : 0u;
+                            }
                             const uint32_t rs = code(uc, x, yy, zz);
-                            const uint32_t d = decide_moves<K>(r, v, nf, 0u, trow(rs, code(uc, x - 1, yy, zz)),
-                                                               trow(rs, code(uc, x + 1, yy, zz)), k0, k1, b0.x);
-                            rec_store<K>(SP.rec_out, ri, r, make_uint4(d, b0.y, b0.z, b0.w));
+                            const uint32_t clo = PP == 1 ? code(uc, x, yy - 1, zz) : code(uc, x, yy, zz - 1);
+                            const uint32_t chi = PP == 1 ? code(uc, x, yy + 1, zz) : code(uc, x, yy, zz + 1);
+                            const uint32_t d =
+                                decide_moves<K>(r, v, frame, (uint32_t)PP, trow(rs, clo), trow(rs, chi), k0, k1, wd);
+                            rec_store<K>(rout, ri, r, make_uint4(d, wn1, wn2, 0u));
+                            atomicOr(acc + i, bit);
                             if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
                             if (d >> 16) atomicOr(acc + 64 + i, bit);
                         }
+                    } else {
+                        const uint32_t rv = P.reservoir ? (uint32_t)P.reservoir[rd.base + v] : 0u;
+                        bool listed = false;
+                        if (rv != 0u || zero_order || !vox_empty<K>(r)) {
+                            const uint32_t w3 = own_in ? tw.y : d_philox(v, frame, 0u, 0u, k0, k1).w;
+                            const bool calm =
+                                rv == 0u && !zero_order &&
+                                calm_voxel<K>(r, w3, P.T.quiet + (size_t)rd.counts_index * S1 * P.T.QS, P.T.QS,
+                                              P.T.one + (size_t)rd.counts_index * S1 * 3, P.T.g23 + 2 * rd.counts_index,
+                                              P.T.a2 ? P.T.a2 + (size_t)rd.counts_index * S1 * S1 : nullptr, P.T.tau);
+                            if (!calm) {
+                                // pass 4 runs this voxel's SSA: its content waits in its output record
+                                rec_store<K>(rout, ri, r, make_uint4(v, w3, rv, G.rep));
+                                SP.ssa_list[atomicAdd(SP.ssa_count, 1u)] = ri;
+                                listed = true;
+                            }
+                        }
+                        if (!listed && !vox_empty<K>(r)) {
+                            st_vox_g<K>(P.dst + (rd.base + v) * K, r);
+                            atomicOr(acc + i, bit);
+                            if (SP.fuse) {
+                                // pass 0 of the next frame for this voxel
+                                const uint32_t nf = frame + 1u;
+                                const U4 b0 = d_philox(v, nf, 0u, 0u, k0, k1);
+                                const uint32_t rs = code(uc, x, yy, zz);
+                                const uint32_t d = decide_moves<K>(r, v, nf, 0u, trow(rs, code(uc, x - 1, yy, zz)),
+                                                                   trow(rs, code(uc, x + 1, yy, zz)), k0, k1, b0.x);
+                                rec_store<K>(rout, ri, r, make_uint4(d, b0.y, b0.z, b0.w));
+                                if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
+                                if (d >> 16) atomicOr(acc + 64 + i, bit);
+                            }
+                        }
                     }
                 }
             }
-        }
-        __syncwarp();
-        if (valid) {
-            if constexpr (PASS == 0) {
-                SP.out.mv_m[wo] = acc[32 + lane];
-                SP.out.mv_p[wo] = acc[64 + lane];
-                SP.out.work[wo] = work;
-                SP.out.base[wo] = f[F_OBS * 32 + lane];
-            } else if constexpr (PASS == 3) {
-                P.odst[wo] = acc[lane];
-                // voxels the destination held that end the frame empty get zeros
-                for (uint32_t bits = old & ~acc[lane]; bits; bits &= bits - 1u)
-                    st_vox_g<K>(P.dst + (rd.base + f[F_VROW * 32 + lane] + (uint32_t)zb + (uint32_t)(__ffs((int)bits) - 1)) * K,
-                                vox_zero<K>());
-                if (SP.fuse) {
+            __syncwarp();
+            if (valid) {
+                if constexpr (PP == 0) {
+                    SP.out.mv_m[wo] = acc[32 + lane];
+                    SP.out.mv_p[wo] = acc[64 + lane];
+                    SP.out.work[wo] = work;
+                    SP.out.base[wo] = f[F_OBS * 32 + lane];
+                } else if constexpr (PP == 3) {
+                    P.odst[wo] = acc[lane];
+                    // voxels the destination held that end the frame empty get zeros
+                    for (uint32_t bits = old & ~acc[lane]; bits; bits &= bits - 1u)
+                        st_vox_g<K>(P.dst + (rd.base + f[F_VROW * 32 + lane] + (uint32_t)zb + (uint32_t)(__ffs((int)bits) - 1)) * K,
+                                    vox_zero<K>());
+                    if (SP.fuse) {
+                        SP.out.mv_m[wo] = acc[32 + lane];
+                        SP.out.mv_p[wo] = acc[64 + lane];
+                        SP.out.work[wo] = work;
+                        SP.out.base[wo] = f[F_OBS * 32 + lane];
+                    }
+                } else if constexpr (!CH) {
+                    SP.out.occ[wo] = acc[lane];
                     SP.out.mv_m[wo] = acc[32 + lane];
                     SP.out.mv_p[wo] = acc[64 + lane];
                     SP.out.work[wo] = work;
                     SP.out.base[wo] = f[F_OBS * 32 + lane];
                 }
-            } else {
-                SP.out.occ[wo] = acc[lane];
-                SP.out.mv_m[wo] = acc[32 + lane];
-                SP.out.mv_p[wo] = acc[64 + lane];
-                SP.out.work[wo] = work;
-                SP.out.base[wo] = f[F_OBS * 32 + lane];
             }
+            __syncwarp();
+        };  // sweep
+        if constexpr (PASS == PASS_YZ) {
+            sweep(std::integral_constant<int, 2>{}, std::true_type{});
+            sweep(std::integral_constant<int, 3>{}, std::true_type{});
+        } else {
+            sweep(std::integral_constant<int, PASS>{}, std::false_type{});
         }
-        __syncwarp();
         g = g_next;
     }
     __syncthreads();
@@ -511,9 +565,11 @@ bool stream_ssa_launch(int K, int grid, size_t smem, cudaStream_t s, const Strea
 namespace {
 struct Variant {
     int NT, MINB, MINB3;  // threads per block, minimum resident blocks per SM of passes 0-2 and of pass 3
+    bool fused;           // passes 2 and 3 as one launch (PASS_YZ at MINB3 blocks per SM)
 };
 // compiled launch shapes; pass 3 (reactions) needs more registers than the sweeps
-constexpr Variant kVariants[] = {{256, 2, 2}, {256, 4, 4}, {256, 4, 3}, {256, 4, 2}};
+constexpr Variant kVariants[] = {{256, 2, 2, false}, {256, 4, 4, false}, {256, 4, 3, false}, {256, 4, 2, false},
+                                 {256, 4, 3, true}, {256, 4, 4, true}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 template <int K, int NT, int MINB, int MINB3>
@@ -526,6 +582,17 @@ void* pass_fn(int pass) {
     }
 }
 
+// fused variants: the Y and Z sweeps are launched as pass 2; there is no pass 3
+template <int K, int NT, int MINB, int MINB3>
+void* pass_fn_fused(int pass) {
+    switch (pass) {
+        case 0: return reinterpret_cast<void*>(&sweep_pass_kernel<K, 0, NT, MINB>);
+        case 1: return reinterpret_cast<void*>(&sweep_pass_kernel<K, 1, NT, MINB>);
+        case 2: return reinterpret_cast<void*>(&sweep_pass_kernel<K, PASS_YZ, NT, MINB3>);
+        default: return nullptr;
+    }
+}
+
 template <int K>
 void* fn_of(int variant, int pass) {
     switch (variant) {
@@ -533,6 +600,8 @@ void* fn_of(int variant, int pass) {
         case 1: return pass_fn<K, 256, 4, 4>(pass);
         case 2: return pass_fn<K, 256, 4, 3>(pass);
         case 3: return pass_fn<K, 256, 4, 2>(pass);
+        case 4: return pass_fn_fused<K, 256, 4, 3>(pass);
+        case 5: return pass_fn_fused<K, 256, 4, 4>(pass);
         default: return nullptr;
     }
 }
@@ -544,6 +613,7 @@ void* kernel_of(int K, int variant, int pass) {
 }  // namespace
 
 int stream_variant_count() { return kNumVariants; }
+bool stream_variant_fused(int variant) { return variant >= 0 && variant < kNumVariants && kVariants[variant].fused; }
 int stream_variant_threads(int variant) { return variant >= 0 && variant < kNumVariants ? kVariants[variant].NT : 0; }
 
 // Launch with programmatic stream serialization (see wait_previous_launch).

@@ -171,6 +171,7 @@ void prod_set_tiling(DeviceProd* d, int cfg_index, uint32_t seg_len);
 int prod_tiling_count();
 void prod_tiling_desc(int i, int* K, int* TY, int* TZ, int* NT);
 void prod_tiling_kind(int i, int* kind, int* BX);
+int prod_tiling_launches(int i);
 void prod_set_counts(DeviceProd* d, const int64_t* counts);
 // out_device (V floats, caller-owned device memory) or, when null, out_host
 void prod_render_view(DeviceProd* d, int32_t view, int32_t slice_axis, uint32_t slice, float* out_host, void* out_device);

@@ -22,6 +22,16 @@
 // standalone pass 0 when those decisions are absent or stale (the first
 // frame, a new lattice, seed, frame number or step configuration).
 //
+// The Z sweep of a row needs nothing but that row's z-decisions, and a group
+// holds whole rows when a row has at most 32 words (Z <= 1024).  The fused
+// variants then run passes 2 and 3 as one launch (PASS_YZ): each warp sweeps
+// its group along y and at once along z, the z-decision words passing
+// through the warp's shared memory and registers instead of global arrays.
+// Their records take three buffers with fixed roles (x-, y- and z-decisions),
+// because the Y sweep of one group still reads the y-decision records of the
+// neighbouring groups' rows while another group's Z sweep writes next-frame
+// x-decisions.
+//
 // A warp takes a word group: up to 32 bitmap words of one replicate, one per
 // lane (rows of one x plane, z fastest).  Each lane builds the word's work
 // mask from its own words and those of the neighbouring rows (or, for the
@@ -81,15 +91,22 @@ struct StreamParams {
     SweepWords in;   // produced by the previous pass (pass 0: unused)
     SweepWords out;  // produced by this pass (pass 3: the next frame's x-decisions when fused)
     const uint4* rec_in;
+    uint4* rec_mid;  // PASS_YZ: the z-decision records its Y sweep writes and its Z sweep reads
     uint4* rec_out;
     uint32_t* ssa_list;   // output record indices of the voxels listed for pass 4
     uint32_t* ssa_count;  // their number (zero at the start of the frame)
 };
 
+// Template value of the fused Y and Z sweep (passes 2 and 3 in one launch).
+constexpr int PASS_YZ = 5;
+
 // Compiled launch shapes ("variants": threads per block and minimum resident
 // blocks per SM) of the four passes.
 int stream_variant_count();
 int stream_variant_threads(int variant);
+// True when the variant runs passes 2 and 3 as one launch (PASS_YZ, launched
+// as its pass 2); it needs rows of at most 32 bitmap words.
+bool stream_variant_fused(int variant);
 // Launches pass `pass` (0..3) of variant `variant` for slot count K.
 // Returns false when no such kernel is compiled.
 bool stream_launch(int K, int variant, int pass, int grid, size_t smem, cudaStream_t s, const StreamParams& SP);

@@ -107,6 +107,7 @@ SIGNATURES = {
     "cs_tiling_count": (st, [i32p]),
     "cs_tiling_describe": (st, [C.c_int32, i32p, i32p, i32p, i32p]),
     "cs_tiling_kind": (st, [C.c_int32, i32p, i32p]),
+    "cs_tiling_launches": (st, [C.c_int32, i32p]),
     "cs_autotune": (st, [P, C.c_uint32, i32p, C.POINTER(C.c_float)]),
     "cs_checkpoint_save": (st, [P, C.c_char_p]),
     "cs_checkpoint_load": (st, [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p)]),

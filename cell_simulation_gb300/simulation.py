@@ -373,6 +373,20 @@ def tiling_kinds() -> list[tuple[int, int]]:
     return out
 
 
+def tiling_launches() -> list[int]:
+    """Kernel launches per frame of every compiled variant, once a run is under
+    way (cs_tiling_launches)."""
+    lib = N.load()
+    n = C.c_int32()
+    N.check(lib.cs_tiling_count(C.byref(n)))
+    out = []
+    for i in range(n.value):
+        k = C.c_int32()
+        N.check(lib.cs_tiling_launches(i, C.byref(k)))
+        out.append(k.value)
+    return out
+
+
 class Ensemble:
     """Replicates of one model stepped by one launch per frame (cs_ensemble_*)."""
 

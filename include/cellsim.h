@@ -274,11 +274,15 @@ cs_status cs_step_philox_timed(cs_sim* sim, uint32_t n_steps, uint64_t seed, flo
  * bricks, crowded bricks finished by a full-capacity second brick pass;
  * kind 2 = sweep stream (the default): barrier-free passes over groups of 32
  * occupancy-bitmap words (TY = 0, TZ = 32, brick_planes = 0).  Every variant
- * computes the same lattice.  No reference counterpart (the reference has one
- * fixed dispatch shape per shader). */
+ * computes the same lattice.  cs_tiling_launches: kernel launches per frame
+ * once a run is under way (the sweep stream: 4, or 3 where the Y and Z sweeps
+ * are one launch; those variants need Z <= 1024 and cs_set_tiling refuses
+ * them otherwise).  No reference counterpart (the reference has one fixed
+ * dispatch shape per shader). */
 cs_status cs_tiling_count(int32_t* n);
 cs_status cs_tiling_describe(int32_t index, int32_t* K, int32_t* TY, int32_t* TZ, int32_t* threads);
 cs_status cs_tiling_kind(int32_t index, int32_t* kind, int32_t* brick_planes);
+cs_status cs_tiling_launches(int32_t index, int32_t* launches);
 cs_status cs_set_tiling(cs_sim* sim, int32_t index, uint32_t segment_length);
 cs_status cs_get_tiling(const cs_sim* sim, int32_t* index);
 /* Autotuner: times every compiled variant for this K on the handle's own

@@ -4,8 +4,8 @@ conservation, region confinement and batched-ensemble equivalence."""
 import numpy as np
 import pytest
 
-from cell_simulation_gb300 import (Ensemble, PREC_FP32, PREC_FP64, PREC_MIXED, RNG_PHILOX, configs, tiling_kinds,
-                                   tiling_variants)
+from cell_simulation_gb300 import (CellsimError, Ensemble, PREC_FP32, PREC_FP64, PREC_MIXED, RNG_PHILOX, configs,
+                                   tiling_kinds, tiling_launches, tiling_variants)
 from tests.helpers import crowded_model, multi_region_model, oracle_args, patchy_model
 
 pytestmark = pytest.mark.gpu
@@ -130,6 +130,22 @@ def test_sweep_stream_matches_oracle(orc, K):
             assert np.array_equal(got_s, want_s), (ti, np.flatnonzero(got_s != want_s)[:8])
             assert np.array_equal(got_c, want_c), ti
             assert np.array_equal(got_d[:4], want_d[:4]), (ti, got_d, want_d)
+
+
+def test_fused_sweep_stream_needs_short_rows(orc):
+    """The fused Y and Z sweeps need rows of at most 32 bitmap words: on a lattice with Z = 1056
+    (33 words) cs_set_tiling refuses them and the handle keeps stepping with its own variant."""
+    mk = lambda: multi_region_model(res=(3, 4, 1056), K=16, counts=(40, 30, 20, 10))
+    want_s, want_c, _ = oracle_prod(orc, mk(), 3, seed=31)
+    sim = mk()
+    sim.prepare_for_gpu(RNG_PHILOX, 0)
+    launches = tiling_launches()
+    fused = next(i for i in stream_tilings(16) if launches[i] == 3)
+    with pytest.raises(CellsimError, match="at most 32 bitmap words"):
+        sim.set_tiling(fused)
+    sim.step_philox(3, 31)
+    assert np.array_equal(sim.get_lattice()[0].astype(np.uint8), want_s)
+    assert np.array_equal(sim.counts(), want_c)
 
 
 def test_sweep_stream_recomputes_stale_decisions(orc):
@@ -269,18 +285,21 @@ def test_switching_step_kinds_mid_run_matches_oracle(orc):
 
 
 def test_switching_to_and_from_the_sweep_stream_matches_oracle(orc):
-    """Brick, sweep-stream and tile frames in one run: frames of another kind (and an upload)
-    make the x-decisions the last stream frame left for the next frame stale, so the stream
-    recomputes them.  Odd frame counts change the parity the kinds hand over."""
+    """Brick, sweep-stream (four launches, and Y and Z sweeps fused) and tile frames in one run:
+    frames of another kind (and an upload) make the x-decisions the last stream frame left for the
+    next frame stale, so the stream recomputes them.  Odd frame counts change the parity the kinds
+    hand over; the fused variant keeps its records in buffers of fixed roles."""
     mk = lambda: multi_region_model(res=(13, 17, 40), K=16, counts=(90, 70, 50, 40))
-    want_s, want_c, _ = oracle_prod(orc, mk(), 21, seed=777)
+    want_s, want_c, _ = oracle_prod(orc, mk(), 24, seed=777)
     sim = mk()
     sim.prepare_for_gpu(RNG_PHILOX, 0)
     kinds = tiling_kinds()
     tile = next(i for i, (t, k) in enumerate(zip(tiling_variants(), kinds)) if t[0] == 16 and k[0] == 0)
     brick = next(i for i, (t, k) in enumerate(zip(tiling_variants(), kinds)) if t[0] == 16 and k == (1, 8))
-    stream = stream_tilings(16)[-1]
-    for ti, n in ((stream, 3), (brick, 4), (stream, 5), (tile, 3), (stream, 2)):
+    launches = tiling_launches()
+    stream = [i for i in stream_tilings(16) if launches[i] == 4][-1]
+    fused = next(i for i in stream_tilings(16) if launches[i] == 3)
+    for ti, n in ((stream, 3), (brick, 4), (fused, 5), (tile, 3), (stream, 2), (fused, 3)):
         sim.set_tiling(ti)
         sim.step_philox(n, 777)
     sim.set_lattice(sim.get_lattice()[0])
