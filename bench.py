@@ -299,8 +299,11 @@ def main():
     peak, peak_kind = measured_peaks()
     alg_bytes = V * (2 * K + 1)
     achieved = alg_bytes / per_launch_s / 1e9
-    kernel = {"brick": "brick_step_kernel", "stream": "sweep_pass_kernel"}.get(describe_variant(variant)["kind"],
-                                                                             "prod_step_kernel")
+    desc = describe_variant(variant)
+    kernel = {"brick": "brick_step_kernel", "stream": "sweep_pass_kernel"}.get(desc["kind"], "prod_step_kernel")
+    if desc["kind"] == "stream":
+        # the frame's longest launch: pass 3, or the fused Y and Z sweeps (template pass 5)
+        kernel += "<5>" if desc["passes_per_frame"] == 3 else "<3>"
     traffic = profiled_traffic(kernel, w.name)
     diag = sim.diagnostics()
 
