@@ -1,5 +1,6 @@
-// device_stream.cu — the four passes of the sweep-stream step and their
-// launchers (see stream_kernel.cuh for the scheme).
+// device_stream.cu — the passes of the sweep-stream step (four, or three
+// launches with the Y and Z sweeps fused) and their launchers (see
+// stream_kernel.cuh for the scheme).
 #include <cuda_runtime.h>
 
 #include <type_traits>

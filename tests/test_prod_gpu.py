@@ -227,7 +227,11 @@ def test_graph_replay_equals_single_launches():
     assert np.array_equal(a.counts(), b.counts())
 
 
-def test_ensemble_batched_equals_plain_and_oracle(orc):
+@pytest.mark.parametrize("variant", ["default", "four_launches", "fused_last"])
+def test_ensemble_batched_equals_plain_and_oracle(orc, variant):
+    """Replicates of different sizes in one launch per pass: batched frames equal per-replicate
+    (plain) frames and the oracle, for the default step (fused Y and Z sweeps), a four-launch
+    sweep stream and the fused stream at four blocks per SM."""
     tmpl = configs.c4_ensemble_template(K=8)
     res = np.array([[9, 9, 9], [12, 12, 12], [7, 7, 7], [16, 16, 16]], np.uint32)
     seeds = np.array([11, 22, 33, 44], np.uint64)
@@ -235,6 +239,12 @@ def test_ensemble_batched_equals_plain_and_oracle(orc):
     init = np.array([0, 40, 40, 5], np.uint32)
     eb = Ensemble(tmpl, res, seeds, mult, init)
     ep = Ensemble(tmpl, res, seeds, mult, init)
+    if variant != "default":
+        launches = tiling_launches()
+        want = 4 if variant == "four_launches" else 3
+        ti = [i for i in stream_tilings(8) if launches[i] == want][-1]
+        eb.set_tiling(ti)
+        ep.set_tiling(ti)
     s0 = eb.slots()
     eb.step(30, batched=True)
     ep.step(30, batched=False)
