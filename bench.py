@@ -307,16 +307,17 @@ def main():
     traffic = profiled_traffic(kernel, w.name)
     diag = sim.diagnostics()
 
-    # end to end through the C ABI: every frame one step call (frame number up)
-    # and one blocking read of the species counts (down), like the
-    # reference's per-frame submit + stats readback
+    # end to end through the C ABI: every frame one step call (its frame number
+    # up, 4 bytes; the seed is uploaded only when it changes) and one blocking
+    # read of the species counts (down), like the reference's per-frame itime
+    # write, submit and stats readback
     n_e2e = min(args.steps, 500)
     t0 = time.perf_counter()
     for _ in range(n_e2e):
         sim.step_philox(1, seed)
         sim.counts()
     e2e_s = time.perf_counter() - t0
-    e2e = {"value": world * V * n_e2e / dist.max(e2e_s), "unit": UNIT, "h2d_bytes_per_step": 4 + 8,
+    e2e = {"value": world * V * n_e2e / dist.max(e2e_s), "unit": UNIT, "h2d_bytes_per_step": 4,
            "d2h_bytes_per_step": S1 * 8, "steps": n_e2e,
            "setup_s": {"host_model_build": t_build, "upload_prepare_for_gpu": t_upload}}
 

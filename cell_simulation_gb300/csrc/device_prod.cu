@@ -181,6 +181,13 @@ struct DeviceProd {
     int xdec_cur = 0, xdec_cfg = -1;
     uint64_t seed_epoch = 0;  // advanced whenever the Philox keys change
     uint64_t next_frame = 0;  // host copy of the frame number in stepbuf[cur]
+    unsigned long long* h_counts = nullptr;  // pinned read-back buffer of the counts (n_rep * S1)
+    // pinned slots of the first frame number of each step call, copied in stream order; a slot
+    // is reused once its event shows that its copy has run
+    static constexpr int kFrameSlots = 8;
+    uint32_t* h_frames = nullptr;
+    cudaEvent_t frame_ev[kFrameSlots] = {};
+    int frame_slot = 0;
     int cur = 0;
     ProdTables T{};
     int cfg_index = -1;
@@ -191,6 +198,10 @@ struct DeviceProd {
     int graph_cfg = -1;
     ~DeviceProd() {
         if (graph) cudaGraphExecDestroy(graph);
+        if (h_counts) cudaFreeHost(h_counts);
+        if (h_frames) cudaFreeHost(h_frames);
+        for (cudaEvent_t e : frame_ev)
+            if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -1120,6 +1131,23 @@ static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched) {
     }
 }
 
+// The frame number of the next frame into stepbuf[cur] (the step's one
+// host-to-device input, like the reference's per-frame itime write), in
+// stream order and without a host wait.
+static void upload_frame(DeviceProd* d, uint64_t frame0) {
+    if (!d->h_frames) {
+        CS_CUDA(cudaMallocHost(&d->h_frames, DeviceProd::kFrameSlots * sizeof(uint32_t)));
+        for (cudaEvent_t& e : d->frame_ev) CS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const int s = d->frame_slot;
+    d->frame_slot = (s + 1) % DeviceProd::kFrameSlots;
+    CS_CUDA(cudaEventSynchronize(d->frame_ev[s]));  // the slot's previous copy has run (at once if never recorded)
+    d->h_frames[s] = (uint32_t)frame0;
+    CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, d->h_frames + s, 4, cudaMemcpyHostToDevice, d->stream));
+    CS_CUDA(cudaEventRecord(d->frame_ev[s], d->stream));
+    d->next_frame = frame0;
+}
+
 void prod_step(DeviceProd* d, uint32_t n_steps, uint64_t seed, int precision, uint64_t frame0, uint32_t write_freq,
                const std::vector<uint32_t>& logging, std::vector<cs_stat_sample>& samples) {
     DeviceGuard g(d->device);
@@ -1136,10 +1164,7 @@ void prod_step(DeviceProd* d, uint32_t n_steps, uint64_t seed, int precision, ui
     // Samples are device-to-device copies of the counts into a ring, read back
     // once at the end: the frames in between are enqueued without host waits.
     uint64_t f = frame0, end = frame0 + n_steps;
-    const uint32_t f32 = (uint32_t)frame0;
-    CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, &f32, 4, cudaMemcpyHostToDevice, d->stream));
-    CS_CUDA(cudaStreamSynchronize(d->stream));
-    d->next_frame = frame0;
+    upload_frame(d, frame0);
     if (!sample_frames.empty() && d->sample_ring.n < sample_frames.size() * d->S1)
         d->sample_ring.alloc(sample_frames.size() * d->S1);
     for (size_t i = 0; i < sample_frames.size(); i++) {
@@ -1161,10 +1186,11 @@ void prod_step(DeviceProd* d, uint32_t n_steps, uint64_t seed, int precision, ui
 
 void prod_get_counts(DeviceProd* d, int64_t* counts) {
     DeviceGuard g(d->device);
-    std::vector<unsigned long long> h((size_t)d->n_rep * d->S1);
-    CS_CUDA(cudaMemcpyAsync(h.data(), d->counts.p, h.size() * 8, cudaMemcpyDeviceToHost, d->stream));
+    const size_t n = (size_t)d->n_rep * d->S1;
+    if (!d->h_counts) CS_CUDA(cudaMallocHost(&d->h_counts, n * 8));
+    CS_CUDA(cudaMemcpyAsync(d->h_counts, d->counts.p, n * 8, cudaMemcpyDeviceToHost, d->stream));
     CS_CUDA(cudaStreamSynchronize(d->stream));
-    for (size_t i = 0; i < h.size(); i++) counts[i] = (int64_t)h[i];
+    for (size_t i = 0; i < n; i++) counts[i] = (int64_t)d->h_counts[i];
 }
 
 void prod_set_counts(DeviceProd* d, const int64_t* counts) {

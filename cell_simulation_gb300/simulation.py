@@ -261,11 +261,13 @@ class Simulation:
         """Simulation::step (src/simulation.rs:99-150) for len(itimes) frames with the reference RNG."""
         it = np.ascontiguousarray(itimes, np.uint32)
         N.check(self._lib.cs_step(self._h, len(it), N.ptr(it, C.c_uint32), write_freq))
-        self._drain_stats()
+        if write_freq:  # samples come only from calls that log
+            self._drain_stats()
 
     def step_philox(self, n_steps: int, seed: int, write_freq: int = 0) -> None:
         N.check(self._lib.cs_step_philox(self._h, n_steps, seed, write_freq))
-        self._drain_stats()
+        if write_freq:
+            self._drain_stats()
 
     def step_timed(self, itimes: Sequence[int]) -> float:
         it = np.ascontiguousarray(itimes, np.uint32)
@@ -318,8 +320,10 @@ class Simulation:
 
     def counts(self) -> np.ndarray:
         """Species counts (StatisticsGroup buffer 0, src/statistics.rs:11-69)."""
-        out = np.zeros(self.info().n_species + 1, np.int64)
+        s1 = getattr(self, "_s1", None) or self.info().n_species + 1
+        out = np.zeros(s1, np.int64)
         N.check(self._lib.cs_get_counts(self._h, N.ptr(out, C.c_int64)))
+        self._s1 = s1  # counts exist once the model is prepared, and it no longer changes then
         return out
 
     def diagnostics(self, n: int = 8) -> np.ndarray:
