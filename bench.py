@@ -221,14 +221,17 @@ def launches_per_frame(i):
     return tiling_launches()[i]
 
 
-def ensemble_numbers(device, steps_batched=200, steps_plain=20):
+def ensemble_numbers(device, steps_batched=200, steps_plain=20, variant=-1):
     from cell_simulation_gb300 import Ensemble, configs
 
     tmpl = configs.c4_ensemble_template(K=8)
     res, seeds, mult, init = configs.c4_ensemble_spec()
     ens = Ensemble(tmpl, res, seeds, mult, init, device=device)
     tot, items = ens.info()
-    variant, _ = ens.autotune(3)
+    if variant >= 0:
+        ens.set_tiling(variant)
+    else:
+        variant, _ = ens.autotune(3)
     per_frame = launches_per_frame(variant)
     ens.step(3, batched=True)
     ms_b = ens.step_timed(steps_batched, batched=True)
@@ -256,6 +259,9 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip ensemble, reference-RNG, e2e and CPU legs")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--variant", type=int, default=-1, help="step variant index (default: autotuned)")
+    ap.add_argument("--ensemble-only", action="store_true",
+                    help="only the 512-replicate ensemble leg: --steps batched frames, a tenth as many plain ones "
+                         "(for profiling; prints that leg's numbers)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = env_rank()
@@ -265,6 +271,9 @@ def main():
 
     import __graft_entry__
     __graft_entry__.build()
+    if args.ensemble_only:
+        print(json.dumps(ensemble_numbers(local, args.steps, max(1, args.steps // 10), args.variant)), flush=True)
+        return
     from cell_simulation_gb300 import PREC_MIXED, RNG_PHILOX, RNG_REFERENCE, configs
 
     dist = Dist(world)

@@ -209,6 +209,40 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                     }
                 }
             }
+            // A group without work (most groups of sparse replicates) writes what the full path
+            // would: empty words (base = the group's first record), and in the Z sweep zeros for
+            // the voxels the destination held.  The fused Y sweep leaves its empty words in
+            // shared memory.
+            if (!__any_sync(0xffffffffu, work != 0u)) {
+                if constexpr (CH && PP == 2) {
+                    acc[lane] = 0u;
+                    acc[32 + lane] = 0u;
+                    acc[64 + lane] = 0u;
+                    f[F_OWK * 32 + lane] = 0u;
+                    f[F_OBS * 32 + lane] = (uint32_t)G.rbase;
+                } else if (valid) {
+                    if constexpr (PP == 3) {
+                        P.odst[wo] = 0u;
+                        const uint32_t vrow = ((uint32_t)x * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z + (uint32_t)zb;
+                        for (uint32_t bits = old; bits; bits &= bits - 1u)
+                            st_vox_g<K>(P.dst + (rd.base + vrow + (uint32_t)(__ffs((int)bits) - 1)) * K, vox_zero<K>());
+                        if (SP.fuse) {
+                            SP.out.mv_m[wo] = 0u;
+                            SP.out.mv_p[wo] = 0u;
+                            SP.out.work[wo] = 0u;
+                            SP.out.base[wo] = (uint32_t)G.rbase;
+                        }
+                    } else {
+                        if constexpr (PP != 0) SP.out.occ[wo] = 0u;
+                        SP.out.mv_m[wo] = 0u;
+                        SP.out.mv_p[wo] = 0u;
+                        SP.out.work[wo] = 0u;
+                        SP.out.base[wo] = (uint32_t)G.rbase;
+                    }
+                }
+                __syncwarp();
+                return;
+            }
             f[F_OCC * 32 + lane] = own_occ;
             f[F_M * 32 + lane] = own_m;
             f[F_P * 32 + lane] = own_p;
