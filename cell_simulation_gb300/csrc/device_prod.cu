@@ -562,9 +562,7 @@ static void build_groups(DeviceProd* d) {
         }
     }
     d->rep_group_off[d->n_rep] = (uint32_t)gs.size();
-    const bool fused = stream_variant_fused(all_cfgs()[d->cfg_index].variant);
-    if (fused && !fused_fits(d))
-        throw Error(CS_ERR_INVALID_ARG, "fused sweep-stream variant needs rows of at most 32 bitmap words (Z <= 1024)");
+    const bool fused = stream_variant_fused(all_cfgs()[d->cfg_index].variant);  // set_cfg checked that rows fit
     if (rb >= (1ull << 32) || gs.size() >= (1ull << 32))
         throw Error(CS_ERR_LIMIT, "lattice too large for the sweep-stream step (at most 2^32 records)");
     d->n_groups = (uint32_t)gs.size();
@@ -736,10 +734,10 @@ static uint32_t* group_ctr(DeviceProd* d, int g, int p) { return d->counters.p +
 // parity p are in rec[p]; pass 1 writes rec[p ^ 1], pass 2 rec[p], and pass 3
 // (fused) the next frame's x-decisions into rec[p ^ 1].  Fused variants keep
 // x-, y- and z-decisions in rec[0], rec[1] and rec[2]: their pass 2 sweeps
-// along y and z and writes the next frame's x-decisions back into rec[0].  Pass 1, the first
-// pass of every frame, resets the other parity's work counters (as the brick
-// pass does, so that the kinds can alternate); pass 3 advances the frame
-// number.
+// along y and z and writes the next frame's x-decisions back into rec[0].
+// Pass 1, the first pass of every frame, resets the other parity's work
+// counters (as the brick pass does, so that the kinds can alternate); pass 3
+// (fused variants: pass 2) advances the frame number.
 static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity, int pass) {
     uint32_t goff = 0, ng = d->n_groups;
     if (rep >= 0) {
@@ -1341,8 +1339,14 @@ void prod_set_tiling(DeviceProd* d, int cfg_index, uint32_t seg_len) {
     if (cfg_index < 0 || cfg_index >= (int)c.size() || c[cfg_index].K != (int)d->K)
         throw Error(CS_ERR_INVALID_ARG, "tile configuration does not exist for this K");
     CS_CUDA(cudaStreamSynchronize(d->stream));
+    const uint32_t keep = d->seg_len;
     d->seg_len = seg_len;
-    set_cfg(d, cfg_index);
+    try {
+        set_cfg(d, cfg_index);
+    } catch (...) {
+        d->seg_len = keep;  // a refused variant leaves the handle as it was
+        throw;
+    }
 }
 
 int prod_tiling_count() { return (int)all_cfgs().size(); }
