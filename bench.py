@@ -2,16 +2,19 @@
 
 Default workload: the 256^3, 16-slot, 16-species / 30-reaction multi-region
 lattice (the roofline configuration), production path (Philox, FP32
-propensities with FP64 clock), one fused launch per frame.  `value` is
-voxel-steps/s over the whole job with the lattice resident in HBM; the
-lattice (2 x 256 MiB) is larger than L2, so no flush is needed between
-timed frames.  Also reported: the batched 512-replicate ensemble vs the
-plain one-launch-per-replicate path (replicate-steps/s), the reference-RNG
-CUDA path on the same lattice, an end-to-end number through the C ABI, the
-roofline of the fused kernel and a CPU baseline (the oracle's
-reference-semantics port, OpenMP on the host cores).
+propensities with FP64 clock), the autotuned step variant (the sweep stream:
+three or four launches per frame).  `value` is voxel-steps/s over the whole
+job with the lattice resident in HBM; the lattice (2 x 256 MiB) is larger
+than L2, so no flush is needed between timed frames.  Also reported: the
+batched 512-replicate ensemble vs the plain one-launch-group-per-replicate
+path (replicate-steps/s), the reference-RNG CUDA path on the same lattice,
+an end-to-end number through the C ABI, the frame's roofline (algorithmic
+bytes over the frame time, with the profiled DRAM traffic of its longest
+launch) and a CPU baseline (the oracle's reference-semantics port, OpenMP on
+the host cores).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py --ensemble-only --variant V --steps K   (the ensemble leg alone, for profiling)
 """
 from __future__ import annotations
 

@@ -57,3 +57,14 @@ def test_reference_arm_runs_on_rank_zero_only():
                          cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
     assert res.returncode == 0, res.stderr[-2000:]
     assert res.stdout.strip() == ""
+
+
+def test_profiled_traffic_covers_the_reported_kernels():
+    """bench.py reads the DRAM traffic of the frame's longest launch from the committed ncu
+    summaries: every kernel it can report on the 256^3 workload has an entry."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    for kernel in ("sweep_pass_kernel<5>", "sweep_pass_kernel<3>", "brick_step_kernel", "prod_step_kernel"):
+        t = bench.profiled_traffic(kernel, "c3_multi_region_256x256x256_K16")
+        assert t is not None and t > 1e7, kernel
