@@ -71,7 +71,12 @@ class Dist:
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms with a host timestamp per row.
+
+    A timed region of a few milliseconds is shorter than nvidia-smi's sampling interval, so the
+    benchmark keeps the GPU busy with untimed frames right after the timed region until the
+    window that starts at the timed region holds at least three rows, and reports the rows of that
+    window (`window` in the result says so)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -80,23 +85,34 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.lines: list[str] = []
+        self.rows: list[tuple[float, list[str]]] = []
 
-    def start(self):
+    def start(self, wait_s: float = 5.0):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, bufsize=1)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while not self.rows and time.perf_counter() - t0 < wait_s and self.proc.poll() is None:
+            time.sleep(0.02)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            if line.count(",") >= 8:
+                self.rows.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
 
-    def stop(self):
+    def rows_since(self, t: float) -> int:
+        return sum(1 for ts, _ in self.rows if ts >= t)
+
+    def alive(self) -> bool:
+        return self.proc is not None and self.proc.poll() is None
+
+    def stop(self, t_from: float, t_to: float):
         if not self.proc:
             return None
         self.proc.terminate()
@@ -105,16 +121,23 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.t.join(timeout=2)
-        rows = [[x.strip() for x in l.split(",")] for l in self.lines if l.count(",") >= 8]
+        rows = [r for ts, r in self.rows if t_from <= ts <= t_to]
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [v for v in (num(r[1]) for r in rows) if v is not None]
+        mx = [v for v in (num(r[2]) for r in rows) if v is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
-        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
-        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "window": "the timed region and the untimed frames right after it (one window, GPU busy "
+                          "throughout)"}
 
 
 def measured_peaks():
@@ -135,38 +158,60 @@ def profiled_traffic(kernel: str, workload: str):
     return None
 
 
-def cpu_reference_rate(budget_s: float, threads: int):
-    """Oracle reference-semantics step (gather + OpenMP) on an x-slab through
-    the centre of the 256^3 multi-region cell; returns (voxel-steps/s, sample)."""
+def central_slab(workload, nx: int):
+    """The nx planes through the centre of a workload's lattice, cut out of the full lattice (same
+    particles, regions and tables): reference-layout arguments and state for the oracle.  The slab's
+    faces act as the lattice boundary."""
     import oracle
-    from cell_simulation_gb300 import configs
+
+    sim = workload.sim
+    i = sim.info()
+    X, Y, Z = (int(r) for r in i.res)
+    K, S1 = i.max_particles_site, i.n_species + 1
+    x0 = max(0, X // 2 - nx // 2)
+    x1 = min(X, x0 + nx)
+    s, o, c = sim.get_lattice()
+    tab = sim.tables()
+    cut = lambda a, w: np.ascontiguousarray(a.reshape(X, Y, Z * w)[x0:x1]).reshape(-1)
+    t = type(tab)(cut(tab.regions, 1), tab.diffusion, tab.stoich, tab.reactants, tab.rates, cut(tab.reservoir, 1))
+    s, o, c = cut(s, K), cut(o, 1), cut(c, S1)
+    st = c.reshape(-1, S1).sum(0).astype(np.int32)
+    args = ((x1 - x0, Y, Z), K, i.n_regions, i.n_species, i.n_reactions, float(np.float32(i.tau)),
+            float(np.float32(i.lambda_)), t)
+    V = (x1 - x0) * Y * Z
+    desc = (f"the {x1 - x0}x{Y}x{Z} x-slab through the centre of {workload.name}, cut out of the full lattice "
+            f"({V} voxels, {int((s > 0).sum())} particles: the full lattice's own particles and regions)")
+    return args, oracle.RefState(s, o, c, st), V, desc
+
+
+def cpu_reference_rate(workload, nx: int, budget_s: float, threads: int, max_frames: int = 100_000):
+    """The oracle's reference-semantics step (gather form, OpenMP) on a slab of a workload:
+    frames until budget_s has passed; returns (voxel-steps/s, sample description)."""
+    import oracle
 
     oracle.build()
-    nx = 8
-    w = configs.c3_multi_region(res=(nx, 256, 256), total_particles=int(1_000_000 * nx / 256))
-    sim = w.sim
-    i = sim.info()
-    s, o, c = sim.get_lattice()
-    st = c.reshape(-1, i.n_species + 1).sum(0).astype(np.int32)
-    state = oracle.RefState(s, o, c, st)
-    args = (tuple(i.res), i.max_particles_site, i.n_regions, i.n_species, i.n_reactions, float(np.float32(i.tau)),
-            float(np.float32(i.lambda_)), sim.tables())
-    it = (np.arange(10_000, dtype=np.uint64) * 7919 + 12345).astype(np.uint32)
+    args, state, V, desc = central_slab(workload, nx)
+    it = (np.arange(max_frames + 1, dtype=np.uint64) * 7919 + 12345).astype(np.uint32)
     oracle.ref_run(*args, state, it[:1], mode=1, threads=threads)  # warm-up
     t0 = time.perf_counter()
-    n = 0
-    while time.perf_counter() - t0 < budget_s and n < len(it) - 1:
-        oracle.ref_run(*args, state, it[1 + n:2 + n], mode=1, threads=threads)
-        n += 1
+    n, chunk = 0, 1
+    while time.perf_counter() - t0 < budget_s and n + chunk <= max_frames:
+        oracle.ref_run(*args, state, it[1 + n:1 + n + chunk], mode=1, threads=threads)
+        n += chunk
+        if time.perf_counter() - t0 < budget_s / 20:
+            chunk = min(chunk * 2, 1000)
     dt = time.perf_counter() - t0
-    V = int(np.prod(i.res))
-    return V * n / dt, f"{n} reference-semantics frames of the {nx}x256x256 x-slab through the cell centre " \
-                       f"(membrane, cytoplasm, nucleus; {V} voxels, same particle density)"
+    return V * n / dt, f"{n} reference-semantics frames of {desc}"
+
+
+CPU_SLAB = 8  # planes of the 256^3 cell in the CPU samples (cpu_baseline and the reference arm)
 
 
 def reference_arm(args, rank, world):
-    """The reference's algorithm on the host cores (the oracle's port of the
-    WGSL shaders: the reference itself needs Vulkan and a Rust toolchain)."""
+    """The reference's algorithm on the host cores: the oracle's restatement of the WGSL shaders
+    (the reference itself needs Vulkan and a Rust toolchain), on the same central slab of the 256^3
+    cell as cpu_baseline.  The slab is cut from the lattice the product library's host model
+    builder makes (outside the timed region); the timed loop runs the oracle alone."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
@@ -174,57 +219,57 @@ def reference_arm(args, rank, world):
     from cell_simulation_gb300 import configs
 
     oracle.build()
-    nx = 4
-    w = configs.c3_multi_region(res=(nx, 256, 256), total_particles=int(1_000_000 * nx / 256))
-    sim = w.sim
-    i = sim.info()
-    s, o, c = sim.get_lattice()
-    st = c.reshape(-1, i.n_species + 1).sum(0).astype(np.int32)
-    state = oracle.RefState(s, o, c, st)
-    a = (tuple(i.res), i.max_particles_site, i.n_regions, i.n_species, i.n_reactions, float(np.float32(i.tau)),
-         float(np.float32(i.lambda_)), sim.tables())
+    a, state, V, desc = central_slab(configs.c3_multi_region(), CPU_SLAB)
     n_total = args.warmup + args.steps
     it = (np.arange(n_total, dtype=np.uint64) * 7919 + 12345).astype(np.uint32)
     oracle.ref_run(*a, state, it[:args.warmup], mode=1, threads=threads)
     t0 = time.perf_counter()
     oracle.ref_run(*a, state, it[args.warmup:], mode=1, threads=threads)
     dt = time.perf_counter() - t0
-    V = int(np.prod(i.res))
     value = V * args.steps / dt
-    sample = (f"each step: one reference-semantics frame of the {nx}x256x256 x-slab through the centre of the "
-              f"256^3 multi-region cell ({V} voxels, same particle density)")
+    sample = f"each step: one reference-semantics frame of {desc}"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": "c3_multi_region_256x256x256_K16 (x-slab sample)", "rng": "reference PCG",
-                       "threads": threads},
+            "config": {"workload": f"c3_multi_region_256x256x256_K16 ({CPU_SLAB}-plane central x-slab)",
+                       "rng": "reference PCG", "threads": threads},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 def describe_variant(i):
-    from cell_simulation_gb300 import tiling_kinds, tiling_variants
+    from cell_simulation_gb300 import tiling_kinds, tiling_launches, tiling_variants
     k, ty, tz, nt = tiling_variants()[i]
     kind, bx = tiling_kinds()[i]
     if kind == 1:
         return {"index": i, "kind": "brick", "slots": k, "brick": [bx, ty, tz], "threads": nt}
     if kind == 2:
-        from cell_simulation_gb300 import tiling_launches
         return {"index": i, "kind": "stream", "slots": k, "words_per_group": 32, "threads": nt,
                 "passes_per_frame": tiling_launches()[i]}
     return {"index": i, "kind": "tile", "slots": k, "tile": [ty, tz], "threads": nt}
 
 
 def launches_per_frame(i):
-    """Kernel launches per frame of variant i: a brick pass with bounded pools is
-    followed by the pass over its spilled bricks; the sweep stream is four passes,
-    or three where the Y and Z sweeps are one launch."""
+    """Kernel launches per frame of variant i once a run is under way: the sweep stream's passes
+    (three where the Y and Z sweeps are one launch, else four), a brick pass and the pass over its
+    spilled bricks, or one tile-pipeline launch."""
     from cell_simulation_gb300 import tiling_launches
     return tiling_launches()[i]
 
 
-def ensemble_numbers(device, steps_batched=200, steps_plain=20, variant=-1):
+def frame_kernels(desc):
+    """The kernels of one frame of a variant, as named in the committed ncu summaries."""
+    if desc["kind"] == "stream":
+        if desc["passes_per_frame"] == 3:
+            return ["sweep_pass_kernel<1>", "sweep_pass_kernel<5>", "sweep_ssa_kernel"]
+        return ["sweep_pass_kernel<1>", "sweep_pass_kernel<2>", "sweep_pass_kernel<3>", "sweep_ssa_kernel"]
+    return ["brick_step_kernel"] if desc["kind"] == "brick" else ["prod_step_kernel"]
+
+
+def ensemble_numbers(device, steps_batched=5000, steps_plain=200, variant=-1):
+    """The 512-replicate ensemble: batched (one launch per pass for all replicates) against plain
+    (one launch group per replicate), replicate-steps/s."""
     from cell_simulation_gb300 import Ensemble, configs
 
     tmpl = configs.c4_ensemble_template(K=8)
@@ -243,13 +288,69 @@ def ensemble_numbers(device, steps_batched=200, steps_plain=20, variant=-1):
     n = len(res)
     rb = n * steps_batched / (ms_b / 1e3)
     rp = n * steps_plain / (ms_p / 1e3)
+    peak, _ = measured_peaks()
     out = {"workload": f"c4_ensemble_{n}rep_L32-96_K8", "total_voxels": int(tot), "work_items": int(items),
            "replicate_steps_per_s_batched": rb, "replicate_steps_per_s_plain": rp,
            "voxel_steps_per_s_batched": tot * steps_batched / (ms_b / 1e3),
            "batched_over_plain": rb / rp, "steps_batched": steps_batched, "steps_plain": steps_plain,
+           "ms_per_step_batched": ms_b / steps_batched, "ms_per_step_plain": ms_p / steps_plain,
+           "roofline_frac_batched": tot * steps_batched / (ms_b / 1e3) * 17 / 1e9 / peak,
            "launches_per_frame_batched": per_frame, "launches_per_frame_plain": n * per_frame,
            "variant": describe_variant(variant)}
     ens.close()
+    return out
+
+
+def philox_leg(workload, device, steps, warmup=5, tune_frames=5):
+    """The production step of one workload (autotuned), timed with CUDA events."""
+    from cell_simulation_gb300 import PREC_MIXED, RNG_PHILOX
+    sim = workload.sim
+    info = sim.info()
+    V, K = int(info.n_voxels), info.max_particles_site
+    sim.prepare_for_gpu(RNG_PHILOX, device)
+    sim.set_precision(PREC_MIXED)
+    variant, _ = sim.autotune(tune_frames)
+    sim.step_philox(warmup, 7)
+    ms = sim.step_philox_timed(steps, 7)
+    sim.close()
+    peak, _ = measured_peaks()
+    rate = V * steps / (ms / 1e3)
+    return {"voxel_steps_per_s": rate, "ms_per_step": ms / steps, "steps": steps, "voxels": V,
+            "roofline_frac": rate * (2 * K + 1) / 1e9 / peak, "variant": describe_variant(variant)}
+
+
+def reference_rng_leg(workload, device, steps, warmup=3):
+    """The reference-RNG (bit-parity) CUDA path of one workload, timed with CUDA events."""
+    from cell_simulation_gb300 import RNG_REFERENCE
+    sim = workload.sim
+    V = int(sim.info().n_voxels)
+    sim.prepare_for_gpu(RNG_REFERENCE, device)
+    it = (np.arange(warmup + steps, dtype=np.uint64) * 7919 + 12345).astype(np.uint32)
+    sim.step(it[:warmup])
+    ms = sim.step_timed(it[warmup:])
+    sim.close()
+    return {"voxel_steps_per_s": V * steps / (ms / 1e3), "ms_per_step": ms / steps, "steps": steps, "voxels": V}
+
+
+def config_legs(device, cpu_budget, threads, with_cpu):
+    """Every named configuration other than the headline: GPU production and reference-RNG paths,
+    and the CPU restatement on a slab of the same lattice."""
+    from cell_simulation_gb300 import configs
+    out = {}
+    c1 = {"philox": philox_leg(configs.c1_plain_2d(), device, 10_000, tune_frames=20),
+          "reference_rng": reference_rng_leg(configs.c1_plain_2d(), device, 10_000)}
+    c2 = {"philox": philox_leg(configs.c2_single_cell(), device, 1000),
+          "reference_rng": reference_rng_leg(configs.c2_single_cell(), device, 100)}
+    c5 = {"philox": philox_leg(configs.c5_stiff(), device, 200),
+          "reference_rng": reference_rng_leg(configs.c5_stiff(), device, 50)}
+    if with_cpu:
+        for leg, w, nx in ((c1, configs.c1_plain_2d(), 64), (c2, configs.c2_single_cell(), 16),
+                           (c5, configs.c5_stiff(), 8)):
+            rate, sample = cpu_reference_rate(w, nx, cpu_budget, threads)
+            leg["cpu_reference_semantics"] = {"voxel_steps_per_s": rate, "cores": threads, "sample": sample}
+    out["c1_plain_64x64x1_K8"] = c1
+    out["c2_single_cell_128x128x128_K16"] = c2
+    out["c5_stiff_192x192x192_K16"] = c5
     return out
 
 
@@ -259,12 +360,15 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--no-extras", action="store_true", help="skip ensemble, reference-RNG, e2e and CPU legs")
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-extras", action="store_true", help="skip the ensemble, other configurations, "
+                                                             "reference-RNG, e2e and CPU legs")
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--variant", type=int, default=-1, help="step variant index (default: autotuned)")
     ap.add_argument("--ensemble-only", action="store_true",
                     help="only the 512-replicate ensemble leg: --steps batched frames, a tenth as many plain ones "
                          "(for profiling; prints that leg's numbers)")
+    ap.add_argument("--refrng-only", action="store_true",
+                    help="only the reference-RNG CUDA path on the 256^3 cell: --steps frames (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = env_rank()
@@ -274,10 +378,13 @@ def main():
 
     import __graft_entry__
     __graft_entry__.build()
+    from cell_simulation_gb300 import PREC_MIXED, RNG_PHILOX, configs
     if args.ensemble_only:
         print(json.dumps(ensemble_numbers(local, args.steps, max(1, args.steps // 10), args.variant)), flush=True)
         return
-    from cell_simulation_gb300 import PREC_MIXED, RNG_PHILOX, RNG_REFERENCE, configs
+    if args.refrng_only:
+        print(json.dumps(reference_rng_leg(configs.c3_multi_region(), local, args.steps, args.warmup)), flush=True)
+        return
 
     dist = Dist(world)
     device = local
@@ -297,26 +404,33 @@ def main():
         sim.set_tiling(variant)
     else:
         variant, _ = sim.autotune(10)  # state restored: the timed frames start from the same lattice
-    sim.step_philox(args.warmup, seed)
-    sim.synchronize()
     clocks = ClockSampler(device)
     clocks.start()
+    sim.step_philox(args.warmup, seed)
+    sim.synchronize()
     dist.barrier()
+    t_region = time.perf_counter()
     ms = sim.step_philox_timed(args.steps, seed)
     dist.barrier()
-    clk = clocks.stop()
+    # keep the GPU busy (untimed frames) until the clock window holds three samples
+    t_hold = time.perf_counter()
+    while clocks.alive() and clocks.rows_since(t_region) < 3 and time.perf_counter() - t_hold < 5.0:
+        sim.step_philox(200, seed)
+        sim.synchronize()
+    clk = clocks.stop(t_region, time.perf_counter())
     ms_max = dist.max(ms)
     value = world * V * args.steps / (ms_max / 1e3)
-    per_launch_s = ms / 1e3 / args.steps
+    frame_s = ms / 1e3 / args.steps
     peak, peak_kind = measured_peaks()
     alg_bytes = V * (2 * K + 1)
-    achieved = alg_bytes / per_launch_s / 1e9
+    achieved = alg_bytes / frame_s / 1e9
     desc = describe_variant(variant)
-    kernel = {"brick": "brick_step_kernel", "stream": "sweep_pass_kernel"}.get(desc["kind"], "prod_step_kernel")
-    if desc["kind"] == "stream":
-        # the frame's longest launch: pass 3, or the fused Y and Z sweeps (template pass 5)
-        kernel += "<5>" if desc["passes_per_frame"] == 3 else "<3>"
-    traffic = profiled_traffic(kernel, w.name)
+    kernels = frame_kernels(desc)
+    longest = "sweep_pass_kernel<5>" if "sweep_pass_kernel<5>" in kernels else (
+        "sweep_pass_kernel<3>" if "sweep_pass_kernel<3>" in kernels else kernels[0])
+    traffic = profiled_traffic(longest, w.name)
+    per_kernel = {k: profiled_traffic(k, w.name) for k in kernels}
+    frame_dram = sum(per_kernel.values()) if all(v is not None for v in per_kernel.values()) else None
     diag = sim.diagnostics()
 
     # end to end through the C ABI: every frame one step call (its frame number
@@ -332,24 +446,17 @@ def main():
     e2e = {"value": world * V * n_e2e / dist.max(e2e_s), "unit": UNIT, "h2d_bytes_per_step": 4,
            "d2h_bytes_per_step": S1 * 8, "steps": n_e2e,
            "setup_s": {"host_model_build": t_build, "upload_prepare_for_gpu": t_upload}}
+    sim.close()
 
     extras = {}
+    threads = os.cpu_count() or 1
     if not args.no_extras and rank == 0:
         extras["ensemble"] = ensemble_numbers(device)
-        # reference-RNG (bit-parity) CUDA path on the same lattice
-        w2 = configs.c3_multi_region()
-        s2 = w2.sim
-        s2.prepare_for_gpu(RNG_REFERENCE, device)
-        it = (np.arange(200, dtype=np.uint64) * 7919 + 12345).astype(np.uint32)
-        s2.step(it[:3])
-        ms_ref = s2.step_timed(it[3:103])
-        extras["reference_rng_path"] = {"voxel_steps_per_s": V * 100 / (ms_ref / 1e3), "launches_per_frame": 5,
-                                        "steps": 100}
-        s2.close()
+        extras["reference_rng_path"] = reference_rng_leg(configs.c3_multi_region(), device, 100)
+        extras["configs"] = config_legs(device, min(args.cpu_budget, 4.0), threads, world == 1)
     cpu = None
     if not args.no_extras and rank == 0 and world == 1:
-        threads = os.cpu_count() or 1
-        rate, sample = cpu_reference_rate(args.cpu_budget, threads)
+        rate, sample = cpu_reference_rate(configs.c3_multi_region(), CPU_SLAB, args.cpu_budget, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
     dist.close()
     if rank != 0:
@@ -361,11 +468,15 @@ def main():
         "config": {"workload": w.name, "voxels": V, "slots_per_voxel": K, "species": S1 - 1,
                    "reactions": int(info.n_reactions), "rng": "philox4x32-10", "precision": "fp32 propensities, fp64 clock",
                    "l2": "inputs larger than L2 (2 x 256 MiB lattice buffers)", "parallelism": f"replicas x{world}",
-                   "variant": describe_variant(variant)},
+                   "variant": desc},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": alg_bytes, "kernel": kernel,
-                     "achieved_over": "frame time (every launch of the frame)"},
+                     "algorithmic_bytes_per_launch": alg_bytes, "kernel": longest,
+                     "achieved_over": "frame time (every launch of the frame)",
+                     "frame_dram_bytes": frame_dram, "frame_dram_bytes_per_kernel": per_kernel,
+                     "dram_frac": (frame_dram / frame_s / 1e9 / peak) if frame_dram else None,
+                     "dram_frac_note": "the frame's profiled DRAM bytes (every launch, one cold-cache ncu capture) "
+                                       "over the measured frame time, against the measured copy bandwidth"},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": args.steps * launches_per_frame(variant),

@@ -667,8 +667,17 @@ static void set_cfg(DeviceProd* d, int idx) {
         throw Error(CS_ERR_INVALID_ARG, "fused sweep-stream variant needs rows of at most 32 bitmap words (Z <= 1024)");
     set_attrs(d, cfg);
     if (cfg.spill >= 0) set_attrs(d, all_cfgs()[cfg.spill]);
+    // build_items reads cfg_index; when it refuses the new configuration (a lattice too large for
+    // its work lists), the previous configuration and its lists are restored
+    const int prev = d->cfg_index;
     d->cfg_index = idx;
-    build_items(d);
+    try {
+        build_items(d);
+    } catch (...) {
+        d->cfg_index = prev;
+        if (prev >= 0) build_items(d);
+        throw;
+    }
     if (d->graph) {
         cudaGraphExecDestroy(d->graph);
         d->graph = nullptr;
@@ -1408,7 +1417,8 @@ namespace cellsim {
 // the current state and the state is restored afterwards, so tuning does not
 // advance or change the simulation (every configuration computes the same
 // frame anyway).  Choices are cached per (K, species, reactions, regions,
-// lattice shapes, device) for the life of the process.
+// zero-order reactions or reservoirs present, lattice shapes, device) for the
+// life of the process.
 int prod_autotune(DeviceProd* d, uint32_t frames, uint64_t frame0, bool batched, float* best_ms) {
     DeviceGuard g(d->device);
     static std::mutex mu;
@@ -1416,7 +1426,9 @@ int prod_autotune(DeviceProd* d, uint32_t frames, uint64_t frame0, bool batched,
     cudaDeviceProp prop{};
     CS_CUDA(cudaGetDeviceProperties(&prop, d->device));
     std::string key = std::string(prop.name) + "|" + std::to_string(d->K) + "," + std::to_string(d->S1) + "," +
-                      std::to_string(d->R) + "," + std::to_string(d->NC) + "," + std::to_string(batched ? 1 : 0);
+                      std::to_string(d->R) + "," + std::to_string(d->NC) + "," + std::to_string(batched ? 1 : 0) +
+                      // reservoirs and zero-order reactions make the brick pass step every interior voxel
+                      "," + std::to_string(d->T.n_zero_order != 0u ? 1 : 0) + std::to_string(d->reservoir.n ? 1 : 0);
     for (const RepDesc& r : d->h_reps) key += "|" + std::to_string(r.X) + "x" + std::to_string(r.Y) + "x" + std::to_string(r.Z);
     {
         std::lock_guard<std::mutex> lk(mu);

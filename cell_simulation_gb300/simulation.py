@@ -320,10 +320,9 @@ class Simulation:
 
     def counts(self) -> np.ndarray:
         """Species counts (StatisticsGroup buffer 0, src/statistics.rs:11-69)."""
-        s1 = getattr(self, "_s1", None) or self.info().n_species + 1
-        out = np.zeros(s1, np.int64)
+        # the species count is read every call: cs_set_tables may change it between preparations
+        out = np.zeros(self.info().n_species + 1, np.int64)
         N.check(self._lib.cs_get_counts(self._h, N.ptr(out, C.c_int64)))
-        self._s1 = s1  # counts exist once the model is prepared, and it no longer changes then
         return out
 
     def diagnostics(self, n: int = 8) -> np.ndarray:

@@ -14,6 +14,14 @@ def itime_schedule(n, seed=987654321, stride=7919):
     return ((np.uint64(seed) + np.uint64(stride) * np.arange(n, dtype=np.uint64)) & np.uint64(0xFFFFFFFF)).astype(np.uint32)
 
 
+def compact_slots(slots_u32, K):
+    """Reference-layout slots (u32, V*K) as the production path's compacted u8 voxels: each voxel's
+    particles moved to its first slots in slot order."""
+    s = np.asarray(slots_u32).reshape(-1, K).astype(np.uint8)
+    order = np.argsort(s == 0, axis=1, kind="stable")
+    return np.take_along_axis(s, order, axis=1).reshape(-1)
+
+
 def ref_state(sim: Simulation):
     i = sim.info()
     s, o, c = sim.get_lattice()

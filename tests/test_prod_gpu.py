@@ -335,3 +335,25 @@ def test_autotune_keeps_state_and_results(orc):
     got_s, _, _ = sim.get_lattice()
     assert np.array_equal(got_s.astype(np.uint8), want_s)
     assert np.array_equal(sim.counts(), want_c)
+
+
+def test_counts_follow_a_change_of_species_count():
+    """cs_set_tables may raise the species count after a preparation: the next preparation's
+    counts have the new length and equal the new lattice's particles plus reservoir species."""
+    sim = multi_region_model(res=(12, 10, 14), K=8)
+    sim.prepare_for_gpu(RNG_PHILOX, 0)
+    assert len(sim.counts()) == 5
+    other = multi_region_model(res=(12, 10, 14), K=8, reservoir=True)
+    t, i = other.tables(), other.info()
+    sim.set_tables(i.n_regions, i.n_species, i.n_reactions, t.regions, t.diffusion, t.stoich, t.reactants, t.rates,
+                   t.reservoir)
+    slots = other.get_lattice()[0]
+    sim.set_lattice(slots)
+    sim.prepare_for_gpu(RNG_PHILOX, 0)
+    want = np.bincount(slots, minlength=i.n_species + 1).astype(np.int64)
+    want[0] = 0
+    for q in t.reservoir[t.reservoir > 0]:
+        want[q] += 1
+    got = sim.counts()
+    assert len(got) == i.n_species + 1 == 6
+    assert np.array_equal(got, want)

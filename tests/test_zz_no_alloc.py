@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from cell_simulation_gb300 import RNG_REFERENCE, CellsimError, native
-from tests.helpers import itime_schedule, multi_region_model
+from tests.helpers import crowded_model, itime_schedule, multi_region_model
 
 pytestmark = pytest.mark.gpu
 
@@ -29,9 +29,17 @@ def _host(t, dtype):
     return t.cpu().numpy().view(dtype)
 
 
-def test_noalloc_frames_match_cs_step(lib):
+@pytest.mark.parametrize("model", ["multi_region", "crowded"])
+def test_noalloc_frames_match_cs_step(lib, model):
+    """Two frames through each entry point.  On the crowded lattice the first frame has moves
+    that compete for room, so it takes the serial-resolution branch, which reads the contention
+    flag the frame set in the library's shared scratch; the second frame takes the gather
+    branch and must find that flag cleared."""
     torch = pytest.importorskip("torch")
-    sim = multi_region_model(res=(12, 10, 14), K=8, reservoir=True)
+    if model == "crowded":
+        sim = crowded_model()
+    else:
+        sim = multi_region_model(res=(12, 10, 14), K=8, reservoir=True)
     info = sim.info()
     K, S1, R, NR = info.max_particles_site, info.n_species + 1, info.n_reactions, info.n_regions
     V = int(info.n_voxels)
@@ -79,6 +87,8 @@ def test_noalloc_frames_match_cs_step(lib):
         assert np.array_equal(_host(dst[2], np.int32), wc), f"concentrations differ after frame {i + 1}"
         assert np.array_equal(_host(counts, np.int32).astype(np.int64), sim.counts()), f"counts differ after frame {i + 1}"
         assert np.array_equal(_host(diag, np.uint32), sim.diagnostics()), f"diagnostics differ after frame {i + 1}"
+        if model == "crowded":
+            assert _host(diag, np.uint32)[2] == 1  # frame 1 resolved serially, frame 2 by the gather
 
 
 def test_noalloc_rejects_oversized_lattice(lib):
