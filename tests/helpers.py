@@ -101,3 +101,29 @@ def patchy_model(res=(19, 21, 70), K=16, seed=11, dense=3200, sparse=150, D=1e-1
     sim.add_reaction(["C"], ["A", "B"], 60.0)
     sim.add_reaction(["A"], ["B"], 20.0)
     return sim
+
+
+def network_template(sim: Simulation, res=(24, 24, 24), K=16, D=1e-12) -> Simulation:
+    """A one-region ensemble template carrying sim's species and reactions (read back from its
+    reference-layout tables) with diffusion D for every species: the well-mixed form of a
+    configuration's reaction network."""
+    t, i = sim.tables(), sim.info()
+    S1, R = i.n_species + 1, i.n_reactions
+    names = sim.particle_names
+    tmpl = Simulation(LatticeParams([r * LAM for r in res], list(res), configs.stable_tau(D), LAM, K))
+    tmpl.set_diffusion_rate("background", D)
+    tmpl.prepare_regions()
+    for n in names[1:]:
+        tmpl.add_particle_count(n, "background", 0, True, False)
+    tmpl.set_diffusion_rate("background", D)
+    re = t.reactants.reshape(R + 1, 3)
+    st = t.stoich.reshape(R + 1, S1)
+    for r in range(1, R + 1):
+        rs = [int(s) for s in re[r] if s]
+        change = st[r].astype(np.int64).copy()
+        prod = []
+        have = np.bincount(np.array(rs, np.int64), minlength=S1) if rs else np.zeros(S1, np.int64)
+        for s in range(1, S1):
+            prod += [s] * int(have[s] + change[s])
+        tmpl.add_reaction([names[s] for s in rs], [names[s] for s in prod], float(t.rates[r]))
+    return tmpl
