@@ -5,23 +5,51 @@
 // in linear index order, slots in index order (the reference's own GPU order
 // is nondeterministic because of its spin locks and CAS slot insertion).
 //
-// Per frame, five launches on the handle's stream:
-//   1. ref_directions  one thread per voxel: for every occupied slot, the
-//      direction drawn from PCG(itime + x%y + z + slot index) against the
-//      cumulative move probabilities (rdme.wgsl:138-226); 7 = no particle.
-//   2. ref_gather      one thread per destination voxel: arrivals from the -x,
-//      -y, -z neighbours, own departures, arrivals from the +z, +y, +x
-//      neighbours, each arrival into the lowest free slot.  This equals the
-//      serial order when no arrival can be rejected; a voxel for which
-//      max(occupancy, nonzero slots) + arrivals > K raises `contended`.
-//   3. ref_serial_copy / 4. ref_serial (one thread) run only when `contended`
-//      is set and redo the diffusion in serial order with the capacity rule.
-//   5. ref_cme         one thread per voxel: one-event reaction test, slot
-//      rewrite with rollback, stable compaction (final_stage.wgsl:25-33),
-//      species-count deltas reduced per block then added atomically.
-// The lattice, occupancy and concentration buffers ping-pong between frames,
-// which replaces the reference's dest->src buffer copies
-// (src/simulation.rs:134-144).
+// Directions depend only on the source lattice, so each destination voxel can
+// assemble its slots on its own, in serial order: arrivals from the -x, -y, -z
+// neighbours, its own departures, arrivals from the +z, +y, +x neighbours,
+// each arrival into the lowest free slot.  This equals the serial order when
+// no arrival can be rejected; when max(occupancy, nonzero slots) + arrivals >
+// K for some voxel (`contended`), a one-thread kernel redoes the frame's
+// diffusion in serial order with the capacity rule.
+//
+// cs_step runs the sparse form on single (in-place) state buffers.  Each pass
+// is a grid-stride loop over a voxel list compacted from a bitmap (one atomic
+// per warp, word order kept within a warp), so every lane has a voxel however
+// sparse the lattice.  Six launches per frame:
+//   ref_sp_list_act     the act list: voxels holding a particle, a non-zero
+//                       occupancy or a non-zero species count.
+//   ref_sp_directions   over the act list: the direction of every particle
+//                       from PCG(itime + x%y + z + slot index)
+//                       (rdme.wgsl:138-226); voxels with a departure store
+//                       their directions and a snapshot of their slots and set
+//                       their `dep` bit; every departure counts one arrival at
+//                       its destination, sets both voxels' `touch` bits and
+//                       raises `contended` when the destination could overflow.
+//   ref_sp_list_touch   the touch list and the union of act and touch.
+//   ref_sp_gather       (not contended) over the touch list: the gather above,
+//                       in place, with the species of arriving particles read
+//                       from their sources' snapshots and the concentrations
+//                       updated in place.
+//   ref_sp_serial       (contended) one thread: the serial diffusion, in place.
+//   ref_sp_cme          over the union list: one-event reaction test, rewrite
+//                       with rollback, stable compaction (final_stage.wgsl:25-33),
+//                       species-count deltas reduced per block; the next
+//                       frame's act bitmap.
+// A voxel on neither list holds no particle and no species count, its slots
+// are compacted and its conc[v][0] is already 1, so the reaction pass leaves
+// it unchanged unless its first uniform is 0: r1 = UniformFloat(PCG(itime +
+// x*y + z)) is 0 exactly when the seed is 0 (PCG and the xorshift are
+// bijections that fix 0), and r1 <= 1 - exp(-0 * tau) = 0 then fires the
+// selection.  Pass 1 puts those voxels (x*y + z = -itime mod 2^32) on the
+// touch list.  The first frame after an upload, and every frame of a model
+// with a reaction without reactants (non-zero propensity in every voxel), run
+// the reaction pass over every voxel.
+//
+// The allocation-free entry point (cs_ref_frame_noalloc) runs the dense form
+// of the same frame on caller-owned ping-pong buffers: five launches of one
+// thread per voxel (ref_directions, ref_gather, ref_serial_copy, ref_serial,
+// ref_cme), the per-voxel operations shared with the sparse form.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,19 +80,25 @@ struct RefParams {
     const uint8_t* reservoir;  // [V]
 };
 
+// State of a reference-RNG handle: one in-place copy of the lattice (slots,
+// occupancy, concentrations) and the bitmaps and scratch of the sparse form.
 struct DeviceRef {
     int device = 0;
     cudaStream_t stream = nullptr;
     RefParams p{};
-    DevBuf<uint8_t> slots[2];
-    DevBuf<uint32_t> occ[2];
-    DevBuf<int32_t> conc[2];
-    DevBuf<uint8_t> regions, reservoir, dirs;
+    DevBuf<uint8_t> slots;
+    DevBuf<uint32_t> occ;
+    DevBuf<int32_t> conc;
+    DevBuf<uint8_t> regions, reservoir, dirs, snap;
     DevBuf<float> P, rates;
     DevBuf<int32_t> stoich, stat;
     DevBuf<uint32_t> reactants, diag, flag, itimes;
+    DevBuf<uint32_t> act_bm[2], touch_bm, dep_bm, act_list, touch_list, union_list, cnt, arrivals;
     DevBuf<int32_t> sample_ring;
-    int cur = 0;
+    uint32_t par = 0;         // parity of the next frame's lists
+    int grid = 1;             // blocks of the sparse passes (grid-stride loops)
+    bool dense_next = true;   // the next reaction pass visits every voxel (first frame after an upload)
+    bool dense_always = false;  // a reaction without reactants: every voxel may fire in every frame
     ~DeviceRef() {
         if (stream) cudaStreamDestroy(stream);
     }
@@ -244,93 +278,100 @@ __global__ void ref_serial(RefParams p, const uint32_t* contended, const uint8_t
     diag[DIAG_SLOW_STEPS] += 1u;
 }
 
-// cme.wgsl:26-120 followed by final_stage.wgsl:25-33.
-__global__ void ref_cme(RefParams p, uint8_t* __restrict__ dst, uint32_t* __restrict__ occD, int32_t* __restrict__ concD,
-                        const uint32_t* __restrict__ itimes, uint32_t step, int32_t* stat, uint32_t* diag) {
-    extern __shared__ int32_t s_delta[];  // [S1] + 2 counters
-    for (uint32_t s = threadIdx.x; s < p.S1 + 2; s += blockDim.x) s_delta[s] = 0;
-    __syncthreads();
-    uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v < p.V) {
-        const uint32_t K = p.K, S1 = p.S1, R = p.R;
-        const uint32_t S = S1 - 1;
-        uint32_t z = (uint32_t)(v % p.Z);
-        uint32_t y = (uint32_t)((v / p.Z) % p.Y);
-        uint32_t x = (uint32_t)(v / p.YZ);
-        int32_t* c = concD + v * S1;
-        uint8_t* sl = dst + v * K;
-        c[0] = 1;
-        float total = 0.0f;
-        for (uint32_t r = 1; r <= R; r++) {
-            uint32_t prod = (uint32_t)c[p.reactants[r * 3]] * (uint32_t)c[p.reactants[r * 3 + 1]] *
-                            (uint32_t)c[p.reactants[r * 3 + 2]];
-            total = __fadd_rn(total, __fmul_rn(p.rates[r], __int2float_rn((int32_t)prod)));
+// cme.wgsl:26-120 followed by final_stage.wgsl:25-33 for voxel v, in place:
+// conc[v][0] = 1, the one-event test, the species-major rewrite with rollback
+// and the stable compaction.  s_delta[0..S1) collects species deltas,
+// s_delta[S1] fired voxels and s_delta[S1 + 1] rollbacks (block-shared).
+// Coordinates of voxel v (V * K < 2^32 on this path: the reference indexes
+// slots with u32, functions.wgsl:42-51).
+__device__ __forceinline__ void ref_coords(const RefParams& p, uint32_t v, uint32_t& x, uint32_t& y, uint32_t& z) {
+    const uint32_t t = v / p.Z;
+    z = v - t * p.Z;
+    x = t / p.Y;
+    y = t - x * p.Y;
+}
+
+__device__ void ref_cme_voxel(const RefParams& p, uint64_t v, uint8_t* __restrict__ slots, uint32_t* __restrict__ occ,
+                              int32_t* __restrict__ conc, uint32_t itime, int32_t* s_delta) {
+    const uint32_t K = p.K, S1 = p.S1, R = p.R;
+    const uint32_t S = S1 - 1;
+    uint32_t x, y, z;
+    ref_coords(p, (uint32_t)v, x, y, z);
+    int32_t* c = conc + v * S1;
+    uint8_t* sl = slots + v * K;
+    c[0] = 1;
+    float total = 0.0f;
+    for (uint32_t r = 1; r <= R; r++) {
+        uint32_t prod = (uint32_t)c[p.reactants[r * 3]] * (uint32_t)c[p.reactants[r * 3 + 1]] *
+                        (uint32_t)c[p.reactants[r * 3 + 2]];
+        total = __fadd_rn(total, __fmul_rn(p.rates[r], __int2float_rn((int32_t)prod)));
+    }
+    uint8_t snap[16];
+    for (uint32_t s = 0; s < K; s++) snap[s] = sl[s];
+    uint32_t state = d_pcg(itime + x * y + z);
+    float r1 = d_uniform_float(state);
+    float fire_p = __fsub_rn(1.0f, d_expf(__fmul_rn(-total, p.tau)));
+    if (r1 <= fire_p) {
+        atomicAdd(&s_delta[S1], 1);
+        float r2 = d_uniform_float(state + 1u);
+        // selection over cum[i] = cum[i-1] + a_i, normalised for i < R (cme.wgsl:50-52,70-73)
+        uint32_t i = 0;
+        float run = 0.0f;
+        while (i < R) {
+            if (!(r2 > __fdiv_rn(run, total))) break;
+            i++;
+            uint32_t prod = (uint32_t)c[p.reactants[i * 3]] * (uint32_t)c[p.reactants[i * 3 + 1]] *
+                            (uint32_t)c[p.reactants[i * 3 + 2]];
+            run = __fadd_rn(run, __fmul_rn(p.rates[i], __int2float_rn((int32_t)prod)));
         }
-        uint8_t snap[16];
-        for (uint32_t s = 0; s < K; s++) snap[s] = sl[s];
-        uint32_t itime = itimes[step];
-        uint32_t state = d_pcg(itime + x * y + z);
-        float r1 = d_uniform_float(state);
-        float fire_p = __fsub_rn(1.0f, d_expf(__fmul_rn(-total, p.tau)));
-        if (r1 <= fire_p) {
-            atomicAdd(&s_delta[S1], 1);
-            float r2 = d_uniform_float(state + 1u);
-            // selection over cum[i] = cum[i-1] + a_i, normalised for i < R (cme.wgsl:50-52,70-73)
-            uint32_t i = 0;
-            float run = 0.0f;
-            while (i < R) {
-                if (!(r2 > __fdiv_rn(run, total))) break;
-                i++;
-                uint32_t prod = (uint32_t)c[p.reactants[i * 3]] * (uint32_t)c[p.reactants[i * 3 + 1]] *
-                                (uint32_t)c[p.reactants[i * 3 + 2]];
-                run = __fadd_rn(run, __fmul_rn(p.rates[i], __int2float_rn((int32_t)prod)));
-            }
-            const int32_t* st = p.stoich + (size_t)i * S1;
-            uint32_t j = 0;
-            int32_t new_occ = (int32_t)occD[v];
-            uint64_t ri = v * K;  // reservoirs[idx_lattice], cme.wgsl:80
-            uint32_t resv = (ri < p.V) ? p.reservoir[ri] : 0u;
-            bool rolled = false;
-            for (uint32_t s = 1; s <= S && !rolled; s++) {
-                if (resv == s) continue;
-                int32_t d = st[s];
-                c[s] = (int32_t)((uint32_t)c[s] + (uint32_t)d);
-                new_occ = (int32_t)((uint32_t)new_occ + (uint32_t)d);
-                if (d) atomicAdd(&s_delta[s], d);
-                int32_t cc = c[s];
-                while (cc > 0) {
-                    sl[j] = (uint8_t)s;
-                    cc--;
-                    j++;
-                    if (j >= K) {
-                        for (uint32_t k = 0; k < K; k++) sl[k] = snap[k];
-                        for (uint32_t s2 = 1; s2 <= s; s2++) {
-                            int32_t d2 = st[s2];
-                            c[s2] = (int32_t)((uint32_t)c[s2] - (uint32_t)d2);
-                            if (d2) atomicAdd(&s_delta[s2], -d2);
-                        }
-                        atomicAdd(&s_delta[S1 + 1], 1);
-                        rolled = true;
-                        break;
+        const int32_t* st = p.stoich + (size_t)i * S1;
+        uint32_t j = 0;
+        int32_t new_occ = (int32_t)occ[v];
+        uint64_t ri = v * K;  // reservoirs[idx_lattice], cme.wgsl:80
+        uint32_t resv = (ri < p.V) ? p.reservoir[ri] : 0u;
+        bool rolled = false;
+        for (uint32_t s = 1; s <= S && !rolled; s++) {
+            if (resv == s) continue;
+            int32_t d = st[s];
+            c[s] = (int32_t)((uint32_t)c[s] + (uint32_t)d);
+            new_occ = (int32_t)((uint32_t)new_occ + (uint32_t)d);
+            if (d) atomicAdd(&s_delta[s], d);
+            int32_t cc = c[s];
+            while (cc > 0) {
+                sl[j] = (uint8_t)s;
+                cc--;
+                j++;
+                if (j >= K) {
+                    for (uint32_t k = 0; k < K; k++) sl[k] = snap[k];
+                    for (uint32_t s2 = 1; s2 <= s; s2++) {
+                        int32_t d2 = st[s2];
+                        c[s2] = (int32_t)((uint32_t)c[s2] - (uint32_t)d2);
+                        if (d2) atomicAdd(&s_delta[s2], -d2);
                     }
+                    atomicAdd(&s_delta[S1 + 1], 1);
+                    rolled = true;
+                    break;
                 }
             }
-            if (!rolled) {
-                occD[v] = (uint32_t)new_occ;
-                while (j < K) sl[j++] = 0;
-            }
         }
-        uint32_t jj = 0;
-        for (uint32_t s = 0; s < K; s++) {
-            uint8_t q = sl[s];
-            if (q != 0) {
-                sl[s] = sl[jj];
-                sl[jj] = q;
-                jj++;
-            }
+        if (!rolled) {
+            occ[v] = (uint32_t)new_occ;
+            while (j < K) sl[j++] = 0;
         }
     }
-    __syncthreads();
+    uint32_t jj = 0;
+    for (uint32_t s = 0; s < K; s++) {
+        uint8_t q = sl[s];
+        if (q != 0) {
+            sl[s] = sl[jj];
+            sl[jj] = q;
+            jj++;
+        }
+    }
+}
+
+// Adds a block's species deltas, fired voxels and rollbacks to the totals.
+__device__ __forceinline__ void ref_flush_block(const RefParams& p, const int32_t* s_delta, int32_t* stat, uint32_t* diag) {
     for (uint32_t s = threadIdx.x; s < p.S1; s += blockDim.x)
         if (s_delta[s]) atomicAdd(stat + s, s_delta[s]);
     if (threadIdx.x == 0) {
@@ -339,7 +380,360 @@ __global__ void ref_cme(RefParams p, uint8_t* __restrict__ dst, uint32_t* __rest
     }
 }
 
+// Dense reaction pass: one thread per voxel.
+__global__ void ref_cme(RefParams p, uint8_t* __restrict__ dst, uint32_t* __restrict__ occD, int32_t* __restrict__ concD,
+                        const uint32_t* __restrict__ itimes, uint32_t step, int32_t* stat, uint32_t* diag) {
+    extern __shared__ int32_t s_delta[];  // [S1] + 2 counters
+    for (uint32_t s = threadIdx.x; s < p.S1 + 2; s += blockDim.x) s_delta[s] = 0;
+    __syncthreads();
+    uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < p.V) ref_cme_voxel(p, v, dst, occD, concD, itimes[step], s_delta);
+    __syncthreads();
+    ref_flush_block(p, s_delta, stat, diag);
+}
+
+// ------------------------------------------------------------------ sparse form
+
+// Bitmaps over the linear voxel index (word i holds voxels 32i .. 32i+31) and
+// the voxel lists compacted from them, for a frame of parity c:
+//   act bitmap c   voxels that hold a particle, a non-zero occupancy or a
+//                  non-zero species count (s >= 1); the reaction pass sets
+//                  act bitmap c ^ 1 for the next frame
+//   touch bitmap   voxels that gain or lose particles this frame, or whose
+//                  reaction seed is 0
+//   dep bitmap     voxels with a departure this frame
+//   act list       act bitmap c, compacted at the start of the frame
+//   touch list     the touch bitmap, compacted after the directions pass
+//   union list     act bitmap c | touch bitmap, compacted with it
+// cnt[0..2]: entries of the act, touch and union lists.
+struct RefSparse {
+    uint32_t* act_bm[2];
+    uint32_t* touch_bm;
+    uint32_t* dep_bm;
+    uint32_t* act_list;
+    uint32_t* touch_list;
+    uint32_t* union_list;
+    uint32_t* cnt;       // [3]
+    uint32_t* arrivals;  // [V] particles moving into the voxel this frame (zero between frames)
+    uint8_t* dirs;       // [V*K] direction codes of a voxel with a departure (7 = stays)
+    uint8_t* snap;       // [V*K] slots of a voxel with a departure, as the frame started
+    uint32_t W;          // bitmap words
+    uint32_t c;          // frame parity
+};
+
+__device__ __forceinline__ void ref_load_k(const uint8_t* __restrict__ src, uint32_t K, uint8_t* out) {
+    if (K == 16) {
+        const uint4 t = *reinterpret_cast<const uint4*>(src);
+        const uint32_t w[4] = {t.x, t.y, t.z, t.w};
+        for (int i = 0; i < 16; i++) out[i] = (uint8_t)(w[i >> 2] >> (8 * (i & 3)));
+    } else if (K == 8) {
+        const uint2 t = *reinterpret_cast<const uint2*>(src);
+        const uint32_t w[2] = {t.x, t.y};
+        for (int i = 0; i < 8; i++) out[i] = (uint8_t)(w[i >> 2] >> (8 * (i & 3)));
+    } else {
+        for (uint32_t i = 0; i < K; i++) out[i] = src[i];
+    }
+}
+
+__device__ __forceinline__ void ref_store_k(uint8_t* __restrict__ dst, uint32_t K, const uint8_t* in) {
+    if (K == 16 || K == 8) {
+        uint32_t w[4] = {0u, 0u, 0u, 0u};
+        for (uint32_t i = 0; i < K; i++) w[i >> 2] |= (uint32_t)in[i] << (8 * (i & 3));
+        if (K == 16) *reinterpret_cast<uint4*>(dst) = make_uint4(w[0], w[1], w[2], w[3]);
+        else *reinterpret_cast<uint2*>(dst) = make_uint2(w[0], w[1]);
+    } else {
+        for (uint32_t i = 0; i < K; i++) dst[i] = in[i];
+    }
+}
+
+__device__ __forceinline__ bool bit_of(const uint32_t* bm, uint32_t v) { return (__ldcg(bm + (v >> 5)) >> (v & 31u)) & 1u; }
+__device__ __forceinline__ void set_bit(uint32_t* bm, uint32_t v) { atomicOr(bm + (v >> 5), 1u << (v & 31u)); }
+
+__device__ __forceinline__ uint32_t grid_threads() { return gridDim.x * blockDim.x; }
+__device__ __forceinline__ uint32_t grid_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+// Appends the voxels of bitmap word `m` (word index i) to a list, every lane of
+// the warp calling it with its own word: one atomic per warp reserves the
+// warp's entries, which keep word order within the warp.
+__device__ __forceinline__ void warp_compact(uint32_t m, uint32_t i, uint32_t* list, uint32_t* counter) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t n = (uint32_t)__popc(m);
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += u;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0u) return;
+    uint32_t base = 0;
+    if (lane == 31u) base = atomicAdd(counter, total);
+    base = __shfl_sync(0xffffffffu, base, 31) + incl - n;
+    for (; m; m &= m - 1u) list[base++] = i * 32u + (uint32_t)(__ffs((int)m) - 1);
+}
+
+// The act list of act bitmap c.
+__global__ void __launch_bounds__(256) ref_sp_list_act(RefSparse sp) {
+    for (uint32_t i0 = grid_tid() & ~31u; i0 < sp.W; i0 += grid_threads()) {
+        const uint32_t i = i0 + (threadIdx.x & 31u);
+        warp_compact(i < sp.W ? sp.act_bm[sp.c][i] : 0u, i, sp.act_list, sp.cnt + 0);
+    }
+}
+
+// The touch list, and the union list of act bitmap c and the touch bitmap.
+__global__ void __launch_bounds__(256) ref_sp_list_touch(RefSparse sp) {
+    for (uint32_t i0 = grid_tid() & ~31u; i0 < sp.W; i0 += grid_threads()) {
+        const uint32_t i = i0 + (threadIdx.x & 31u);
+        const uint32_t t = i < sp.W ? __ldcg(sp.touch_bm + i) : 0u;
+        const uint32_t a = i < sp.W ? sp.act_bm[sp.c][i] : 0u;
+        warp_compact(t, i, sp.touch_list, sp.cnt + 1);
+        warp_compact(a | t, i, sp.union_list, sp.cnt + 2);
+    }
+}
+
+// Pass 1: directions of every particle of the act list; departures, arrival
+// counts, touched voxels and the contention test.  Also marks the voxels whose
+// reaction seed itime + x*y + z is 0 this frame, clears act bitmap c ^ 1 (the
+// reaction pass fills it) and the touch and union list counters.
+__global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse sp, const uint8_t* __restrict__ slots,
+                                                         const uint32_t* __restrict__ occ,
+                                                         const uint32_t* __restrict__ itimes, uint32_t step,
+                                                         uint32_t* diag, uint32_t* contended) {
+    const uint32_t itime = __ldg(itimes + step);
+    const uint32_t K = p.K;
+    const uint32_t n = __ldcg(sp.cnt + 0);
+    if (grid_tid() == 0) {
+        sp.cnt[1] = 0u;
+        sp.cnt[2] = 0u;
+    }
+    for (uint32_t i = grid_tid(); i < sp.W; i += grid_threads()) sp.act_bm[sp.c ^ 1u][i] = 0u;
+    const uint32_t XY = p.X * p.Y;
+    for (uint32_t g = grid_tid(); g < XY; g += grid_threads()) {
+        const uint32_t x = g / p.Y, y = g - x * p.Y;
+        const uint32_t z = 0u - itime - x * y;  // u32 wrap, as the shader's seed arithmetic
+        if (z < p.Z) set_bit(sp.touch_bm, g * p.Z + z);
+    }
+    for (uint32_t e = grid_tid(); e < n; e += grid_threads()) {
+        const uint32_t v = sp.act_list[e];
+        uint32_t o = occ[v];
+        if (o > K) {
+            // the gather's contention test fails for this voxel whatever arrives
+            atomicAdd(diag + DIAG_OCC_RANGE, 1u);
+            atomicOr(contended, 1u);
+            o = K;
+        }
+        uint8_t sl[16], dr[16];
+        ref_load_k(slots + (size_t)v * K, K, sl);
+        uint32_t x, y, z;
+        ref_coords(p, v, x, y, z);
+        bool has_dep = false;
+        for (uint32_t s = 0; s < K; s++) {
+            dr[s] = 7;
+            if (s < o && sl[s] != 0u) {
+                const int d = ref_decide(p, v, x, y, z, sl[s], v * K + s, itime);
+                dr[s] = (uint8_t)d;
+                has_dep |= d < 6;
+            }
+        }
+        if (!has_dep) continue;
+        ref_store_k(sp.dirs + (size_t)v * K, K, dr);
+        ref_store_k(sp.snap + (size_t)v * K, K, sl);
+        set_bit(sp.dep_bm, v);
+        set_bit(sp.touch_bm, v);
+        for (uint32_t s = 0; s < K; s++) {
+            if (dr[s] >= 6) continue;
+            const uint32_t w = (uint32_t)((int64_t)v + ref_nb_offset(p, dr[s]));
+            const uint32_t before = atomicAdd(sp.arrivals + w, 1u);
+            uint8_t ws[16];
+            ref_load_k(slots + (size_t)w * K, K, ws);
+            uint32_t nnz = 0;
+            for (uint32_t t = 0; t < K; t++) nnz += ws[t] != 0u;
+            const uint32_t ow = occ[w];
+            const uint32_t base = ow > nnz ? ow : nnz;
+            if ((uint64_t)base + before + 1u > K) atomicOr(contended, 1u);
+            set_bit(sp.touch_bm, w);
+        }
+    }
+}
+
+// Pass 2 (frames without contention): the gather of every touched voxel, in place.
+__global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, uint8_t* __restrict__ slots,
+                                                     uint32_t* __restrict__ occ, int32_t* __restrict__ conc,
+                                                     const uint32_t* __restrict__ contended) {
+    if (*contended) return;
+    const uint32_t K = p.K, S1 = p.S1;
+    const uint32_t n = __ldcg(sp.cnt + 1);
+    for (uint32_t e = grid_tid(); e < n; e += grid_threads()) {
+        const uint32_t w = sp.touch_list[e];
+        sp.arrivals[w] = 0u;
+        uint32_t x, y, z;
+        ref_coords(p, w, x, y, z);
+        const bool has_nb[6] = {x > 0u, x < p.X - 1u, y > 0u, y < p.Y - 1u, z > 0u, z < p.Z - 1u};
+        uint8_t sl[16], nd[16], ns[16];
+        ref_load_k(slots + (size_t)w * K, K, sl);
+        uint32_t o = occ[w];
+        int32_t* cw = conc + (size_t)w * S1;
+        // arrivals from the neighbour on `side`: the particles it moves in direction side ^ 1
+        auto arrive = [&](int side) {
+            if (!has_nb[side]) return;
+            const uint32_t u = (uint32_t)((int64_t)w + ref_nb_offset(p, side));
+            if (!bit_of(sp.dep_bm, u)) return;
+            const uint8_t want = (uint8_t)(side ^ 1);
+            ref_load_k(sp.dirs + (size_t)u * K, K, nd);
+            ref_load_k(sp.snap + (size_t)u * K, K, ns);
+            for (uint32_t s = 0; s < K; s++) {
+                if (nd[s] != want) continue;
+                const uint8_t q = ns[s];
+                uint32_t j = 0;
+                while (j < K && sl[j] != 0) j++;
+                if (j == K) continue;  // unreachable without contention
+                sl[j] = q;
+                o++;
+                cw[q] = (int32_t)((uint32_t)cw[q] + 1u);
+            }
+        };
+        arrive(0);  // from -x
+        arrive(2);  // from -y
+        arrive(4);  // from -z
+        if (bit_of(sp.dep_bm, w)) {
+            ref_load_k(sp.dirs + (size_t)w * K, K, nd);
+            for (uint32_t s = 0; s < K; s++) {
+                if (nd[s] >= 6) continue;
+                const uint8_t q = sl[s];
+                sl[s] = 0;
+                o--;
+                cw[q] = (int32_t)((uint32_t)cw[q] - 1u);
+            }
+        }
+        arrive(5);  // from +z
+        arrive(3);  // from +y
+        arrive(1);  // from +x
+        ref_store_k(slots + (size_t)w * K, K, sl);
+        occ[w] = o;
+    }
+}
+
+// Pass 3 (contended frames): the serial diffusion of rdme.wgsl:45-88 in place,
+// voxels in linear order.  A departing slot still holds its particle when its
+// voxel's turn comes (arrivals only fill empty slots), and a slot that an
+// arrival filled has direction 7.  One block scans the departure bitmap; its
+// first thread makes the moves.
+__global__ void ref_sp_serial(RefParams p, RefSparse sp, uint8_t* __restrict__ slots, uint32_t* __restrict__ occ,
+                              int32_t* __restrict__ conc, uint32_t* diag, const uint32_t* __restrict__ contended) {
+    if (*contended == 0u) return;
+    __shared__ uint32_t s_words[1024];
+    const uint32_t K = p.K, S1 = p.S1;
+    uint32_t spills = 0;
+    for (uint32_t w0 = 0; w0 < sp.W; w0 += 1024) {
+        const uint32_t i = w0 + threadIdx.x;
+        s_words[threadIdx.x] = i < sp.W ? sp.dep_bm[i] : 0u;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (uint32_t k = 0; k < 1024 && w0 + k < sp.W; k++) {
+                for (uint32_t m = s_words[k]; m; m &= m - 1u) {
+                    const uint32_t v = (w0 + k) * 32u + (uint32_t)(__ffs((int)m) - 1);
+                    for (uint32_t s = 0; s < K; s++) {
+                        const int d = sp.dirs[(size_t)v * K + s];
+                        if (d >= 6) continue;
+                        const uint32_t w = (uint32_t)((int64_t)v + ref_nb_offset(p, d));
+                        sp.arrivals[w] = 0u;
+                        if (occ[w] >= K) { spills++; continue; }
+                        uint32_t j = 0;
+                        while (j < K && slots[(size_t)w * K + j] != 0) j++;
+                        if (j == K) { spills++; continue; }
+                        const uint8_t q = slots[(size_t)v * K + s];
+                        slots[(size_t)w * K + j] = q;
+                        occ[w] += 1u;
+                        conc[(size_t)w * S1 + q] = (int32_t)((uint32_t)conc[(size_t)w * S1 + q] + 1u);
+                        occ[v] -= 1u;
+                        slots[(size_t)v * K + s] = 0;
+                        conc[(size_t)v * S1 + q] = (int32_t)((uint32_t)conc[(size_t)v * S1 + q] - 1u);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        diag[DIAG_SPILL] += spills;
+        diag[DIAG_SLOW_STEPS] += 1u;
+    }
+}
+
+// The reaction pass on one voxel and its bit in act bitmap c ^ 1.
+__device__ __forceinline__ void ref_sp_react(const RefParams& p, const RefSparse& sp, uint32_t v, uint8_t* slots,
+                                             uint32_t* occ, int32_t* conc, uint32_t itime, int32_t* s_delta) {
+    ref_cme_voxel(p, v, slots, occ, conc, itime, s_delta);
+    const uint32_t K = p.K, S1 = p.S1;
+    uint8_t sl[16];
+    ref_load_k(slots + (size_t)v * K, K, sl);
+    bool keep = occ[v] != 0u;
+    for (uint32_t s = 0; s < K; s++) keep |= sl[s] != 0u;
+    const int32_t* c = conc + (size_t)v * S1;
+    for (uint32_t s = 1; s < S1 && !keep; s++) keep |= c[s] != 0;
+    if (keep) set_bit(sp.act_bm[sp.c ^ 1u], v);
+}
+
+// Pass 4: the reaction pass over the union list (every voxel when `dense`),
+// setting act bitmap c ^ 1; clears the contention flag, the touch and
+// departure bitmaps and the act list counter for the next frame.
+__global__ void __launch_bounds__(256) ref_sp_cme(RefParams p, RefSparse sp, uint8_t* __restrict__ slots,
+                                                  uint32_t* __restrict__ occ, int32_t* __restrict__ conc,
+                                                  const uint32_t* __restrict__ itimes, uint32_t step, uint32_t dense,
+                                                  int32_t* stat, uint32_t* diag, uint32_t* contended) {
+    extern __shared__ int32_t s_delta[];  // [S1] + 2 counters
+    for (uint32_t s = threadIdx.x; s < p.S1 + 2; s += blockDim.x) s_delta[s] = 0;
+    if (grid_tid() == 0) {
+        *contended = 0u;  // every reader of this frame's flag has run
+        sp.cnt[0] = 0u;
+    }
+    __syncthreads();
+    const uint32_t itime = __ldg(itimes + step);
+    for (uint32_t i = grid_tid(); i < sp.W; i += grid_threads()) {
+        sp.touch_bm[i] = 0u;
+        sp.dep_bm[i] = 0u;
+    }
+    if (dense) {
+        for (uint32_t v = grid_tid(); v < (uint32_t)p.V; v += grid_threads())
+            ref_sp_react(p, sp, v, slots, occ, conc, itime, s_delta);
+    } else {
+        const uint32_t n = __ldcg(sp.cnt + 2);
+        for (uint32_t e = grid_tid(); e < n; e += grid_threads())
+            ref_sp_react(p, sp, sp.union_list[e], slots, occ, conc, itime, s_delta);
+    }
+    __syncthreads();
+    ref_flush_block(p, s_delta, stat, diag);
+}
+
+// Act bitmap c of a freshly uploaded lattice.
+__global__ void ref_sp_build_act(RefParams p, RefSparse sp, const uint8_t* __restrict__ slots,
+                                 const uint32_t* __restrict__ occ, const int32_t* __restrict__ conc) {
+    for (uint32_t v = grid_tid(); v < (uint32_t)p.V; v += grid_threads()) {
+        bool keep = occ[v] != 0u;
+        for (uint32_t s = 0; s < p.K && !keep; s++) keep |= slots[(size_t)v * p.K + s] != 0u;
+        for (uint32_t s = 1; s < p.S1 && !keep; s++) keep |= conc[(size_t)v * p.S1 + s] != 0;
+        if (keep) set_bit(sp.act_bm[sp.c], v);
+    }
+}
+
 // ------------------------------------------------------------------ host side
+
+static RefSparse ref_sparse(DeviceRef* d) {
+    RefSparse sp{};
+    for (int b = 0; b < 2; b++) sp.act_bm[b] = d->act_bm[b].p;
+    sp.touch_bm = d->touch_bm.p;
+    sp.dep_bm = d->dep_bm.p;
+    sp.act_list = d->act_list.p;
+    sp.touch_list = d->touch_list.p;
+    sp.union_list = d->union_list.p;
+    sp.cnt = d->cnt.p;
+    sp.arrivals = d->arrivals.p;
+    sp.dirs = d->dirs.p;
+    sp.snap = d->snap.p;
+    sp.W = (uint32_t)d->touch_bm.n;
+    sp.c = d->par;
+    return sp;
+}
 
 static void ref_bind(DeviceRef* d) {
     d->p.P = d->P.p;
@@ -353,6 +747,8 @@ static void ref_bind(DeviceRef* d) {
 DeviceRef* ref_create(const Model& m, int device) {
     m.check_tables();
     if (m.n_reactions > 99) throw Error(CS_ERR_LIMIT, "at most 99 reactions");
+    if (m.V * m.K >= (1ull << 32))
+        throw Error(CS_ERR_LIMIT, "the reference-RNG path indexes slots with u32: V * K must be below 2^32");
     if (m.nr > 256) throw Error(CS_ERR_LIMIT, "at most 256 regions");
     if (m.n_species > 255) throw Error(CS_ERR_LIMIT, "at most 255 species");
     int ndev = 0;
@@ -370,14 +766,29 @@ DeviceRef* ref_create(const Model& m, int device) {
     p.V = m.V;
     p.tau = m.tau;
     uint64_t VK = m.V * m.K, VS = m.V * p.S1;
-    for (int b = 0; b < 2; b++) {
-        d->slots[b].alloc(VK);
-        d->occ[b].alloc(m.V);
-        d->conc[b].alloc(VS);
-    }
+    d->slots.alloc(VK);
+    d->occ.alloc(m.V);
+    d->conc.alloc(VS);
     d->regions.alloc(m.V);
     d->reservoir.alloc(m.V);
     d->dirs.alloc(VK);
+    d->snap.alloc(VK);
+    const uint64_t W = (m.V + 31) / 32;
+    for (int b = 0; b < 2; b++) d->act_bm[b].alloc(W);
+    d->touch_bm.alloc(W);
+    d->dep_bm.alloc(W);
+    d->act_list.alloc(m.V);
+    d->touch_list.alloc(m.V);
+    d->union_list.alloc(m.V);
+    d->cnt.alloc(3);
+    d->arrivals.alloc(m.V);
+    CS_CUDA(cudaMemset(d->arrivals.p, 0, m.V * 4));
+    int sms = 1;
+    CS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    d->grid = sms * 8;
+    for (uint32_t r = 1; r <= m.n_reactions; r++)
+        if (m.reactants[r * 3] == 0u && m.reactants[r * 3 + 1] == 0u && m.reactants[r * 3 + 2] == 0u)
+            d->dense_always = true;
     std::vector<float> P;
     compute_ref_probabilities(m, P);
     d->P.alloc(P.size());
@@ -419,10 +830,23 @@ void ref_set_lattice(DeviceRef* d, const uint32_t* slots, const uint32_t* occ, c
         s8[i] = (uint8_t)slots[i];
     }
     CS_CUDA(cudaStreamSynchronize(d->stream));
-    d->cur = 0;
-    CS_CUDA(cudaMemcpy(d->slots[0].p, s8.data(), VK, cudaMemcpyHostToDevice));
-    CS_CUDA(cudaMemcpy(d->occ[0].p, occ, d->p.V * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    CS_CUDA(cudaMemcpy(d->conc[0].p, conc, VS * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->slots.p, s8.data(), VK, cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->occ.p, occ, d->p.V * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CS_CUDA(cudaMemcpy(d->conc.p, conc, VS * sizeof(int32_t), cudaMemcpyHostToDevice));
+    // the sparse passes start from the act list of the new lattice and empty
+    // touch lists and bitmaps; its first reaction pass visits every voxel
+    // (conc[v][0] = 1, compaction)
+    const size_t wb = d->touch_bm.bytes();
+    for (int b = 0; b < 2; b++) CS_CUDA(cudaMemset(d->act_bm[b].p, 0, wb));
+    CS_CUDA(cudaMemset(d->touch_bm.p, 0, wb));
+    CS_CUDA(cudaMemset(d->dep_bm.p, 0, wb));
+    CS_CUDA(cudaMemset(d->cnt.p, 0, d->cnt.bytes()));
+    CS_CUDA(cudaMemset(d->arrivals.p, 0, d->arrivals.bytes()));
+    d->par = 0;
+    ref_sp_build_act<<<d->grid, 256, 0, d->stream>>>(d->p, ref_sparse(d), d->slots.p, d->occ.p, d->conc.p);
+    CS_LAUNCH_CHECK();
+    CS_CUDA(cudaStreamSynchronize(d->stream));
+    d->dense_next = true;
     // create_statistics, src/simulation.rs:361-388: the counts restart from the sum of the concentrations
     std::vector<int32_t> st(d->p.S1, 0);
     for (uint64_t v = 0; v < d->p.V; v++)
@@ -447,7 +871,7 @@ void ref_render_view(DeviceRef* d, int32_t view, int32_t slice_axis, uint32_t sl
         out_dev = tmp.p;
     }
     ViewParams v{};
-    v.slots = d->slots[d->cur].p;
+    v.slots = d->slots.p;
     v.K = d->p.K;
     v.X = d->p.X; v.Y = d->p.Y; v.Z = d->p.Z;
     v.region_id = d->regions.p;
@@ -468,33 +892,30 @@ void ref_get_lattice(DeviceRef* d, uint32_t* slots, uint32_t* occ, int32_t* conc
     uint64_t VK = d->p.V * d->p.K, VS = d->p.V * d->p.S1;
     if (slots) {
         std::vector<uint8_t> s8(VK);
-        CS_CUDA(cudaMemcpy(s8.data(), d->slots[d->cur].p, VK, cudaMemcpyDeviceToHost));
+        CS_CUDA(cudaMemcpy(s8.data(), d->slots.p, VK, cudaMemcpyDeviceToHost));
         for (uint64_t i = 0; i < VK; i++) slots[i] = s8[i];
     }
-    if (occ) CS_CUDA(cudaMemcpy(occ, d->occ[d->cur].p, d->p.V * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-    if (conc) CS_CUDA(cudaMemcpy(conc, d->conc[d->cur].p, VS * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (occ) CS_CUDA(cudaMemcpy(occ, d->occ.p, d->p.V * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (conc) CS_CUDA(cudaMemcpy(conc, d->conc.p, VS * sizeof(int32_t), cudaMemcpyDeviceToHost));
 }
 
-// Enqueues the five launches of one frame reading itimes[k].
+// Enqueues the sparse passes of one frame reading itimes[k].
 static void ref_enqueue_frame(DeviceRef* d, uint32_t k) {
     const RefParams& p = d->p;
+    const RefSparse sp = ref_sparse(d);
     const int TB = 256;
-    unsigned nb = (unsigned)((p.V + TB - 1) / TB);
-    size_t smem = (p.S1 + 2) * sizeof(int32_t);
-    int a = d->cur, b = a ^ 1;
-    ref_directions<<<nb, TB, 0, d->stream>>>(p, d->slots[a].p, d->occ[a].p, d->itimes.p, k, d->dirs.p, d->diag.p,
-                                             d->flag.p);
-    ref_gather<<<nb, TB, 0, d->stream>>>(p, d->slots[a].p, d->occ[a].p, d->conc[a].p, d->dirs.p, d->slots[b].p,
-                                         d->occ[b].p, d->conc[b].p, d->flag.p);
-    ref_serial_copy<<<std::min<unsigned>(nb, 4096u), TB, 0, d->stream>>>(p, d->flag.p, d->slots[a].p, d->occ[a].p,
-                                                                         d->conc[a].p, d->slots[b].p, d->occ[b].p,
-                                                                         d->conc[b].p);
-    ref_serial<<<1, 32, 0, d->stream>>>(p, d->flag.p, d->slots[a].p, d->occ[a].p, d->dirs.p, d->slots[b].p,
-                                        d->occ[b].p, d->conc[b].p, d->diag.p);
-    ref_cme<<<nb, TB, smem, d->stream>>>(p, d->slots[b].p, d->occ[b].p, d->conc[b].p, d->itimes.p, k, d->stat.p,
-                                         d->diag.p);
+    const size_t smem = (p.S1 + 2) * sizeof(int32_t);
+    ref_sp_list_act<<<d->grid, TB, 0, d->stream>>>(sp);
+    ref_sp_directions<<<d->grid, TB, 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->itimes.p, k, d->diag.p, d->flag.p);
+    ref_sp_list_touch<<<d->grid, TB, 0, d->stream>>>(sp);
+    ref_sp_gather<<<d->grid, TB, 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->conc.p, d->flag.p);
+    ref_sp_serial<<<1, 1024, 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->conc.p, d->diag.p, d->flag.p);
+    const uint32_t dense = (d->dense_next || d->dense_always) ? 1u : 0u;
+    ref_sp_cme<<<d->grid, TB, smem, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->conc.p, d->itimes.p, k, dense, d->stat.p,
+                                                 d->diag.p, d->flag.p);
     CS_LAUNCH_CHECK();
-    d->cur = b;
+    d->dense_next = false;
+    d->par ^= 1u;
 }
 
 static void ref_enqueue(DeviceRef* d, uint32_t n) {

@@ -70,9 +70,10 @@ def _three_species_case(res, precision, seed0):
     tau = float(np.float32(tmpl.info().tau))
     n_vox = int(np.prod(res))
     init = [0, 200, 200, 0]
-    times = (0.25, 1.0, 3.0)
-    frames = [int(round(t / tau)) for t in times]
     every = 5
+    # sample frames on the first-passage grid (multiples of `every`)
+    frames = [every * int(round(t / tau / every)) for t in (0.25, 1.0, 3.0)]
+    times = [round(f * tau, 4) for f in frames]
     # SSA: stationary mean of C, then the sample times and a first-passage grid
     re, rates, csp, cd = _ssa_tables(tmpl, n_vox)
     long, _ = oracle.ssa_batch(3, re, rates, csp, cd, init, 1, 400, [40.0])
@@ -84,15 +85,17 @@ def _three_species_case(res, precision, seed0):
     # lattice: the first-passage grid, then the remaining frames to the sample times
     ens = _ens(tmpl, res, init, seed0, precision)
     traj = []
-    for _ in range(grid_n):
-        ens.step(every)
-        traj.append(ens.counts()[:, 3])
-    done = grid_n * every
     got_t = []
-    for f in frames:
-        if f > done:
-            ens.step(f - done)
-            done = f
+    for k in range(grid_n):
+        ens.step(every)
+        c = ens.counts()
+        traj.append(c[:, 3])
+        if (k + 1) * every in frames:
+            got_t.append(c)
+    done = grid_n * every
+    for f in frames[len(got_t):]:
+        ens.step(f - done)
+        done = f
         got_t.append(ens.counts())
     ens.close()
     tr = np.stack(traj, 1)
