@@ -206,8 +206,12 @@ cs_status cs_set_precision(cs_sim* sim, int32_t precision);
 cs_status cs_get_counts(cs_sim* sim, int64_t* counts);
 /* Drains the recorded samples (Simulation::stats, src/simulation.rs:36). */
 cs_status cs_pop_stats(cs_sim* sim, cs_stat_sample* out, uint32_t capacity, uint32_t* n_out);
-/* Diagnostic counters: capacity spills, occupancy range,
- * serial-resolution steps, rollbacks, fired voxels, ... */
+/* Diagnostic counters, diag[n].  Reference-RNG path: [0] moves rejected for
+ * capacity, [1] voxels whose occupancy exceeded K, [2] frames resolved in
+ * serial order, [3] reaction rollbacks, [4] voxels that fired.  Production
+ * path: [0] reaction events, [1] events rejected for capacity, [2] voxels that
+ * hit the event cap, [3] FP64 selections, [4] bricks spilled to the second
+ * brick pass, [5] bricks lost (always 0), [6] voxels that ran the SSA. */
 cs_status cs_get_diagnostics(cs_sim* sim, uint32_t* diag, uint32_t n);
 cs_status cs_synchronize(cs_sim* sim);
 

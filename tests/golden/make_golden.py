@@ -31,7 +31,8 @@ from cell_simulation_gb300 import configs  # noqa: E402
 from cell_simulation_gb300.simulation import Simulation  # noqa: E402
 from tests.helpers import crowded_model, itime_schedule, multi_region_model, oracle_args, ref_state  # noqa: E402
 
-REFERENCE_EASY_JSON = Path("/root/reference/saved_models/easy.json")
+# the reference's own saved model (saved_models/easy.json), kept beside the fixtures
+REFERENCE_EASY_JSON = Path(__file__).resolve().parent / "saved_models" / "easy.json"
 
 
 def tables_dict(prefix, sim):

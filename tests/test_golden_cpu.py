@@ -56,3 +56,45 @@ def test_drop_in_rebuild_from_golden_tables():
         s, _, _ = sim.get_lattice()
         assert np.array_equal(s.astype(np.uint8), c.g["in_slots"])
         sim.close()
+
+
+def test_reference_saved_model_loads_to_the_stored_tables(lib):
+    """The reference's own saved model (tests/golden/saved_models/easy.json, the file the reference
+    ships as saved_models/easy.json) through cs_from_json_string: region mask, diffusion matrix,
+    stoichiometry, reactants, rates and the seeded initial lattice equal the stored golden case."""
+    from pathlib import Path
+
+    from cell_simulation_gb300.simulation import Simulation
+    text = (Path(G.PATH).parent / "saved_models" / "easy.json").read_text()
+    sim = Simulation.from_json(text, placement_seed=7)
+    c = G.case(DATA, "easy")
+    t = sim.tables()
+    i = sim.info()
+    assert tuple(int(x) for x in i.res) == c.res and i.max_particles_site == c.K
+    assert (i.n_regions, i.n_species, i.n_reactions) == (c.NR, c.S, c.R)
+    assert np.array_equal(t.regions.astype(np.uint8), c.g["regions"])
+    assert np.array_equal(t.diffusion, c.g["diffusion"])
+    assert np.array_equal(t.stoich, c.g["stoich"])
+    assert np.array_equal(t.reactants.astype(np.uint8), c.g["reactants"])
+    assert np.array_equal(t.rates, c.g["rates"])
+    assert np.array_equal(t.reservoir.astype(np.uint8), c.g["reservoir"])
+    s, o, conc = sim.get_lattice()
+    assert np.array_equal(s, c.g["in_slots"].astype(np.uint32))
+    assert np.array_equal(o, c.g["in_occ"].astype(np.uint32))
+    assert np.array_equal(conc, c.g["in_conc"].astype(np.int32))
+
+
+def test_second_reference_saved_model_is_refused_like_the_reference(lib):
+    """saved_models/easy_2.json declares a "sparse" region, which the reference's loader does not
+    build (it panics, src/simulation.rs:275-276): cs_from_json_string refuses it with
+    CS_ERR_PARSE and says why, instead of panicking."""
+    from pathlib import Path
+
+    import pytest
+
+    from cell_simulation_gb300 import CellsimError
+    from cell_simulation_gb300.simulation import Simulation
+    text = (Path(G.PATH).parent / "saved_models" / "easy_2.json").read_text()
+    with pytest.raises(CellsimError) as e:
+        Simulation.from_json(text, placement_seed=3)
+    assert e.value.status == 5 and "sparse" in str(e.value)
