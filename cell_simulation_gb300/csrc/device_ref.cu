@@ -278,10 +278,6 @@ __global__ void ref_serial(RefParams p, const uint32_t* contended, const uint8_t
     diag[DIAG_SLOW_STEPS] += 1u;
 }
 
-// cme.wgsl:26-120 followed by final_stage.wgsl:25-33 for voxel v, in place:
-// conc[v][0] = 1, the one-event test, the species-major rewrite with rollback
-// and the stable compaction.  s_delta[0..S1) collects species deltas,
-// s_delta[S1] fired voxels and s_delta[S1 + 1] rollbacks (block-shared).
 // Coordinates of voxel v (V * K < 2^32 on this path: the reference indexes
 // slots with u32, functions.wgsl:42-51).
 __device__ __forceinline__ void ref_coords(const RefParams& p, uint32_t v, uint32_t& x, uint32_t& y, uint32_t& z) {
@@ -291,6 +287,56 @@ __device__ __forceinline__ void ref_coords(const RefParams& p, uint32_t v, uint3
     y = t - x * p.Y;
 }
 
+// The K (<= 16) slot bytes of one voxel held in two 64-bit registers, byte i =
+// slot i, so that the reaction pass touches the slot array with one load and
+// at most one store per voxel.
+struct RefSlots {
+    uint64_t lo, hi;
+};
+
+__device__ __forceinline__ uint32_t rs_get(const RefSlots& a, uint32_t i) {
+    return (uint32_t)((i < 8u ? a.lo >> (8u * i) : a.hi >> (8u * (i - 8u))) & 0xFFull);
+}
+
+__device__ __forceinline__ void rs_set(RefSlots& a, uint32_t i, uint32_t q) {
+    if (i < 8u) a.lo = (a.lo & ~(0xFFull << (8u * i))) | ((uint64_t)q << (8u * i));
+    else a.hi = (a.hi & ~(0xFFull << (8u * (i - 8u)))) | ((uint64_t)q << (8u * (i - 8u)));
+}
+
+// Vector access when K is 8 or 16 and the voxel's slots are aligned to it (the library's own
+// buffers always are; a caller's buffer of the allocation-free entry point may not be).
+__device__ __forceinline__ RefSlots rs_load(const uint8_t* sl, uint32_t K) {
+    RefSlots a{0ull, 0ull};
+    const uintptr_t al = (uintptr_t)sl;
+    if (K == 16u && (al & 15u) == 0u) {
+        const uint4 t = *reinterpret_cast<const uint4*>(sl);
+        a.lo = (uint64_t)t.x | ((uint64_t)t.y << 32);
+        a.hi = (uint64_t)t.z | ((uint64_t)t.w << 32);
+    } else if (K == 8u && (al & 7u) == 0u) {
+        const uint2 t = *reinterpret_cast<const uint2*>(sl);
+        a.lo = (uint64_t)t.x | ((uint64_t)t.y << 32);
+    } else {
+        for (uint32_t i = 0; i < K; i++) rs_set(a, i, sl[i]);
+    }
+    return a;
+}
+
+__device__ __forceinline__ void rs_store(uint8_t* sl, uint32_t K, const RefSlots& a) {
+    const uintptr_t al = (uintptr_t)sl;
+    if (K == 16u && (al & 15u) == 0u) {
+        *reinterpret_cast<uint4*>(sl) = make_uint4((uint32_t)a.lo, (uint32_t)(a.lo >> 32), (uint32_t)a.hi,
+                                                   (uint32_t)(a.hi >> 32));
+    } else if (K == 8u && (al & 7u) == 0u) {
+        *reinterpret_cast<uint2*>(sl) = make_uint2((uint32_t)a.lo, (uint32_t)(a.lo >> 32));
+    } else {
+        for (uint32_t i = 0; i < K; i++) sl[i] = (uint8_t)rs_get(a, i);
+    }
+}
+
+// cme.wgsl:26-120 and final_stage.wgsl:25-33 for voxel v, in place:
+// conc[v][0] = 1, the one-event test, the species-major rewrite with rollback
+// and the stable compaction.  s_delta[0..S1) collects species deltas,
+// s_delta[S1] fired voxels and s_delta[S1 + 1] rollbacks (block-shared).
 __device__ void ref_cme_voxel(const RefParams& p, uint64_t v, uint8_t* __restrict__ slots, uint32_t* __restrict__ occ,
                               int32_t* __restrict__ conc, uint32_t itime, int32_t* s_delta) {
     const uint32_t K = p.K, S1 = p.S1, R = p.R;
@@ -298,16 +344,16 @@ __device__ void ref_cme_voxel(const RefParams& p, uint64_t v, uint8_t* __restric
     uint32_t x, y, z;
     ref_coords(p, (uint32_t)v, x, y, z);
     int32_t* c = conc + v * S1;
-    uint8_t* sl = slots + v * K;
-    c[0] = 1;
+    uint8_t* slp = slots + v * K;
+    if (c[0] != 1) c[0] = 1;  // stored only when it changes: an unchanged row is not written back
     float total = 0.0f;
     for (uint32_t r = 1; r <= R; r++) {
         uint32_t prod = (uint32_t)c[p.reactants[r * 3]] * (uint32_t)c[p.reactants[r * 3 + 1]] *
                         (uint32_t)c[p.reactants[r * 3 + 2]];
         total = __fadd_rn(total, __fmul_rn(p.rates[r], __int2float_rn((int32_t)prod)));
     }
-    uint8_t snap[16];
-    for (uint32_t s = 0; s < K; s++) snap[s] = sl[s];
+    const RefSlots snap = rs_load(slp, K);
+    RefSlots sl = snap;
     uint32_t state = d_pcg(itime + x * y + z);
     float r1 = d_uniform_float(state);
     float fire_p = __fsub_rn(1.0f, d_expf(__fmul_rn(-total, p.tau)));
@@ -338,11 +384,11 @@ __device__ void ref_cme_voxel(const RefParams& p, uint64_t v, uint8_t* __restric
             if (d) atomicAdd(&s_delta[s], d);
             int32_t cc = c[s];
             while (cc > 0) {
-                sl[j] = (uint8_t)s;
+                rs_set(sl, j, s);
                 cc--;
                 j++;
                 if (j >= K) {
-                    for (uint32_t k = 0; k < K; k++) sl[k] = snap[k];
+                    sl = snap;
                     for (uint32_t s2 = 1; s2 <= s; s2++) {
                         int32_t d2 = st[s2];
                         c[s2] = (int32_t)((uint32_t)c[s2] - (uint32_t)d2);
@@ -356,18 +402,17 @@ __device__ void ref_cme_voxel(const RefParams& p, uint64_t v, uint8_t* __restric
         }
         if (!rolled) {
             occ[v] = (uint32_t)new_occ;
-            while (j < K) sl[j++] = 0;
+            while (j < K) rs_set(sl, j++, 0u);
         }
     }
+    // stable move of the non-zero slots to the front
+    RefSlots out{0ull, 0ull};
     uint32_t jj = 0;
     for (uint32_t s = 0; s < K; s++) {
-        uint8_t q = sl[s];
-        if (q != 0) {
-            sl[s] = sl[jj];
-            sl[jj] = q;
-            jj++;
-        }
+        const uint32_t q = rs_get(sl, s);
+        if (q != 0u) rs_set(out, jj++, q);
     }
+    if (out.lo != snap.lo || out.hi != snap.hi) rs_store(slp, K, out);
 }
 
 // Adds a block's species deltas, fired voxels and rollbacks to the totals.
@@ -421,30 +466,10 @@ struct RefSparse {
     uint32_t c;          // frame parity
 };
 
-__device__ __forceinline__ void ref_load_k(const uint8_t* __restrict__ src, uint32_t K, uint8_t* out) {
-    if (K == 16) {
-        const uint4 t = *reinterpret_cast<const uint4*>(src);
-        const uint32_t w[4] = {t.x, t.y, t.z, t.w};
-        for (int i = 0; i < 16; i++) out[i] = (uint8_t)(w[i >> 2] >> (8 * (i & 3)));
-    } else if (K == 8) {
-        const uint2 t = *reinterpret_cast<const uint2*>(src);
-        const uint32_t w[2] = {t.x, t.y};
-        for (int i = 0; i < 8; i++) out[i] = (uint8_t)(w[i >> 2] >> (8 * (i & 3)));
-    } else {
-        for (uint32_t i = 0; i < K; i++) out[i] = src[i];
-    }
-}
-
-__device__ __forceinline__ void ref_store_k(uint8_t* __restrict__ dst, uint32_t K, const uint8_t* in) {
-    if (K == 16 || K == 8) {
-        uint32_t w[4] = {0u, 0u, 0u, 0u};
-        for (uint32_t i = 0; i < K; i++) w[i >> 2] |= (uint32_t)in[i] << (8 * (i & 3));
-        if (K == 16) *reinterpret_cast<uint4*>(dst) = make_uint4(w[0], w[1], w[2], w[3]);
-        else *reinterpret_cast<uint2*>(dst) = make_uint2(w[0], w[1]);
-    } else {
-        for (uint32_t i = 0; i < K; i++) dst[i] = in[i];
-    }
-}
+// act bitmaps of this frame and the next, chosen by select (indexing the kernel parameter's
+// array by a run-time value would copy the parameters to local memory)
+__device__ __forceinline__ uint32_t* act_cur(const RefSparse& sp) { return sp.c ? sp.act_bm[1] : sp.act_bm[0]; }
+__device__ __forceinline__ uint32_t* act_next(const RefSparse& sp) { return sp.c ? sp.act_bm[0] : sp.act_bm[1]; }
 
 __device__ __forceinline__ bool bit_of(const uint32_t* bm, uint32_t v) { return (__ldcg(bm + (v >> 5)) >> (v & 31u)) & 1u; }
 __device__ __forceinline__ void set_bit(uint32_t* bm, uint32_t v) { atomicOr(bm + (v >> 5), 1u << (v & 31u)); }
@@ -476,7 +501,7 @@ __device__ __forceinline__ void warp_compact(uint32_t m, uint32_t i, uint32_t* l
 __global__ void __launch_bounds__(256) ref_sp_list_act(RefSparse sp) {
     for (uint32_t i0 = grid_tid() & ~31u; i0 < sp.W; i0 += grid_threads()) {
         const uint32_t i = i0 + (threadIdx.x & 31u);
-        warp_compact(i < sp.W ? sp.act_bm[sp.c][i] : 0u, i, sp.act_list, sp.cnt + 0);
+        warp_compact(i < sp.W ? act_cur(sp)[i] : 0u, i, sp.act_list, sp.cnt + 0);
     }
 }
 
@@ -485,7 +510,7 @@ __global__ void __launch_bounds__(256) ref_sp_list_touch(RefSparse sp) {
     for (uint32_t i0 = grid_tid() & ~31u; i0 < sp.W; i0 += grid_threads()) {
         const uint32_t i = i0 + (threadIdx.x & 31u);
         const uint32_t t = i < sp.W ? __ldcg(sp.touch_bm + i) : 0u;
-        const uint32_t a = i < sp.W ? sp.act_bm[sp.c][i] : 0u;
+        const uint32_t a = i < sp.W ? act_cur(sp)[i] : 0u;
         warp_compact(t, i, sp.touch_list, sp.cnt + 1);
         warp_compact(a | t, i, sp.union_list, sp.cnt + 2);
     }
@@ -506,7 +531,7 @@ __global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse 
         sp.cnt[1] = 0u;
         sp.cnt[2] = 0u;
     }
-    for (uint32_t i = grid_tid(); i < sp.W; i += grid_threads()) sp.act_bm[sp.c ^ 1u][i] = 0u;
+    for (uint32_t i = grid_tid(); i < sp.W; i += grid_threads()) act_next(sp)[i] = 0u;
     const uint32_t XY = p.X * p.Y;
     for (uint32_t g = grid_tid(); g < XY; g += grid_threads()) {
         const uint32_t x = g / p.Y, y = g - x * p.Y;
@@ -522,32 +547,32 @@ __global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse 
             atomicOr(contended, 1u);
             o = K;
         }
-        uint8_t sl[16], dr[16];
-        ref_load_k(slots + (size_t)v * K, K, sl);
+        const RefSlots sl = rs_load(slots + (size_t)v * K, K);
         uint32_t x, y, z;
         ref_coords(p, v, x, y, z);
         bool has_dep = false;
+        RefSlots dr{0x0707070707070707ull, 0x0707070707070707ull};  // 7: stays
         for (uint32_t s = 0; s < K; s++) {
-            dr[s] = 7;
-            if (s < o && sl[s] != 0u) {
-                const int d = ref_decide(p, v, x, y, z, sl[s], v * K + s, itime);
-                dr[s] = (uint8_t)d;
+            const uint32_t q = rs_get(sl, s);
+            if (s < o && q != 0u) {
+                const int d = ref_decide(p, v, x, y, z, q, v * K + s, itime);
+                rs_set(dr, s, (uint32_t)d);
                 has_dep |= d < 6;
             }
         }
         if (!has_dep) continue;
-        ref_store_k(sp.dirs + (size_t)v * K, K, dr);
-        ref_store_k(sp.snap + (size_t)v * K, K, sl);
+        rs_store(sp.dirs + (size_t)v * K, K, dr);
+        rs_store(sp.snap + (size_t)v * K, K, sl);
         set_bit(sp.dep_bm, v);
         set_bit(sp.touch_bm, v);
         for (uint32_t s = 0; s < K; s++) {
-            if (dr[s] >= 6) continue;
-            const uint32_t w = (uint32_t)((int64_t)v + ref_nb_offset(p, dr[s]));
+            const uint32_t ds = rs_get(dr, s);
+            if (ds >= 6u) continue;
+            const uint32_t w = (uint32_t)((int64_t)v + ref_nb_offset(p, (int)ds));
             const uint32_t before = atomicAdd(sp.arrivals + w, 1u);
-            uint8_t ws[16];
-            ref_load_k(slots + (size_t)w * K, K, ws);
+            const RefSlots ws = rs_load(slots + (size_t)w * K, K);
             uint32_t nnz = 0;
-            for (uint32_t t = 0; t < K; t++) nnz += ws[t] != 0u;
+            for (uint32_t t = 0; t < K; t++) nnz += rs_get(ws, t) != 0u;
             const uint32_t ow = occ[w];
             const uint32_t base = ow > nnz ? ow : nnz;
             if ((uint64_t)base + before + 1u > K) atomicOr(contended, 1u);
@@ -569,8 +594,7 @@ __global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, 
         uint32_t x, y, z;
         ref_coords(p, w, x, y, z);
         const bool has_nb[6] = {x > 0u, x < p.X - 1u, y > 0u, y < p.Y - 1u, z > 0u, z < p.Z - 1u};
-        uint8_t sl[16], nd[16], ns[16];
-        ref_load_k(slots + (size_t)w * K, K, sl);
+        RefSlots sl = rs_load(slots + (size_t)w * K, K);
         uint32_t o = occ[w];
         int32_t* cw = conc + (size_t)w * S1;
         // arrivals from the neighbour on `side`: the particles it moves in direction side ^ 1
@@ -578,16 +602,16 @@ __global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, 
             if (!has_nb[side]) return;
             const uint32_t u = (uint32_t)((int64_t)w + ref_nb_offset(p, side));
             if (!bit_of(sp.dep_bm, u)) return;
-            const uint8_t want = (uint8_t)(side ^ 1);
-            ref_load_k(sp.dirs + (size_t)u * K, K, nd);
-            ref_load_k(sp.snap + (size_t)u * K, K, ns);
+            const uint32_t want = (uint32_t)(side ^ 1);
+            const RefSlots nd = rs_load(sp.dirs + (size_t)u * K, K);
+            const RefSlots ns = rs_load(sp.snap + (size_t)u * K, K);
             for (uint32_t s = 0; s < K; s++) {
-                if (nd[s] != want) continue;
-                const uint8_t q = ns[s];
+                if (rs_get(nd, s) != want) continue;
+                const uint32_t q = rs_get(ns, s);
                 uint32_t j = 0;
-                while (j < K && sl[j] != 0) j++;
+                while (j < K && rs_get(sl, j) != 0u) j++;
                 if (j == K) continue;  // unreachable without contention
-                sl[j] = q;
+                rs_set(sl, j, q);
                 o++;
                 cw[q] = (int32_t)((uint32_t)cw[q] + 1u);
             }
@@ -596,11 +620,11 @@ __global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, 
         arrive(2);  // from -y
         arrive(4);  // from -z
         if (bit_of(sp.dep_bm, w)) {
-            ref_load_k(sp.dirs + (size_t)w * K, K, nd);
+            const RefSlots nd = rs_load(sp.dirs + (size_t)w * K, K);
             for (uint32_t s = 0; s < K; s++) {
-                if (nd[s] >= 6) continue;
-                const uint8_t q = sl[s];
-                sl[s] = 0;
+                if (rs_get(nd, s) >= 6u) continue;
+                const uint32_t q = rs_get(sl, s);
+                rs_set(sl, s, 0u);
                 o--;
                 cw[q] = (int32_t)((uint32_t)cw[q] - 1u);
             }
@@ -608,7 +632,7 @@ __global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, 
         arrive(5);  // from +z
         arrive(3);  // from +y
         arrive(1);  // from +x
-        ref_store_k(slots + (size_t)w * K, K, sl);
+        rs_store(slots + (size_t)w * K, K, sl);
         occ[w] = o;
     }
 }
@@ -665,13 +689,11 @@ __device__ __forceinline__ void ref_sp_react(const RefParams& p, const RefSparse
                                              uint32_t* occ, int32_t* conc, uint32_t itime, int32_t* s_delta) {
     ref_cme_voxel(p, v, slots, occ, conc, itime, s_delta);
     const uint32_t K = p.K, S1 = p.S1;
-    uint8_t sl[16];
-    ref_load_k(slots + (size_t)v * K, K, sl);
-    bool keep = occ[v] != 0u;
-    for (uint32_t s = 0; s < K; s++) keep |= sl[s] != 0u;
+    const RefSlots sl = rs_load(slots + (size_t)v * K, K);
+    bool keep = occ[v] != 0u || (sl.lo | sl.hi) != 0ull;
     const int32_t* c = conc + (size_t)v * S1;
     for (uint32_t s = 1; s < S1 && !keep; s++) keep |= c[s] != 0;
-    if (keep) set_bit(sp.act_bm[sp.c ^ 1u], v);
+    if (keep) set_bit(act_next(sp), v);
 }
 
 // Pass 4: the reaction pass over the union list (every voxel when `dense`),
@@ -712,7 +734,7 @@ __global__ void ref_sp_build_act(RefParams p, RefSparse sp, const uint8_t* __res
         bool keep = occ[v] != 0u;
         for (uint32_t s = 0; s < p.K && !keep; s++) keep |= slots[(size_t)v * p.K + s] != 0u;
         for (uint32_t s = 1; s < p.S1 && !keep; s++) keep |= conc[(size_t)v * p.S1 + s] != 0;
-        if (keep) set_bit(sp.act_bm[sp.c], v);
+        if (keep) set_bit(act_cur(sp), v);
     }
 }
 

@@ -15,13 +15,21 @@ namespace {
 // Per-lane words of a warp's current group, kept in shared memory so that
 // the lane running an item can read the words of the item's lane.
 enum : int {
-    F_OCC, F_M, F_P, F_WK, F_BS,     // own word: content, movers down / up, work and base of the producing pass
-    F_LOCC, F_LP, F_LWK, F_LBS,      // lower neighbour's word (previous word of the row in the Z sweep)
-    F_HOCC, F_HM, F_HWK, F_HBS,      // upper neighbour's word (next word of the row in the Z sweep)
-    F_OLD, F_OWK, F_OBS, F_Y, F_KK,  // old destination word, this pass's work and base, the lane's row and word
-    F_VROW, F_CODE,                  // first voxel of the lane's row, the word's uniform region code (or 0)
+    // fields are stored in pairs (even, odd) read together: lane i's pair p is the uint2 at p * 32 + i
+    F_Y, F_KK,        // the lane's row and word
+    F_VROW, F_CODE,   // first voxel of the lane's row, the word's uniform region code (or 0)
+    F_OBS, F_OWK,     // this pass's base and work
+    F_BS, F_WK,       // own word: base and work of the producing pass
+    F_LBS, F_LWK,     // lower neighbour's word (previous word of the row in the Z sweep): base, work
+    F_HBS, F_HWK,     // upper neighbour's word (next word of the row in the Z sweep): base, work
+    F_LOCC, F_LP,     // lower neighbour: content, movers up
+    F_HOCC, F_HM,     // upper neighbour: content, movers down
+    F_M, F_P,         // own word: movers down / up
+    F_OCC, F_OLD,     // own content, old destination word
     NF
 };
+// u32 index of field F of lane i
+__device__ __forceinline__ int fi(int F, int i) { return (F >> 1) * 64 + 2 * i + (F & 1); }
 constexpr int LIST = 1024;  // one group holds at most 32 words x 32 bits
 
 }  // namespace
@@ -89,6 +97,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     const uint32_t S1 = P.T.S1, NC = P.T.NC;
     uint32_t* f = sm + (size_t)w * stream_warp_words();  // [NF][32]
     uint32_t* acc = f + NF * 32;                            // [3][32]: content, movers down, movers up
+    // field pair (F, F + 1) of lane i, F even
+    auto fpair = [&](int F, int i) -> uint2 { return reinterpret_cast<const uint2*>(f)[(F >> 1) * 32 + i]; };
     uint16_t* list = reinterpret_cast<uint16_t*>(acc + 96);
     uint32_t* s_diag = sm + (size_t)NW * stream_warp_words();  // [PD_N]
     uint32_t* s_thr = s_diag + PD_N;
@@ -109,7 +119,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     __syncthreads();
     const bool zero_order = P.T.n_zero_order != 0u;
     const bool all_react = zero_order || P.reservoir != nullptr;
-    auto trow = [&](uint32_t a, uint32_t b) -> const uint32_t* { return thr + ((size_t)a * NC + b) * S1; };
+    auto trow = [&](uint32_t a, uint32_t b) -> const uint32_t* { return thr + (a * NC + b) * S1; };  // < 2^32 entries
 
     const uint32_t TW = gridDim.x * NW;
     // groups from the pass's counter (one atomic per group, fetched a group ahead), else round-robin
@@ -148,8 +158,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                 own_occ = acc[lane];
                 own_m = acc[32 + lane];
                 own_p = acc[64 + lane];
-                own_wk = f[F_OWK * 32 + lane];
-                own_bs = f[F_OBS * 32 + lane];
+                own_wk = f[fi(F_OWK, lane)];
+                own_bs = f[fi(F_OBS, lane)];
                 const uint32_t u_occ = __shfl_up_sync(0xffffffffu, own_occ, 1), u_p = __shfl_up_sync(0xffffffffu, own_p, 1),
                                u_wk = __shfl_up_sync(0xffffffffu, own_wk, 1), u_bs = __shfl_up_sync(0xffffffffu, own_bs, 1);
                 const uint32_t d_occ = __shfl_down_sync(0xffffffffu, own_occ, 1), d_m = __shfl_down_sync(0xffffffffu, own_m, 1),
@@ -218,8 +228,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                     acc[lane] = 0u;
                     acc[32 + lane] = 0u;
                     acc[64 + lane] = 0u;
-                    f[F_OWK * 32 + lane] = 0u;
-                    f[F_OBS * 32 + lane] = (uint32_t)G.rbase;
+                    f[fi(F_OWK, lane)] = 0u;
+                    f[fi(F_OBS, lane)] = (uint32_t)G.rbase;
                 } else if (valid) {
                     if constexpr (PP == 3) {
                         P.odst[wo] = 0u;
@@ -243,29 +253,22 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                 __syncwarp();
                 return;
             }
-            f[F_OCC * 32 + lane] = own_occ;
-            f[F_M * 32 + lane] = own_m;
-            f[F_P * 32 + lane] = own_p;
-            f[F_WK * 32 + lane] = own_wk;
-            f[F_BS * 32 + lane] = own_bs;
-            f[F_LOCC * 32 + lane] = lo_occ;
-            f[F_LP * 32 + lane] = lo_p;
-            f[F_LWK * 32 + lane] = lo_wk;
-            f[F_LBS * 32 + lane] = lo_bs;
-            f[F_HOCC * 32 + lane] = hi_occ;
-            f[F_HM * 32 + lane] = hi_m;
-            f[F_HWK * 32 + lane] = hi_wk;
-            f[F_HBS * 32 + lane] = hi_bs;
-            f[F_OLD * 32 + lane] = old;
-            f[F_Y * 32 + lane] = (uint32_t)y;
-            f[F_KK * 32 + lane] = (uint32_t)kk;
-            f[F_VROW * 32 + lane] = ((uint32_t)x * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z;
             {
                 // the word's uniform region code; bit 8: its whole window lies inside the lattice, so
                 // every neighbour of its voxels has that code too
                 const uint32_t uc = (rd.flags & 1u) ? 1u : (SP.wcode && valid) ? (uint32_t)SP.wcode[wo] : 0u;
                 const bool inner = x > 0 && x + 1 < X && y > 0 && y + 1 < Y && kk > 0 && kk + 1 < (int)Wz;
-                f[F_CODE * 32 + lane] = uc | (uc && inner ? 0x100u : 0u);
+                uint2* fp2 = reinterpret_cast<uint2*>(f) + lane;
+                fp2[(F_OCC >> 1) * 32] = make_uint2(own_occ, old);
+                fp2[(F_M >> 1) * 32] = make_uint2(own_m, own_p);
+                fp2[(F_BS >> 1) * 32] = make_uint2(own_bs, own_wk);
+                fp2[(F_LOCC >> 1) * 32] = make_uint2(lo_occ, lo_p);
+                fp2[(F_LBS >> 1) * 32] = make_uint2(lo_bs, lo_wk);
+                fp2[(F_HOCC >> 1) * 32] = make_uint2(hi_occ, hi_m);
+                fp2[(F_HBS >> 1) * 32] = make_uint2(hi_bs, hi_wk);
+                fp2[(F_Y >> 1) * 32] = make_uint2((uint32_t)y, (uint32_t)kk);
+                fp2[(F_VROW >> 1) * 32] =
+                    make_uint2(((uint32_t)x * (uint32_t)Y + (uint32_t)y) * (uint32_t)Z, uc | (uc && inner ? 0x100u : 0u));
             }
             // List the work bits in three classes, so that the lanes of a warp mostly run the same
             // path: voxels with a record of the previous pass whose content does not change along
@@ -287,8 +290,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
             const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31), total = __shfl_sync(0xffffffffu, inw, 31);
             const uint32_t total_a = tot & 0xFFFFu, total_ab = total_a + (tot >> 16);
             const uint32_t ex = incl - (na | (nb << 16)), exa = ex & 0xFFFFu, exb = ex >> 16, exw = inw - nw;
-            f[F_OWK * 32 + lane] = work;
-            f[F_OBS * 32 + lane] = (uint32_t)G.rbase + exw;
+            reinterpret_cast<uint2*>(f)[(F_OBS >> 1) * 32 + lane] = make_uint2((uint32_t)G.rbase + exw, work);
             acc[lane] = 0u;
             acc[32 + lane] = 0u;
             acc[64 + lane] = 0u;
@@ -322,10 +324,11 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                 const uint32_t e = list[t];
                 const int i = (int)(e >> 5), b = (int)(e & 31u);
                 const uint32_t bit = 1u << b;
-                const int yy = (int)f[F_Y * 32 + i], zz = 32 * (int)f[F_KK * 32 + i] + b;
-                const uint32_t v = f[F_VROW * 32 + i] + (uint32_t)zz;
-                const uint32_t uc = f[F_CODE * 32 + i];
-                const uint32_t ri = f[F_OBS * 32 + i] + below(f[F_OWK * 32 + i], bit);  // this pass's record of the item
+                const uint2 f_yk = fpair(F_Y, i), f_vc = fpair(F_VROW, i), f_ow = fpair(F_OBS, i);
+                const int yy = (int)f_yk.x, zz = 32 * (int)f_yk.y + b;
+                const uint32_t v = f_vc.x + (uint32_t)zz;
+                const uint32_t uc = f_vc.y;
+                const uint32_t ri = f_ow.x + below(f_ow.y, bit);  // this pass's record of the item
                 if constexpr (PP == 0) {
                     const Vox<K> own = ld_vox_g<K>(P.src + (rd.base + v) * K);
                     const U4 b0 = d_philox(v, frame, 0u, 0u, k0, k1);
@@ -336,41 +339,46 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                     if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
                     if (d >> 16) atomicOr(acc + 64 + i, bit);
                 } else {
-                    const uint32_t occ = f[F_OCC * 32 + i];
+                    const uint32_t occ = f[fi(F_OCC, i)];
+                    const uint2 f_bw = fpair(F_BS, i), f_mp = fpair(F_M, i);
                     Vox<K> own = vox_zero<K>(), lo = vox_zero<K>(), hi = vox_zero<K>();
                     uint32_t dme = 0u, dlo = 0u, dhi = 0u;
                     uint4 tw = make_uint4(0u, 0u, 0u, 0u);
                     const bool own_in = (occ & bit) != 0u;
                     if (own_in) {
-                        rec_load<K, !(CH && PP == 3)>(rin, f[F_BS * 32 + i] + below(f[F_WK * 32 + i], bit), own, tw);
+                        rec_load<K, !(CH && PP == 3)>(rin, f_bw.x + below(f_bw.y, bit), own, tw);
                         dme = tw.x;
                     }
                     // a neighbour's record is needed when it sends to this voxel or receives from it
                     bool need_lo, need_hi;
                     uint32_t ilo, ihi;
                     if constexpr (PP == 3) {
-                        const uint32_t m = f[F_M * 32 + i], p = f[F_P * 32 + i];
+                        const uint32_t m = f_mp.x, p = f_mp.y;
                         if (b > 0) {
                             const uint32_t lb = bit >> 1;
                             need_lo = (occ & lb) && ((m & bit) || (p & lb));
-                            ilo = f[F_BS * 32 + i] + below(f[F_WK * 32 + i], lb);
+                            ilo = f_bw.x + below(f_bw.y, lb);
                         } else {
-                            need_lo = (f[F_LOCC * 32 + i] >> 31) && ((m & bit) || (f[F_LP * 32 + i] >> 31));
-                            ilo = f[F_LBS * 32 + i] + below(f[F_LWK * 32 + i], 0x80000000u);
+                            const uint2 f_lo = fpair(F_LOCC, i), f_lb = fpair(F_LBS, i);
+                            need_lo = (f_lo.x >> 31) && ((m & bit) || (f_lo.y >> 31));
+                            ilo = f_lb.x + below(f_lb.y, 0x80000000u);
                         }
                         if (b < 31) {
                             const uint32_t hb = bit << 1;
                             need_hi = (occ & hb) && ((p & bit) || (m & hb));
-                            ihi = f[F_BS * 32 + i] + below(f[F_WK * 32 + i], hb);
+                            ihi = f_bw.x + below(f_bw.y, hb);
                         } else {
-                            need_hi = (f[F_HOCC * 32 + i] & 1u) && ((p & bit) || (f[F_HM * 32 + i] & 1u));
-                            ihi = f[F_HBS * 32 + i];
+                            const uint2 f_hi = fpair(F_HOCC, i);
+                            need_hi = (f_hi.x & 1u) && ((p & bit) || (f_hi.y & 1u));
+                            ihi = f[fi(F_HBS, i)];
                         }
                     } else {
-                        need_lo = (f[F_LOCC * 32 + i] & bit) && ((f[F_M * 32 + i] | f[F_LP * 32 + i]) & bit);
-                        need_hi = (f[F_HOCC * 32 + i] & bit) && ((f[F_P * 32 + i] | f[F_HM * 32 + i]) & bit);
-                        ilo = f[F_LBS * 32 + i] + below(f[F_LWK * 32 + i], bit);
-                        ihi = f[F_HBS * 32 + i] + below(f[F_HWK * 32 + i], bit);
+                        const uint2 f_lo = fpair(F_LOCC, i), f_hi = fpair(F_HOCC, i);
+                        const uint2 f_lb = fpair(F_LBS, i), f_hb = fpair(F_HBS, i);
+                        need_lo = (f_lo.x & bit) && ((f_mp.x | f_lo.y) & bit);
+                        need_hi = (f_hi.x & bit) && ((f_mp.y | f_hi.y) & bit);
+                        ilo = f_lb.x + below(f_lb.y, bit);
+                        ihi = f_hb.x + below(f_hb.y, bit);
                     }
                     if (need_lo) {
                         uint4 tl;
@@ -449,25 +457,25 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                     SP.out.mv_m[wo] = acc[32 + lane];
                     SP.out.mv_p[wo] = acc[64 + lane];
                     SP.out.work[wo] = work;
-                    SP.out.base[wo] = f[F_OBS * 32 + lane];
+                    SP.out.base[wo] = f[fi(F_OBS, lane)];
                 } else if constexpr (PP == 3) {
                     P.odst[wo] = acc[lane];
                     // voxels the destination held that end the frame empty get zeros
                     for (uint32_t bits = old & ~acc[lane]; bits; bits &= bits - 1u)
-                        st_vox_g<K>(P.dst + (rd.base + f[F_VROW * 32 + lane] + (uint32_t)zb + (uint32_t)(__ffs((int)bits) - 1)) * K,
+                        st_vox_g<K>(P.dst + (rd.base + f[fi(F_VROW, lane)] + (uint32_t)zb + (uint32_t)(__ffs((int)bits) - 1)) * K,
                                     vox_zero<K>());
                     if (SP.fuse) {
                         SP.out.mv_m[wo] = acc[32 + lane];
                         SP.out.mv_p[wo] = acc[64 + lane];
                         SP.out.work[wo] = work;
-                        SP.out.base[wo] = f[F_OBS * 32 + lane];
+                        SP.out.base[wo] = f[fi(F_OBS, lane)];
                     }
                 } else if constexpr (!CH) {
                     SP.out.occ[wo] = acc[lane];
                     SP.out.mv_m[wo] = acc[32 + lane];
                     SP.out.mv_p[wo] = acc[64 + lane];
                     SP.out.work[wo] = work;
-                    SP.out.base[wo] = f[F_OBS * 32 + lane];
+                    SP.out.base[wo] = f[fi(F_OBS, lane)];
                 }
             }
             __syncwarp();
@@ -537,6 +545,30 @@ __global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
         const uint32_t v = t.x, w3 = t.y, rv = t.z;
         const RepDesc rd = P.reps[t.w];
         const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
+        // what the store and the next frame's x-decisions need besides the SSA's result (the
+        // voxel's bitmap word, region codes, threshold rows, next frame's Philox block) is loaded and
+        // computed first, so that it is ready when the SSA ends
+        const uint32_t Y = rd.Y, Z = rd.Z, X = rd.X;
+        const uint32_t x = v / (Y * Z), rem = v - x * (Y * Z), y = rem / Z, z = rem - y * Z;
+        const uint64_t wo = rd.obase + ((uint64_t)x * Y + y) * rd.Wz + (z >> 5);
+        const uint32_t bit = 1u << (z & 31u);
+        const uint32_t nf = frame + 1u;
+        const uint32_t* tlo = nullptr;
+        const uint32_t* thi = nullptr;
+        U4 b0{0u, 0u, 0u, 0u};
+        if (SP.fuse) {
+            const uint32_t uc = (rd.flags & 1u) ? 1u : SP.wcode ? (uint32_t)SP.wcode[wo] : 0u;
+            const uint8_t* rpad = P.region_pad + rd.rbase;
+            auto code = [&](int xx, int yy, int zz) -> uint32_t {
+                if ((unsigned)xx >= X || (unsigned)yy >= Y || (unsigned)zz >= Z) return 0u;
+                if (uc) return uc;
+                return rpad[((uint64_t)xx * Y + (uint64_t)yy) * rd.Zr + (uint64_t)zz + 2u];
+            };
+            const uint32_t rs = code((int)x, (int)y, (int)z);
+            tlo = P.T.thr + ((size_t)rs * NC + code((int)x - 1, (int)y, (int)z)) * S1;
+            thi = P.T.thr + ((size_t)rs * NC + code((int)x + 1, (int)y, (int)z)) * S1;
+            b0 = d_philox(v, nf, 0u, 0u, k0, k1);
+        }
         react_voxel_warp<K>(r, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, TS, my0, s_diag, w3);
         __syncwarp();
         if (lane == 0u) {
@@ -546,25 +578,9 @@ __global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
                     my0[s] = 0;
                 }
             if (!vox_empty<K>(r)) {
-                const uint32_t Y = rd.Y, Z = rd.Z, X = rd.X;
-                const uint32_t x = v / (Y * Z), rem = v - x * (Y * Z), y = rem / Z, z = rem - y * Z;
-                const uint64_t wo = rd.obase + ((uint64_t)x * Y + y) * rd.Wz + (z >> 5);
-                const uint32_t bit = 1u << (z & 31u);
                 st_vox_g<K>(P.dst + (rd.base + v) * K, r);
                 atomicOr(P.odst + wo, bit);
                 if (SP.fuse) {
-                    const uint32_t uc = (rd.flags & 1u) ? 1u : SP.wcode ? (uint32_t)SP.wcode[wo] : 0u;
-                    const uint8_t* rpad = P.region_pad + rd.rbase;
-                    auto code = [&](int xx, int yy, int zz) -> uint32_t {
-                        if ((unsigned)xx >= X || (unsigned)yy >= Y || (unsigned)zz >= Z) return 0u;
-                        if (uc) return uc;
-                        return rpad[((uint64_t)xx * Y + (uint64_t)yy) * rd.Zr + (uint64_t)zz + 2u];
-                    };
-                    const uint32_t nf = frame + 1u;
-                    const U4 b0 = d_philox(v, nf, 0u, 0u, k0, k1);
-                    const uint32_t rs = code((int)x, (int)y, (int)z);
-                    const uint32_t* tlo = P.T.thr + ((size_t)rs * NC + code((int)x - 1, (int)y, (int)z)) * S1;
-                    const uint32_t* thi = P.T.thr + ((size_t)rs * NC + code((int)x + 1, (int)y, (int)z)) * S1;
                     const uint32_t d = decide_moves<K>(r, v, nf, 0u, tlo, thi, k0, k1, b0.x);
                     rec_store<K>(SP.rec_out, ri, r, make_uint4(d, b0.y, b0.z, b0.w));
                     if (d & 0xFFFFu) atomicOr(SP.out.mv_m + wo, bit);

@@ -221,7 +221,7 @@ __device__ __forceinline__ uint32_t decide_moves(const Vox<K>& c, uint32_t v, ui
         if ((tm | tp) == 0u) continue;
         const uint32_t u = s == 0u ? w0 : sweep_word(d_philox(v, frame, s, 0u, k0, k1), sweep);
         if (u < tm) mask |= 1u << s;
-        else if ((uint64_t)u < (uint64_t)tm + tp) mask |= 1u << (16 + s);
+        else if (u - tm < tp) mask |= 1u << (16 + s);  // tm <= u < tm + tp, without the 33-bit sum
     }
     return mask;
 }
