@@ -194,10 +194,14 @@ struct DeviceProd {
     uint32_t seg_len = 0;
     uint64_t cur_seed = 0;
     bool seed_set = false;
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;  // two frames, parities 0 then 1
     int graph_cfg = -1;
+    cudaGraphExec_t graph1[2] = {nullptr, nullptr};  // one frame of parity 0 / 1
+    int graph1_cfg[2] = {-1, -1};
     ~DeviceProd() {
         if (graph) cudaGraphExecDestroy(graph);
+        for (cudaGraphExec_t g1 : graph1)
+            if (g1) cudaGraphExecDestroy(g1);
         if (h_counts) cudaFreeHost(h_counts);
         if (h_frames) cudaFreeHost(h_frames);
         for (cudaEvent_t e : frame_ev)
@@ -661,6 +665,19 @@ static void set_attrs(const DeviceProd* d, const KernelCfg& cfg) {
     CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
 }
 
+// Captured frame graphs hold the launch parameters of the current configuration and precision.
+static void drop_graphs(DeviceProd* d) {
+    if (d->graph) {
+        cudaGraphExecDestroy(d->graph);
+        d->graph = nullptr;
+    }
+    for (cudaGraphExec_t& g1 : d->graph1)
+        if (g1) {
+            cudaGraphExecDestroy(g1);
+            g1 = nullptr;
+        }
+}
+
 static void set_cfg(DeviceProd* d, int idx) {
     const KernelCfg& cfg = all_cfgs()[idx];
     if (cfg.kind == KIND_STREAM && stream_variant_fused(cfg.variant) && !fused_fits(d))
@@ -678,10 +695,7 @@ static void set_cfg(DeviceProd* d, int idx) {
         if (prev >= 0) build_items(d);
         throw;
     }
-    if (d->graph) {
-        cudaGraphExecDestroy(d->graph);
-        d->graph = nullptr;
-    }
+    drop_graphs(d);
 }
 
 // Occupancy bitmap of one replicate's slot buffer: one warp per (x, y) row,
@@ -1093,9 +1107,24 @@ static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched) {
     d->xdec_valid = false;
     if (kind == KIND_STREAM && !xdec_ok) launch_stream_pass0(d);
     uint32_t k = 0;
+    // a single frame of parity p, from its own captured graph (a step call of one frame, as the
+    // reference's per-frame step makes, costs one graph launch instead of three kernel launches)
+    auto single = [&](int p) {
+        if (!d->graph1[p] || d->graph1_cfg[p] != d->cfg_index) {
+            if (d->graph1[p]) { cudaGraphExecDestroy(d->graph1[p]); d->graph1[p] = nullptr; }
+            cudaGraph_t g;
+            CS_CUDA(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
+            launch_frame(d, p, -1);
+            CS_CUDA(cudaStreamEndCapture(d->stream, &g));
+            CS_CUDA(cudaGraphInstantiate(&d->graph1[p], g, 0));
+            cudaGraphDestroy(g);
+            d->graph1_cfg[p] = d->cfg_index;
+        }
+        CS_CUDA(cudaGraphLaunch(d->graph1[p], d->stream));
+    };
     if (batched) {
         if (d->cur == 1 && k < n) {
-            launch_frame(d, 1, -1);
+            single(1);
             d->cur = 0;
             k++;
         }
@@ -1117,7 +1146,7 @@ static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched) {
             }
         }
         if (k < n) {
-            launch_frame(d, 0, -1);
+            single(0);
             d->cur = 1;
             k++;
         }
@@ -1162,7 +1191,7 @@ void prod_step(DeviceProd* d, uint32_t n_steps, uint64_t seed, int precision, ui
     prod_seed(d, seed);
     if (d->T.precision != precision) {
         d->T.precision = precision;
-        if (d->graph) { cudaGraphExecDestroy(d->graph); d->graph = nullptr; }
+        drop_graphs(d);
     }
     std::vector<uint64_t> sample_frames;
     if (write_freq)
@@ -1324,7 +1353,7 @@ void prod_ensemble_step(DeviceProd* d, uint32_t n_steps, bool batched, uint64_t 
 void prod_set_precision(DeviceProd* d, int precision) {
     if (d->T.precision != precision) {
         d->T.precision = precision;
-        if (d->graph) { cudaGraphExecDestroy(d->graph); d->graph = nullptr; }
+        drop_graphs(d);
     }
 }
 

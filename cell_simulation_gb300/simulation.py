@@ -117,6 +117,9 @@ class Simulation:
             N.check(self._lib.cs_create(C.byref(lattice_params.to_c()), C.byref(self._h)))
         self.stats: deque[SolverStatisticSample] = deque()
         self.rng_mode: int | None = None
+        # species count (+1) of the prepared model, read once per preparation for counts();
+        # every call that can change the model clears it
+        self._s1: int | None = None
 
     @classmethod
     def from_file(cls, path: str, placement_seed: int = 0) -> "Simulation":
@@ -149,20 +152,24 @@ class Simulation:
         N.check(self._lib.cs_seed_placement(self._h, seed))
 
     def add_region(self, region: N.RegionDescC, diffusion_rate: float) -> None:
+        self._s1 = None
         N.check(self._lib.cs_add_region(self._h, C.byref(region), diffusion_rate))
 
     def prepare_regions(self) -> None:
         N.check(self._lib.cs_prepare_regions(self._h))
 
     def add_particle_count(self, name, to_region, count, logging, is_reservoir) -> None:
+        self._s1 = None
         N.check(self._lib.cs_add_particle_count(self._h, name.encode(), to_region.encode(), count, int(logging),
                                                 int(is_reservoir)))
 
     def add_particle_concentration(self, name, to_region, concentration, logging, is_reservoir) -> None:
+        self._s1 = None
         N.check(self._lib.cs_add_particle_concentration(self._h, name.encode(), to_region.encode(), concentration,
                                                         int(logging), int(is_reservoir)))
 
     def fill_region(self, name, to_region, logging) -> None:
+        self._s1 = None
         N.check(self._lib.cs_fill_region(self._h, name.encode(), to_region.encode(), int(logging)))
 
     def set_diffusion_rate(self, region, diffusion_rate) -> None:
@@ -179,6 +186,7 @@ class Simulation:
                                                           to_region.encode(), transition_rate))
 
     def add_reaction(self, reactants: Iterable[str], products: Iterable[str], k: float) -> None:
+        self._s1 = None
         re = [r.encode() for r in reactants]
         pr = [p.encode() for p in products]
         ra = (C.c_char_p * max(len(re), 1))(*re)
@@ -226,6 +234,7 @@ class Simulation:
 
     def set_tables(self, n_regions, n_species, n_reactions, regions, diffusion, stoich, reactants, rates,
                    reservoir=None) -> None:
+        self._s1 = None
         arrs = [np.ascontiguousarray(a, dt) for a, dt in ((regions, np.uint32), (diffusion, np.float32),
                                                             (stoich, np.int32), (reactants, np.uint32),
                                                             (rates, np.float32))]
@@ -254,8 +263,10 @@ class Simulation:
     # ---------------------------------------------------------------- device
     def prepare_for_gpu(self, rng_mode: int = N.RNG_PHILOX, device: int = 0) -> None:
         """Simulation::prepare_for_gpu, src/simulation.rs:152-208."""
+        self._s1 = None
         N.check(self._lib.cs_prepare_for_gpu(self._h, rng_mode, device))
         self.rng_mode = rng_mode
+        self._s1 = self.info().n_species + 1
 
     def step(self, itimes: Sequence[int], write_freq: int = 0) -> None:
         """Simulation::step (src/simulation.rs:99-150) for len(itimes) frames with the reference RNG."""
@@ -320,8 +331,8 @@ class Simulation:
 
     def counts(self) -> np.ndarray:
         """Species counts (StatisticsGroup buffer 0, src/statistics.rs:11-69)."""
-        # the species count is read every call: cs_set_tables may change it between preparations
-        out = np.zeros(self.info().n_species + 1, np.int64)
+        s1 = self._s1 if self._s1 is not None else self.info().n_species + 1
+        out = np.zeros(s1, np.int64)
         N.check(self._lib.cs_get_counts(self._h, N.ptr(out, C.c_int64)))
         return out
 
