@@ -128,9 +128,29 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         if (lane == 0) q = atomicAdd(SP.queue, 1u);
         return __shfl_sync(0xffffffffu, q, 0);
     };
-    uint32_t g = SP.queue ? fetch() : blockIdx.x * NW + (uint32_t)w;
+    // groups come from the pass's counter in batches of SP.batch consecutive groups (one atomic
+    // per batch: same-address atomics serialise in L2), the next batch fetched while the last group
+    // of the current one runs
+    uint32_t g, g_end;
+    if (SP.queue) {
+        g = fetch() * SP.batch;
+        g_end = g + SP.batch;
+    } else {
+        g = blockIdx.x * NW + (uint32_t)w;
+        g_end = g + 1u;
+    }
     while (g < SP.n_groups) {
-        const uint32_t g_next = SP.queue ? fetch() : g + TW;
+        uint32_t g_next, g_next_end;
+        if (g + 1u < g_end) {
+            g_next = g + 1u;
+            g_next_end = g_end;
+        } else if (SP.queue) {
+            g_next = fetch() * SP.batch;
+            g_next_end = g_next + SP.batch;
+        } else {
+            g_next = g + TW;
+            g_next_end = g_next + 1u;
+        }
         const WordGroup G = SP.groups[g];
         const RepDesc rd = P.reps[G.rep];
         const int X = (int)rd.X, Y = (int)rd.Y, Z = (int)rd.Z;
@@ -487,6 +507,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
             sweep(std::integral_constant<int, PASS>{}, std::false_type{});
         }
         g = g_next;
+        g_end = g_next_end;
     }
     __syncthreads();
     for (int i = tid; i < PD_N; i += NT)

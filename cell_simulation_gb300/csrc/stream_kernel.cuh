@@ -81,6 +81,7 @@ struct StreamParams {
     const WordGroup* groups;
     uint32_t n_groups;
     uint32_t* queue;  // group counter of this pass (zero at launch); null: groups dealt round-robin
+    uint32_t batch;   // consecutive groups taken per increment of the counter (at least 1)
     // per bitmap word: the region code shared by every lattice voxel of the word's window
     // (rows x-1..x+1, y-1..y+1, z from 32k-1 to 32k+32), or 0; null for one-region replicates
     const uint8_t* wcode;
