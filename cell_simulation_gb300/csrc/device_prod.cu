@@ -181,6 +181,9 @@ struct DeviceProd {
     int xdec_cur = 0, xdec_cfg = -1;
     uint64_t seed_epoch = 0;  // advanced whenever the Philox keys change
     uint64_t next_frame = 0;  // host copy of the frame number in stepbuf[cur]
+    // stepbuf[cur] holds next_frame in stream order: it was uploaded, and every frame since wrote
+    // its successor's number (a step call that continues from there uploads nothing)
+    bool frame_known = false;
     unsigned long long* h_counts = nullptr;  // pinned read-back buffer of the counts (n_rep * S1)
     // pinned slots of the first frame number of each step call, copied in stream order; a slot
     // is reused once its event shows that its copy has run
@@ -1037,6 +1040,7 @@ void prod_set_lattice(DeviceProd* d, const Model& m, const uint32_t* slots) {
     }
     CS_CUDA(cudaStreamSynchronize(d->stream));
     d->cur = 0;
+    d->frame_known = false;
     // the next frame has parity 0 whatever the last one had: its work counters start at zero
     CS_CUDA(cudaMemset(d->counters.p, 0, d->counters.bytes()));
     CS_CUDA(cudaMemcpy(d->slots[0].p, s8.data(), s8.size(), cudaMemcpyHostToDevice));
@@ -1093,6 +1097,7 @@ static void run_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched)
     CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, &f32, 4, cudaMemcpyHostToDevice, d->stream));
     CS_CUDA(cudaStreamSynchronize(d->stream));
     d->next_frame = frame0;
+    d->frame_known = true;
     run_frames_nosync(d, n, batched);
 }
 
@@ -1177,6 +1182,7 @@ static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched) {
 // host-to-device input, like the reference's per-frame itime write), in
 // stream order and without a host wait.
 static void upload_frame(DeviceProd* d, uint64_t frame0) {
+    if (d->frame_known && d->next_frame == frame0) return;
     if (!d->h_frames) {
         CS_CUDA(cudaMallocHost(&d->h_frames, DeviceProd::kFrameSlots * sizeof(uint32_t)));
         for (cudaEvent_t& e : d->frame_ev) CS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1188,6 +1194,7 @@ static void upload_frame(DeviceProd* d, uint64_t frame0) {
     CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, d->h_frames + s, 4, cudaMemcpyHostToDevice, d->stream));
     CS_CUDA(cudaEventRecord(d->frame_ev[s], d->stream));
     d->next_frame = frame0;
+    d->frame_known = true;
 }
 
 void prod_step(DeviceProd* d, uint32_t n_steps, uint64_t seed, int precision, uint64_t frame0, uint32_t write_freq,
@@ -1430,6 +1437,7 @@ float prod_time_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched)
         CS_CUDA(cudaMemcpyAsync(d->stepbuf.p + d->cur, &f32, 4, cudaMemcpyHostToDevice, d->stream));
         CS_CUDA(cudaStreamSynchronize(d->stream));
         d->next_frame = frame0;
+        d->frame_known = true;
         CS_CUDA(cudaEventRecord(a, d->stream));
         run_frames_nosync(d, n, batched);
         CS_CUDA(cudaEventRecord(b, d->stream));
@@ -1499,6 +1507,7 @@ int prod_autotune(DeviceProd* d, uint32_t frames, uint64_t frame0, bool batched,
         CS_CUDA(cudaStreamSynchronize(d->stream));
         d->cur = cur0;
         d->occ_valid = false;
+        d->frame_known = false;
     };
     const auto& c = all_cfgs();
     int best = -1;

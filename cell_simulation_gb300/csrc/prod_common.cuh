@@ -480,12 +480,6 @@ __device__ __forceinline__ bool react_voxel_inline(Vox<K>& c, uint32_t resv, uin
     return fired;
 }
 
-// Element q (0..3) of a four-element register array, by selects (no local memory).
-template <typename T>
-__device__ __forceinline__ T pick4(const T (&a)[4], uint32_t q) {
-    return q == 0u ? a[0] : q == 1u ? a[1] : q == 2u ? a[2] : a[3];
-}
-
 // Index of set bit k (0-based) of the 128-bit mask (m0, m1); k < popcount.
 __device__ __forceinline__ int nth_bit(unsigned long long m0, unsigned long long m1, uint32_t k) {
     uint32_t off = 0u;
@@ -517,17 +511,22 @@ __device__ __forceinline__ int nth_bit(unsigned long long m0, unsigned long long
 // The SSA of react_voxel_inline run by a whole warp: every lane calls it with
 // the same voxel and gets the same result.  Lanes evaluate the candidate
 // reactions' propensities in parallel (lane l takes candidates l, l + 32, ...
-// in index order); every sum and running sum is then formed in candidate
-// order with one value shuffled in at a time, so every binary32 and binary64
-// result, and so the lattice, equals react_voxel_inline's.  Counters and
-// species deltas are updated by lane 0.
+// in index order) into the warp's scratch `ws` (shared memory, 2 KB); lane 0
+// then forms the running sums in candidate order, in binary32 and, when the
+// selection needs it, binary64, exactly as react_voxel_inline does, and the
+// selected candidate is the first whose running sum exceeds the target (a
+// ballot over the stored sums), so every result, and so the lattice, equals
+// react_voxel_inline's.  Counters and species deltas are updated by lane 0.
 template <int K>
 __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0,
                                                  uint32_t k1, float mult, uint32_t rep, const ProdTables& T,
-                                                 int32_t* s_delta, uint32_t* s_diag, uint32_t w3) {
+                                                 int32_t* s_delta, uint32_t* s_diag, uint32_t w3, float* ws) {
     const uint32_t lane = threadIdx.x & 31u;
     if (T.R == 0) return false;
     if (lane == 0u) atomicAdd(s_diag + PD_SSA_VOXELS, 1u);
+    float* const a_s = ws;                                     // [128] propensities in candidate order
+    float* const p_s = ws + 128;                               // [128] their binary32 running sums
+    double* const pd_s = reinterpret_cast<double*>(ws + 256);  // [128] binary64 running sums
     uint32_t n = vox_n<K>(c);
     double td = 0.0;
     float tf = 0.0f;
@@ -537,27 +536,38 @@ __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint3
         unsigned long long c0, c1;
         candidates<K>(T, c, n, resv, c0, c1);
         const uint32_t nc = (uint32_t)(__popcll(c0) + __popcll(c1));
-        // this lane's candidates (at most 128 reactions: four rounds) and their propensities
-        float ach[4];
-        int rch[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const uint32_t k = (uint32_t)q * 32u + lane;
-            rch[q] = k < nc ? nth_bit(c0, c1, k) : -1;
-            ach[q] = rch[q] >= 0 ? propensity<K>(T, (uint32_t)rch[q], c, resv, mult) : 0.0f;
+        const uint32_t rounds = (nc + 31u) >> 5;  // at most 128 reactions: four rounds
+        uint32_t bmax = 0u, bmin = 0x7f800000u;   // bit patterns of positive binary32 order like the values
+        for (uint32_t q = 0; q < rounds; q++) {
+            const uint32_t k = q * 32u + lane;
+            if (k < nc) {
+                const float a = propensity<K>(T, (uint32_t)nth_bit(c0, c1, k), c, resv, mult);
+                a_s[k] = a;
+                if (a > 0.0f) {
+                    bmax = max(bmax, __float_as_uint(a));
+                    bmin = min(bmin, __float_as_uint(a));
+                }
+            }
         }
-        float a0 = 0.0f, amax = 0.0f, amin = __int_as_float(0x7f800000);
+        __syncwarp();
+        if (lane == 0u) {
+            float run = 0.0f;
+            for (uint32_t k = 0; k < nc; k++) {
+                run = __fadd_rn(run, a_s[k]);
+                p_s[k] = run;
+            }
+        }
+        __syncwarp();
+        float a0, amax, amin;
         if (resv == 0u && n <= 1u) {
             const float* o = T.one + ((size_t)rep * T.S1 + (n ? vox_get<K>(c, 0) : 0u)) * 3;
             a0 = tab_ld(o);
             amax = tab_ld(o + 1);
             amin = tab_ld(o + 2);
         } else {
-            for (uint32_t k = 0; k < nc; k++) {
-                const float a = __shfl_sync(0xffffffffu, pick4(ach, k >> 5), k & 31u);
-                a0 = __fadd_rn(a0, a);
-                if (a > 0.0f) { amax = fmaxf(amax, a); amin = fminf(amin, a); }
-            }
+            a0 = nc ? p_s[nc - 1u] : 0.0f;
+            amax = __uint_as_float(__reduce_max_sync(0xffffffffu, bmax));
+            amin = __uint_as_float(__reduce_min_sync(0xffffffffu, bmin));
         }
         if (!(a0 > 0.0f)) break;
         U4 ph{0u, 0u, 0u, 0u};
@@ -579,33 +589,43 @@ __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint3
         const uint32_t w2 = ph.y;
         float u2 = __fmul_rn((float)(w2 >> 8), 0x1p-24f);
         bool use64 = (T.precision == 2) || (T.precision == 0 && amax > __fmul_rn(1e6f, amin));
-        int sel = -1;
-        int last_pos = -1;
+        // first candidate whose running sum exceeds the target; else the last one with a positive
+        // propensity (the sequential scan's last_pos)
+        int idx = -1;
         if (!use64) {
-            float target = __fmul_rn(u2, a0), run = 0.0f;
-            for (uint32_t k = 0; k < nc; k++) {
-                const float a = __shfl_sync(0xffffffffu, pick4(ach, k >> 5), k & 31u);
-                const int r = __shfl_sync(0xffffffffu, pick4(rch, k >> 5), k & 31u);
-                if (a > 0.0f) last_pos = r;
-                run = __fadd_rn(run, a);
-                if (target < run) { sel = r; break; }
+            const float target = __fmul_rn(u2, a0);
+            for (uint32_t q = 0; q < rounds && idx < 0; q++) {
+                const uint32_t k = q * 32u + lane;
+                const uint32_t b = __ballot_sync(0xffffffffu, k < nc && target < p_s[k]);
+                if (b) idx = (int)(q * 32u) + __ffs((int)b) - 1;
             }
         } else {
-            if (lane == 0u) atomicAdd(s_diag + PD_FP64_SEL, 1u);
-            double a0d = 0.0;
-            for (uint32_t k = 0; k < nc; k++)
-                a0d = __dadd_rn(a0d, (double)__shfl_sync(0xffffffffu, pick4(ach, k >> 5), k & 31u));
-            double target = __dmul_rn((double)u2, a0d), run = 0.0;
-            for (uint32_t k = 0; k < nc; k++) {
-                const float a = __shfl_sync(0xffffffffu, pick4(ach, k >> 5), k & 31u);
-                const int r = __shfl_sync(0xffffffffu, pick4(rch, k >> 5), k & 31u);
-                if (a > 0.0f) last_pos = r;
-                run = __dadd_rn(run, (double)a);
-                if (target < run) { sel = r; break; }
+            if (lane == 0u) {
+                atomicAdd(s_diag + PD_FP64_SEL, 1u);
+                double run = 0.0;
+                for (uint32_t k = 0; k < nc; k++) {
+                    run = __dadd_rn(run, (double)a_s[k]);
+                    pd_s[k] = run;
+                }
+            }
+            __syncwarp();
+            const double target = __dmul_rn((double)u2, nc ? pd_s[nc - 1u] : 0.0);
+            for (uint32_t q = 0; q < rounds && idx < 0; q++) {
+                const uint32_t k = q * 32u + lane;
+                const uint32_t b = __ballot_sync(0xffffffffu, k < nc && target < pd_s[k]);
+                if (b) idx = (int)(q * 32u) + __ffs((int)b) - 1;
             }
         }
-        if (sel < 0) sel = last_pos;
-        if (sel < 0) break;
+        if (idx < 0) {
+            for (int q = (int)rounds - 1; q >= 0 && idx < 0; q--) {
+                const uint32_t k = (uint32_t)q * 32u + lane;
+                const uint32_t b = __ballot_sync(0xffffffffu, k < nc && a_s[k] > 0.0f);
+                if (b) idx = q * 32 + 31 - __clz((int)b);
+            }
+        }
+        __syncwarp();  // the scratch is rewritten by the next event
+        if (idx < 0) break;
+        const int sel = nth_bit(c0, c1, (uint32_t)idx);
         // apply the change list, skipping the voxel's reservoir species (every lane, same result)
         const uint8_t* csp = T.rx_ch_sp + 8 * sel;
         const int8_t* cd = T.rx_ch_d + 8 * sel;
@@ -632,10 +652,10 @@ __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint3
                 int d = tab_ld(cd + j);
                 if (pass == 0) {
                     for (; d < 0; d++) {
-                        uint32_t idx = 0;
+                        uint32_t idx2 = 0;
                         for (uint32_t i = 0; i < n; i++)
-                            if (vox_get<K>(c, i) == s) idx = i;
-                        vox_set<K>(c, idx, vox_get<K>(c, n - 1));
+                            if (vox_get<K>(c, i) == s) idx2 = i;
+                        vox_set<K>(c, idx2, vox_get<K>(c, n - 1));
                         vox_set<K>(c, n - 1, 0u);
                         n--;
                     }
