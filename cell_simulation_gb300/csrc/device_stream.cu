@@ -526,14 +526,14 @@ __global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
     const uint32_t S1 = P.T.S1, NC = P.T.NC;
     const int tid = threadIdx.x;
     allow_next_launch();
-    float* const ws = reinterpret_cast<float*>(sm) + (size_t)(tid >> 5) * 512u;  // the warp's SSA scratch
-    int32_t* my = reinterpret_cast<int32_t*>(sm + 2048) + (size_t)tid * S1;
-    uint32_t* s_diag = sm + 2048 + (size_t)128 * S1;
+    float* const ws = reinterpret_cast<float*>(sm) + (size_t)(tid >> 5) * SSA_WARP_SCRATCH;  // the warp's SSA scratch
+    int32_t* my = reinterpret_cast<int32_t*>(sm + 4 * SSA_WARP_SCRATCH) + (size_t)tid * S1;
+    uint32_t* s_diag = sm + 4 * SSA_WARP_SCRATCH + (size_t)128 * S1;
     for (uint32_t s = 0; s < S1; s++) my[s] = 0;
     for (int i = tid; i < PD_N; i += 128) s_diag[i] = 0u;
     // the reaction tables in shared memory: each SSA walks them in long dependent chains
     const uint32_t R = P.T.R;
-    uint8_t* rx = reinterpret_cast<uint8_t*>(sm + 2048 + ((size_t)128 * S1 + PD_N + 3) / 4 * 4);
+    uint8_t* rx = reinterpret_cast<uint8_t*>(sm + 4 * SSA_WARP_SCRATCH + ((size_t)128 * S1 + PD_N + 3) / 4 * 4);
     unsigned long long* rm = reinterpret_cast<unsigned long long*>(rx);
     float* rate = reinterpret_cast<float*>(rx + 16 * S1);
     uint8_t* rre = rx + 16 * S1 + 4 * R;
@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
     const uint32_t n = *SP.ssa_count;
     // One warp per listed voxel: the lanes share its SSA (react_voxel_warp), lane 0 stores it.
     const uint32_t warps = gridDim.x * 4u, gw = blockIdx.x * 4u + ((uint32_t)tid >> 5), lane = (uint32_t)tid & 31u;
-    int32_t* my0 = reinterpret_cast<int32_t*>(sm + 2048) + (size_t)(tid - (int)lane) * S1;  // lane 0's deltas
+    int32_t* my0 = reinterpret_cast<int32_t*>(sm + 4 * SSA_WARP_SCRATCH) + (size_t)(tid - (int)lane) * S1;  // lane 0's deltas
     for (uint32_t j = gw; j < n; j += warps) {
         const uint32_t ri = SP.ssa_list[j];
         Vox<K> r;
@@ -617,10 +617,10 @@ __global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
         if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
 }
 
-// the four warps' SSA scratch (2 KB each), per-thread deltas, diagnostics, then the staged
-// tables (16 S1 + 23 R bytes)
+// the four warps' SSA scratch, per-thread deltas, diagnostics, then the staged tables (16 S1 +
+// 23 R bytes)
 size_t stream_ssa_smem(uint32_t S1, uint32_t R) {
-    return (size_t)2048 * 4 + ((size_t)128 * S1 + PD_N + 3) / 4 * 16 + (size_t)16 * S1 + (size_t)23 * R;
+    return (size_t)4 * SSA_WARP_SCRATCH * 4 + ((size_t)128 * S1 + PD_N + 3) / 4 * 16 + (size_t)16 * S1 + (size_t)23 * R;
 }
 
 static void launch_pdl(void* fn, int grid, int threads, size_t smem, cudaStream_t s, const StreamParams& SP);

@@ -508,15 +508,29 @@ __device__ __forceinline__ int nth_bit(unsigned long long m0, unsigned long long
     return (int)off;
 }
 
+// Byte positions [a, b) of a 64-bit word (0 <= a, b <= 8) as a bit mask.
+__device__ __forceinline__ uint64_t byte_run_mask(int a, int b) {
+    a = min(max(a, 0), 8);
+    b = min(max(b, 0), 8);
+    if (b <= a) return 0ull;
+    const uint64_t hi = b == 8 ? ~0ull : (1ull << (8 * b)) - 1ull;
+    return hi & ~((1ull << (8 * a)) - 1ull);  // a < 8 here
+}
+
+// Words of the per-warp shared scratch react_voxel_warp uses (4 KB).
+constexpr int SSA_WARP_SCRATCH = 1024;
+
 // The SSA of react_voxel_inline run by a whole warp: every lane calls it with
-// the same voxel and gets the same result.  Lanes evaluate the candidate
-// reactions' propensities in parallel (lane l takes candidates l, l + 32, ...
-// in index order) into the warp's scratch `ws` (shared memory, 2 KB); lane 0
-// then forms the running sums in candidate order, in binary32 and, when the
-// selection needs it, binary64, exactly as react_voxel_inline does, and the
-// selected candidate is the first whose running sum exceeds the target (a
-// ballot over the stored sums), so every result, and so the lattice, equals
-// react_voxel_inline's.  Counters and species deltas are updated by lane 0.
+// the same voxel and gets the same result.  The warp works on the voxel's
+// species histogram (in its shared scratch `ws`) instead of its slots: every
+// quantity of the SSA depends on the counts alone, and the content it returns
+// is rewritten species-major as react_voxel_inline's is.  Lane l owns
+// reactions l, l + 32, ...: the candidates' propensities go to their rank in
+// index order, lane 0 forms the running sums in that order (binary32 and, when
+// the selection needs it, binary64) exactly as react_voxel_inline does, and
+// the selected candidate is the first whose running sum exceeds the target (a
+// ballot over the stored sums).  An event's change list is applied one entry
+// per lane.  So every result, and so the lattice, equals react_voxel_inline's.
 template <int K>
 __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0,
                                                  uint32_t k1, float mult, uint32_t rep, const ProdTables& T,
@@ -524,29 +538,69 @@ __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint3
     const uint32_t lane = threadIdx.x & 31u;
     if (T.R == 0) return false;
     if (lane == 0u) atomicAdd(s_diag + PD_SSA_VOXELS, 1u);
-    float* const a_s = ws;                                     // [128] propensities in candidate order
-    float* const p_s = ws + 128;                               // [128] their binary32 running sums
-    double* const pd_s = reinterpret_cast<double*>(ws + 256);  // [128] binary64 running sums
+    float* const a_s = ws;                                           // [128] propensities by candidate rank
+    float* const p_s = ws + 128;                                     // [128] their binary32 running sums
+    double* const pd_s = reinterpret_cast<double*>(ws + 256);        // [128] binary64 running sums
+    int32_t* const hist = reinterpret_cast<int32_t*>(ws + 512);      // [256] particles per species
+    uint8_t* const r_s = reinterpret_cast<uint8_t*>(ws + 768);       // [128] reaction of each rank
+    const uint32_t S1 = T.S1, R = T.R;
     uint32_t n = vox_n<K>(c);
+    for (uint32_t s = lane; s < S1; s += 32u) hist[s] = 0;
+    __syncwarp();
+    if (lane < n) atomicAdd(hist + vox_get<K>(c, lane), 1);
+    __syncwarp();
     double td = 0.0;
     float tf = 0.0f;
     bool fired = false;
     uint32_t ev = 0;
     for (; ev < T.max_events; ev++) {
-        unsigned long long c0, c1;
-        candidates<K>(T, c, n, resv, c0, c1);
-        const uint32_t nc = (uint32_t)(__popcll(c0) + __popcll(c1));
-        const uint32_t rounds = (nc + 31u) >> 5;  // at most 128 reactions: four rounds
-        uint32_t bmax = 0u, bmin = 0x7f800000u;   // bit patterns of positive binary32 order like the values
-        for (uint32_t q = 0; q < rounds; q++) {
-            const uint32_t k = q * 32u + lane;
-            if (k < nc) {
-                const float a = propensity<K>(T, (uint32_t)nth_bit(c0, c1, k), c, resv, mult);
-                a_s[k] = a;
-                if (a > 0.0f) {
-                    bmax = max(bmax, __float_as_uint(a));
-                    bmin = min(bmin, __float_as_uint(a));
-                }
+        // candidates: reactions with a reactant present (or none at all)
+        unsigned long long c0 = 0ull, c1 = 0ull;
+        for (uint32_t s = 1u + lane; s < S1; s += 32u)
+            if (hist[s] > 0) {
+                c0 |= tab_ld(T.rmask + 2 * s);
+                c1 |= tab_ld(T.rmask + 2 * s + 1);
+            }
+        c0 = ((unsigned long long)__reduce_or_sync(0xffffffffu, (uint32_t)(c0 >> 32)) << 32) |
+             __reduce_or_sync(0xffffffffu, (uint32_t)c0);
+        c1 = ((unsigned long long)__reduce_or_sync(0xffffffffu, (uint32_t)(c1 >> 32)) << 32) |
+             __reduce_or_sync(0xffffffffu, (uint32_t)c1);
+        c0 |= T.zmask[0];
+        c1 |= T.zmask[1];
+        if (resv) {
+            c0 |= tab_ld(T.rmask + 2 * resv);
+            c1 |= tab_ld(T.rmask + 2 * resv + 1);
+        }
+        const uint32_t p0 = (uint32_t)__popcll(c0);
+        const uint32_t nc = p0 + (uint32_t)__popcll(c1);
+        uint32_t bmax = 0u, bmin = 0x7f800000u;  // bit patterns of positive binary32 order like the values
+        for (uint32_t r = lane; r < R; r += 32u) {
+            const bool cand = r < 64u ? ((c0 >> r) & 1ull) != 0ull : ((c1 >> (r - 64u)) & 1ull) != 0ull;
+            if (!cand) continue;
+            const uint32_t rank = r < 64u ? (uint32_t)__popcll(c0 & ((1ull << r) - 1ull))
+                                          : p0 + (uint32_t)__popcll(c1 & ((1ull << (r - 64u)) - 1ull));
+            // the propensity of react_voxel_inline, from the histogram
+            const uint8_t* re = T.rx_reactants + 3 * r;
+            const uint32_t sp[3] = {tab_ld(re), tab_ld(re + 1), tab_ld(re + 2)};
+            uint32_t ff = 1u;
+            bool zero = false;
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const uint32_t q = sp[j];
+                if (q == 0u) continue;
+                uint32_t m = 0u;
+#pragma unroll
+                for (int i = 0; i < j; i++) m += sp[i] == q;
+                const uint32_t cnt = q == resv ? 1u : (uint32_t)hist[q];
+                if (cnt <= m) zero = true;
+                else ff *= cnt - m;
+            }
+            const float a = zero ? 0.0f : __fmul_rn(__fmul_rn(tab_ld(T.rx_rate + r), mult), (float)ff);
+            a_s[rank] = a;
+            r_s[rank] = (uint8_t)r;
+            if (a > 0.0f) {
+                bmax = max(bmax, __float_as_uint(a));
+                bmin = min(bmin, __float_as_uint(a));
             }
         }
         __syncwarp();
@@ -558,9 +612,19 @@ __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint3
             }
         }
         __syncwarp();
+        const uint32_t rounds = (nc + 31u) >> 5;
         float a0, amax, amin;
         if (resv == 0u && n <= 1u) {
-            const float* o = T.one + ((size_t)rep * T.S1 + (n ? vox_get<K>(c, 0) : 0u)) * 3;
+            uint32_t sole = 0u;  // the species of the voxel's one particle
+            if (n == 1u)
+                for (uint32_t base = 0; base < S1; base += 32u) {
+                    const uint32_t b = __ballot_sync(0xffffffffu, base + lane < S1 && hist[base + lane] > 0);
+                    if (b) {
+                        sole = base + (uint32_t)__ffs((int)b) - 1u;
+                        break;
+                    }
+                }
+            const float* o = T.one + ((size_t)rep * S1 + sole) * 3;
             a0 = tab_ld(o);
             amax = tab_ld(o + 1);
             amin = tab_ld(o + 2);
@@ -623,66 +687,61 @@ __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint3
                 if (b) idx = q * 32 + 31 - __clz((int)b);
             }
         }
+        const uint32_t sel = idx >= 0 ? (uint32_t)r_s[idx] : 0u;
         __syncwarp();  // the scratch is rewritten by the next event
         if (idx < 0) break;
-        const int sel = nth_bit(c0, c1, (uint32_t)idx);
-        // apply the change list, skipping the voxel's reservoir species (every lane, same result)
-        const uint8_t* csp = T.rx_ch_sp + 8 * sel;
-        const int8_t* cd = T.rx_ch_d + 8 * sel;
-        int total = (int)n;
-        bool ok = true;
-        for (int j = 0; j < 8; j++) {
-            uint32_t s = tab_ld(csp + j);
-            if (s == 0) break;
-            if (s == resv) continue;
-            int d = tab_ld(cd + j);
-            int have = (int)vox_count<K>(c, s);
-            if (have + d < 0) ok = false;
-            total += d;
-        }
-        if (!ok || total > (int)K) {
+        // the change list (distinct species, ending at the first zero), one entry per lane; the
+        // voxel's reservoir species is skipped
+        const uint32_t es = lane < 8u ? (uint32_t)tab_ld(T.rx_ch_sp + 8 * sel + lane) : 0u;
+        const int ed = lane < 8u ? (int)tab_ld(T.rx_ch_d + 8 * sel + lane) : 0;
+        const uint32_t zb = __ballot_sync(0xffffffffu, lane < 8u && es == 0u);
+        const uint32_t n_ent = zb ? (uint32_t)__ffs((int)zb) - 1u : 8u;
+        const bool act = lane < n_ent && es != resv;
+        const int have = act ? hist[es] : 0;
+        const int total = (int)n + __reduce_add_sync(0xffffffffu, (uint32_t)(act ? ed : 0));
+        if (__any_sync(0xffffffffu, act && have + ed < 0) || total > (int)K) {
             if (lane == 0u) atomicAdd(s_diag + PD_REJECT_CAP, 1u);
             continue;
         }
-        for (int pass = 0; pass < 2; pass++) {
-            for (int j = 0; j < 8; j++) {
-                uint32_t s = tab_ld(csp + j);
-                if (s == 0) break;
-                if (s == resv) continue;
-                int d = tab_ld(cd + j);
-                if (pass == 0) {
-                    for (; d < 0; d++) {
-                        uint32_t idx2 = 0;
-                        for (uint32_t i = 0; i < n; i++)
-                            if (vox_get<K>(c, i) == s) idx2 = i;
-                        vox_set<K>(c, idx2, vox_get<K>(c, n - 1));
-                        vox_set<K>(c, n - 1, 0u);
-                        n--;
-                    }
-                } else {
-                    for (; d > 0; d--) vox_set<K>(c, n++, s);
-                    if (lane == 0u) atomicAdd(s_delta + s, tab_ld(cd + j));
-                }
-            }
+        if (act) {
+            hist[es] = have + ed;
+            atomicAdd(s_delta + es, ed);
         }
+        __syncwarp();
+        n = (uint32_t)total;
         if (lane == 0u) atomicAdd(s_diag + PD_EVENTS, 1u);
         fired = true;
     }
     if (ev == T.max_events && lane == 0u) atomicAdd(s_diag + PD_EVENT_CAP, 1u);
     if (fired) {
-        Vox<K> out = vox_zero<K>();
-        uint32_t j = 0, prev = 0;
-        for (;;) {
-            uint32_t best = 256;
-            for (uint32_t i = 0; i < n; i++) {
-                uint32_t b = vox_get<K>(c, i);
-                if (b > prev && b < best) best = b;
+        // species-major rewrite, ascending species id: lane l writes the run of species
+        // base + l at its exclusive prefix of the counts
+        uint64_t w[K / 8];
+#pragma unroll
+        for (int i = 0; i < K / 8; i++) w[i] = 0ull;
+        int off = 0;
+        for (uint32_t base = 0; base < S1; base += 32u) {
+            const uint32_t s = base + lane;
+            const int cnt = (s > 0u && s < S1) ? hist[s] : 0;
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)lane >= o) incl += u;
             }
-            if (best == 256) break;
-            uint32_t cnt = vox_count<K>(c, best);
-            for (uint32_t k = 0; k < cnt; k++) vox_or<K>(out, j++, best);
-            prev = best;
+            const int a = off + incl - cnt;
+            if (cnt > 0) {
+                const uint64_t rep8 = (uint64_t)s * 0x0101010101010101ull;
+#pragma unroll
+                for (int i = 0; i < K / 8; i++) w[i] |= rep8 & byte_run_mask(a - 8 * i, a + cnt - 8 * i);
+            }
+            off += __shfl_sync(0xffffffffu, incl, 31);
         }
+        Vox<K> out;
+#pragma unroll
+        for (int i = 0; i < K / 8; i++)
+            out.w[i] = ((uint64_t)__reduce_or_sync(0xffffffffu, (uint32_t)(w[i] >> 32)) << 32) |
+                       __reduce_or_sync(0xffffffffu, (uint32_t)w[i]);
         c = out;
     }
     return fired;

@@ -120,6 +120,9 @@ class Simulation:
         # species count (+1) of the prepared model, read once per preparation for counts();
         # every call that can change the model clears it
         self._s1: int | None = None
+        # counts() reads into one persistent buffer (its ctypes pointer made once) and returns a copy
+        self._counts_buf: np.ndarray | None = None
+        self._counts_ptr = None
 
     @classmethod
     def from_file(cls, path: str, placement_seed: int = 0) -> "Simulation":
@@ -332,9 +335,12 @@ class Simulation:
     def counts(self) -> np.ndarray:
         """Species counts (StatisticsGroup buffer 0, src/statistics.rs:11-69)."""
         s1 = self._s1 if self._s1 is not None else self.info().n_species + 1
-        out = np.zeros(s1, np.int64)
-        N.check(self._lib.cs_get_counts(self._h, N.ptr(out, C.c_int64)))
-        return out
+        buf = self._counts_buf
+        if buf is None or buf.shape[0] != s1:
+            buf = self._counts_buf = np.zeros(s1, np.int64)
+            self._counts_ptr = N.ptr(buf, C.c_int64)
+        N.check(self._lib.cs_get_counts(self._h, self._counts_ptr))
+        return buf.copy()
 
     def diagnostics(self, n: int = 8) -> np.ndarray:
         d = np.zeros(n, np.uint32)
