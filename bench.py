@@ -3,7 +3,7 @@
 Default workload: the 256^3, 16-slot, 16-species / 30-reaction multi-region
 lattice (the roofline configuration), production path (Philox, FP32
 propensities with FP64 clock), the autotuned step variant (the sweep stream:
-three or four launches per frame).  `value` is voxel-steps/s over the whole
+two or three launches per frame).  `value` is voxel-steps/s over the whole
 job with the lattice resident in HBM; the lattice (2 x 256 MiB) is larger
 than L2, so no flush is needed between timed frames.  Also reported: the
 batched 512-replicate ensemble vs the plain one-launch-group-per-replicate
@@ -252,7 +252,7 @@ def describe_variant(i):
 
 def launches_per_frame(i):
     """Kernel launches per frame of variant i once a run is under way: the sweep stream's passes
-    (three where the Y and Z sweeps are one launch, else four), a brick pass and the pass over its
+    (two where the Y and Z sweeps are one launch, else three), a brick pass and the pass over its
     spilled bricks, or one tile-pipeline launch."""
     from cell_simulation_gb300 import tiling_launches
     return tiling_launches()[i]
@@ -261,9 +261,9 @@ def launches_per_frame(i):
 def frame_kernels(desc):
     """The kernels of one frame of a variant, as named in the committed ncu summaries."""
     if desc["kind"] == "stream":
-        if desc["passes_per_frame"] == 3:
-            return ["sweep_pass_kernel<1>", "sweep_pass_kernel<5>", "sweep_ssa_kernel"]
-        return ["sweep_pass_kernel<1>", "sweep_pass_kernel<2>", "sweep_pass_kernel<3>", "sweep_ssa_kernel"]
+        if desc["passes_per_frame"] == 2:
+            return ["sweep_pass_kernel<1>", "sweep_pass_kernel<5>"]
+        return ["sweep_pass_kernel<1>", "sweep_pass_kernel<2>", "sweep_pass_kernel<3>"]
     return ["brick_step_kernel"] if desc["kind"] == "brick" else ["prod_step_kernel"]
 
 

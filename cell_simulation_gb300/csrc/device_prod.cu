@@ -168,7 +168,7 @@ struct DeviceProd {
     DevBuf<uint4> rec[3];  // two parities; fused variants: x-, y- and z-decision records in 0, 1, 2
     DevBuf<uint32_t> sw[14];
     DevBuf<uint8_t> wcode;  // per bitmap word: uniform region code of its window, or 0 (single lattices)
-    DevBuf<uint32_t> ssa_list;  // pass 3: output record indices of the voxels whose SSA runs in pass 4
+    DevBuf<uint2> ssa_over;  // pass 3: per-warp lists of the voxels set aside for the warp's SSA
     std::vector<WordGroup> h_groups;
     bool groups_sorted = false;  // groups dealt heaviest first (sorted once per group build)
     int stream_per_sm[4] = {0, 0, 0, 0};  // resident blocks per SM of the current stream passes
@@ -615,7 +615,13 @@ static void build_groups(DeviceProd* d) {
         if (d->rec[b].n < 2 * rb) d->rec[b].alloc(2 * rb);  // two uint4 per record
     for (auto& a : d->sw)
         if (a.n < d->occ_words) a.alloc(d->occ_words);
-    if (d->ssa_list.n < rb) d->ssa_list.alloc(rb);  // at most one entry per record
+    {
+        // a pass-3 launch has at most 8 blocks of 256 threads per SM, and never more blocks than
+        // its groups fill
+        const uint64_t blocks = std::min<uint64_t>(8ull * (uint64_t)d->num_sms, ((uint64_t)d->n_groups + 7) / 8);
+        const uint64_t need = std::max<uint64_t>(1, blocks) * 8ull * STREAM_SSA_OVER_PER_WARP;
+        if (d->ssa_over.n < need) d->ssa_over.alloc(need);
+    }
 }
 
 // Deals each replicate's word groups heaviest first (most occupied voxels in
@@ -661,7 +667,7 @@ static size_t cfg_smem(const DeviceProd* d, const KernelCfg& cfg) {
 
 static void set_attrs(const DeviceProd* d, const KernelCfg& cfg) {
     if (cfg.kind == KIND_STREAM) {
-        stream_set_attrs(cfg.K, cfg.variant, cfg_smem(d, cfg), stream_ssa_smem(d->S1, d->R));
+        stream_set_attrs(cfg.K, cfg.variant, cfg_smem(d, cfg));
         return;
     }
     CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg_smem(d, cfg)));
@@ -751,8 +757,8 @@ static int grid_for(DeviceProd* d, const KernelCfg& cfg, uint32_t n_items) {
 // Counters of launch group g (0 = all replicates, 1 + r = replicate r alone)
 // for frame parity p.  Brick pass: [0] work queue of the first launch, [1]
 // spilled bricks, [2] work queue of the spill pass.  Sweep stream: [0..2] group
-// queues of passes 1-3, [3] voxels listed for the SSA pass.
-static constexpr int kCtrPerParity = 4;
+// queues of passes 1-3.
+static constexpr int kCtrPerParity = 3;
 static uint32_t* group_ctr(DeviceProd* d, int g, int p) { return d->counters.p + (size_t)(2 * g + p) * kCtrPerParity; }
 
 // One pass of a sweep-stream frame of parity `parity` over all word groups
@@ -797,8 +803,7 @@ static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdPa
     // passes 1-3 take their groups from the frame's three work counters (pass 0: round-robin)
     if (pass > 0) S.queue = group_ctr(d, rep < 0 ? 0 : 1 + rep, parity) + (pass - 1);
     S.wcode = d->wcode.n ? d->wcode.p : nullptr;
-    S.ssa_list = d->ssa_list.p;
-    S.ssa_count = group_ctr(d, rep < 0 ? 0 : 1 + rep, parity) + 3;
+    S.ssa_over = d->ssa_over.p;
     switch (pass) {
         case 0: S.out = x_dec; S.rec_out = rx; break;
         case 1: S.in = x_in; S.rec_in = rx; S.out = y_dec; S.rec_out = ry; break;
@@ -817,18 +822,6 @@ static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdPa
             break;
         default: S.in = z_dec; S.rec_in = rz; S.fuse = 1u; S.out = x_dec; S.rec_out = rnx; break;
     }
-    if (pass == 4) {
-        // the SSA pass over the voxels pass 3 listed: a fixed grid that reads the count on the device
-        S.in = SweepWords{};
-        S.rec_in = nullptr;
-        S.fuse = 1u;
-        S.out = x_dec;
-        S.rec_out = rnx;
-        if (!stream_ssa_launch(cfg.K, 2 * d->num_sms, stream_ssa_smem(d->S1, d->R), d->stream, S))
-            throw Error(CS_ERR_INVALID_ARG, "sweep-stream kernel not compiled for this K");
-        CS_LAUNCH_CHECK();
-        return;
-    }
     if (d->stream_occ_cfg != d->cfg_index) {
         for (int q = 0; q < 4; q++) d->stream_per_sm[q] = stream_blocks_per_sm(cfg.K, cfg.variant, q, cfg_smem(d, cfg));
         d->stream_occ_cfg = d->cfg_index;
@@ -837,6 +830,8 @@ static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdPa
     if (per_sm < 1) throw Error(CS_ERR_CUDA, "sweep-stream pass does not fit on an SM");
     const uint64_t want = ((uint64_t)ng + nw - 1) / nw;
     const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)per_sm * d->num_sms, want));
+    if ((uint64_t)grid * nw * STREAM_SSA_OVER_PER_WARP > d->ssa_over.n)
+        throw Error(CS_ERR_CUDA, "sweep-stream overflow lists smaller than the launch");
     // Groups per counter increment: 2 when every resident warp has 16 or more groups to take (the
     // ensemble's many mostly empty groups, where the same-address atomic is a large part of a
     // group's cost: 0.411 -> 0.354 ms per frame on 512 replicates of 32..96^3), else 1 (the 256^3
@@ -860,7 +855,7 @@ static void launch_stream_pass0(DeviceProd* d) {
 
 static void launch_stream_frame(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity) {
     const bool fused = stream_variant_fused(cfg.variant);
-    for (int pass = 1; pass <= 4; pass++)
+    for (int pass = 1; pass <= 3; pass++)
         if (!(fused && pass == 3)) launch_stream_pass(d, cfg, P, rep, parity, pass);
 }
 
@@ -1414,7 +1409,7 @@ void prod_tiling_kind(int i, int* kind, int* BX) {
 int prod_tiling_launches(int i) {
     const auto& c = all_cfgs();
     if (i < 0 || i >= (int)c.size()) throw Error(CS_ERR_INVALID_ARG, "tile configuration index out of range");
-    if (c[i].kind == KIND_STREAM) return stream_variant_fused(c[i].variant) ? 3 : 4;
+    if (c[i].kind == KIND_STREAM) return stream_variant_fused(c[i].variant) ? 2 : 3;
     return c[i].spill >= 0 ? 2 : 1;
 }
 int prod_tiling_current(const DeviceProd* d) { return d->cfg_index; }

@@ -1,5 +1,5 @@
-// device_stream.cu — the passes of the sweep-stream step (four, or three
-// launches with the Y and Z sweeps fused) and their launchers (see
+// device_stream.cu — the passes of the sweep-stream step (three launches, or
+// two with the Y and Z sweeps fused) and their launchers (see
 // stream_kernel.cuh for the scheme).
 #include <cuda_runtime.h>
 
@@ -31,12 +31,16 @@ enum : int {
 // u32 index of field F of lane i
 __device__ __forceinline__ int fi(int F, int i) { return (F >> 1) * 64 + 2 * i + (F & 1); }
 constexpr int LIST = 1024;  // one group holds at most 32 words x 32 bits
+// Voxels of a group's Z sweep whose SSA the warp runs itself, after the group's items: a count
+// (padded to 16 bytes), then entries of two uint4 (content; Philox word, reservoir, record, item)
+constexpr int PEND = 8;
+constexpr int PEND_WORDS = 4 + 8 * PEND;
 
 }  // namespace
 
 // u32 words of one warp's shared-memory area: fields, three accumulators and
 // the item list (u16)
-__host__ __device__ constexpr size_t stream_warp_words() { return (size_t)NF * 32 + 96 + LIST / 2; }
+__host__ __device__ constexpr size_t stream_warp_words() { return (size_t)NF * 32 + 96 + LIST / 2 + PEND_WORDS; }
 
 size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words) {
     (void)S1;
@@ -100,6 +104,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     // field pair (F, F + 1) of lane i, F even
     auto fpair = [&](int F, int i) -> uint2 { return reinterpret_cast<const uint2*>(f)[(F >> 1) * 32 + i]; };
     uint16_t* list = reinterpret_cast<uint16_t*>(acc + 96);
+    uint32_t* pend = acc + 96 + LIST / 2;  // [PEND_WORDS]
     uint32_t* s_diag = sm + (size_t)NW * stream_warp_words();  // [PD_N]
     uint32_t* s_thr = s_diag + PD_N;
     allow_next_launch();
@@ -110,6 +115,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         thr = s_thr;
     }
     for (int i = tid; i < PD_N; i += NT) s_diag[i] = 0u;
+    if (lane == 0) pend[0] = 0u;
     wait_previous_launch();
     const uint32_t frame = P.stepbuf[P.parity];
     if (blockIdx.x == 0 && tid == 0) {
@@ -122,6 +128,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     auto trow = [&](uint32_t a, uint32_t b) -> const uint32_t* { return thr + (a * NC + b) * S1; };  // < 2^32 entries
 
     const uint32_t TW = gridDim.x * NW;
+    const uint32_t gw = blockIdx.x * NW + (uint32_t)w;  // this warp's index in the launch
     // groups from the pass's counter (one atomic per group, fetched a group ahead), else round-robin
     auto fetch = [&]() -> uint32_t {
         uint32_t q = 0u;
@@ -447,9 +454,21 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                                               P.T.one + (size_t)rd.counts_index * S1 * 3, P.T.g23 + 2 * rd.counts_index,
                                               P.T.a2 ? P.T.a2 + (size_t)rd.counts_index * S1 * S1 : nullptr, P.T.tau);
                             if (!calm) {
-                                // pass 4 runs this voxel's SSA: its content waits in its output record
-                                rec_store<K>(rout, ri, r, make_uint4(v, w3, rv, G.rep));
-                                SP.ssa_list[atomicAdd(SP.ssa_count, 1u)] = ri;
+                                // the warp runs this voxel's SSA after the group's items: the
+                                // first PEND such voxels wait in shared memory, the others in their
+                                // output record and the warp's overflow list
+                                const uint32_t slot = atomicAdd(pend, 1u);
+                                if (slot < (uint32_t)PEND) {
+                                    uint4* pe = reinterpret_cast<uint4*>(pend + 4) + 2 * slot;
+                                    pe[0] = make_uint4((uint32_t)r.w[0], (uint32_t)(r.w[0] >> 32),
+                                                       K == 16 ? (uint32_t)r.w[K / 8 - 1] : 0u,
+                                                       K == 16 ? (uint32_t)(r.w[K / 8 - 1] >> 32) : 0u);
+                                    pe[1] = make_uint4(w3, rv, ri, e);
+                                } else {
+                                    rec_store<K>(rout, ri, r, make_uint4(v, w3, rv, G.rep));
+                                    SP.ssa_over[(size_t)gw * STREAM_SSA_OVER_PER_WARP + (slot - (uint32_t)PEND)] =
+                                        make_uint2(ri, e);
+                                }
                                 listed = true;
                             }
                         }
@@ -472,6 +491,55 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
                 }
             }
             __syncwarp();
+            if constexpr (PP == 3) {
+                // the SSA of the voxels this warp kept, by the whole warp (react_voxel_warp, its
+                // scratch in the list's storage), then what pass 3 does for a quiet voxel: the store,
+                // the occupancy bit and the next frame's x-decisions
+                const uint32_t np = pend[0];
+                if (np != 0u) {
+                    for (uint32_t q = 0; q < np; q++) {
+                        Vox<K> r;
+                        uint4 pt;  // Philox word, reservoir species, record, item
+                        if (q < (uint32_t)PEND) {
+                            const uint4* pe = reinterpret_cast<const uint4*>(pend + 4) + 2 * q;
+                            const uint4 pc = pe[0];
+                            pt = pe[1];
+                            r.w[0] = (uint64_t)pc.x | ((uint64_t)pc.y << 32);
+                            if constexpr (K == 16) r.w[K / 8 - 1] = (uint64_t)pc.z | ((uint64_t)pc.w << 32);
+                        } else {
+                            // written by this warp's lanes in this launch: read through L2
+                            const uint2 oe = __ldcg(SP.ssa_over + (size_t)gw * STREAM_SSA_OVER_PER_WARP + (q - (uint32_t)PEND));
+                            uint4 t;
+                            rec_load<K, false>(rout, oe.x, r, t);
+                            pt = make_uint4(t.y, t.z, oe.x, oe.y);
+                        }
+                        const uint32_t i = pt.w >> 5, bit = 1u << (pt.w & 31u);
+                        const uint2 f_yk = fpair(F_Y, (int)i), f_vc = fpair(F_VROW, (int)i);
+                        const int yy = (int)f_yk.x, zz = 32 * (int)f_yk.y + (int)(pt.w & 31u);
+                        const uint32_t v = f_vc.x + (uint32_t)zz;
+                        react_voxel_warp<K>(r, pt.y, v, frame, k0, k1, rd.rate_mult, rd.counts_index, P.T, nullptr,
+                                            P.counts + (size_t)rd.counts_index * S1, s_diag, pt.x,
+                                            reinterpret_cast<float*>(list));
+                        if (lane == 0 && !vox_empty<K>(r)) {
+                            st_vox_g<K>(P.dst + (rd.base + v) * K, r);
+                            atomicOr(acc + i, bit);
+                            if (SP.fuse) {
+                                const uint32_t nf = frame + 1u;
+                                const U4 b0 = d_philox(v, nf, 0u, 0u, k0, k1);
+                                const uint32_t rs = code(f_vc.y, x, yy, zz);
+                                const uint32_t d = decide_moves<K>(r, v, nf, 0u, trow(rs, code(f_vc.y, x - 1, yy, zz)),
+                                                                   trow(rs, code(f_vc.y, x + 1, yy, zz)), k0, k1, b0.x);
+                                rec_store<K>(rout, pt.z, r, make_uint4(d, b0.y, b0.z, b0.w));
+                                if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
+                                if (d >> 16) atomicOr(acc + 64 + i, bit);
+                            }
+                        }
+                        __syncwarp();
+                    }
+                    if (lane == 0) pend[0] = 0u;
+                    __syncwarp();
+                }
+            }
             if (valid) {
                 if constexpr (PP == 0) {
                     SP.out.mv_m[wo] = acc[32 + lane];
@@ -514,125 +582,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
         if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
 }
 
-// Pass 4: the SSA of the voxels pass 3 listed, one warp per voxel (the lanes
-// evaluate its candidate reactions together, react_voxel_warp), then its store,
-// occupancy bit and next-frame x-decisions by lane 0 (as pass 3 does for the
-// quiet voxels).  Species deltas are flushed per voxel (replicates may differ
-// from voxel to voxel); the reaction tables are staged in shared memory.
-template <int K>
-__global__ void __launch_bounds__(128) sweep_ssa_kernel(const StreamParams SP) {
-    const ProdParams& P = SP.P;
-    extern __shared__ __align__(16) uint32_t sm[];
-    const uint32_t S1 = P.T.S1, NC = P.T.NC;
-    const int tid = threadIdx.x;
-    allow_next_launch();
-    float* const ws = reinterpret_cast<float*>(sm) + (size_t)(tid >> 5) * SSA_WARP_SCRATCH;  // the warp's SSA scratch
-    int32_t* my = reinterpret_cast<int32_t*>(sm + 4 * SSA_WARP_SCRATCH) + (size_t)tid * S1;
-    uint32_t* s_diag = sm + 4 * SSA_WARP_SCRATCH + (size_t)128 * S1;
-    for (uint32_t s = 0; s < S1; s++) my[s] = 0;
-    for (int i = tid; i < PD_N; i += 128) s_diag[i] = 0u;
-    // the reaction tables in shared memory: each SSA walks them in long dependent chains
-    const uint32_t R = P.T.R;
-    uint8_t* rx = reinterpret_cast<uint8_t*>(sm + 4 * SSA_WARP_SCRATCH + ((size_t)128 * S1 + PD_N + 3) / 4 * 4);
-    unsigned long long* rm = reinterpret_cast<unsigned long long*>(rx);
-    float* rate = reinterpret_cast<float*>(rx + 16 * S1);
-    uint8_t* rre = rx + 16 * S1 + 4 * R;
-    uint8_t* csp = rre + 3 * R;
-    int8_t* cdl = reinterpret_cast<int8_t*>(csp + 8 * R);
-    for (uint32_t i = tid; i < 2 * S1; i += 128) rm[i] = P.T.rmask[i];
-    for (uint32_t i = tid; i < R; i += 128) rate[i] = P.T.rx_rate[i];
-    for (uint32_t i = tid; i < 3 * R; i += 128) rre[i] = P.T.rx_reactants[i];
-    for (uint32_t i = tid; i < 8 * R; i += 128) {
-        csp[i] = P.T.rx_ch_sp[i];
-        cdl[i] = P.T.rx_ch_d[i];
-    }
-    ProdTables TS = P.T;
-    TS.rmask = rm;
-    TS.rx_rate = rate;
-    TS.rx_reactants = rre;
-    TS.rx_ch_sp = csp;
-    TS.rx_ch_d = cdl;
-    __syncthreads();
-    wait_previous_launch();
-    const uint32_t frame = P.stepbuf[P.parity];
-    const uint32_t n = *SP.ssa_count;
-    // One warp per listed voxel: the lanes share its SSA (react_voxel_warp), lane 0 stores it.
-    const uint32_t warps = gridDim.x * 4u, gw = blockIdx.x * 4u + ((uint32_t)tid >> 5), lane = (uint32_t)tid & 31u;
-    int32_t* my0 = reinterpret_cast<int32_t*>(sm + 4 * SSA_WARP_SCRATCH) + (size_t)(tid - (int)lane) * S1;  // lane 0's deltas
-    for (uint32_t j = gw; j < n; j += warps) {
-        const uint32_t ri = SP.ssa_list[j];
-        Vox<K> r;
-        uint4 t;
-        rec_load<K>(SP.rec_out, ri, r, t);
-        const uint32_t v = t.x, w3 = t.y, rv = t.z;
-        const RepDesc rd = P.reps[t.w];
-        const uint32_t k0 = rd.seed_lo, k1 = rd.seed_hi;
-        // what the store and the next frame's x-decisions need besides the SSA's result (the
-        // voxel's bitmap word, region codes, threshold rows, next frame's Philox block) is loaded and
-        // computed first, so that it is ready when the SSA ends
-        const uint32_t Y = rd.Y, Z = rd.Z, X = rd.X;
-        const uint32_t x = v / (Y * Z), rem = v - x * (Y * Z), y = rem / Z, z = rem - y * Z;
-        const uint64_t wo = rd.obase + ((uint64_t)x * Y + y) * rd.Wz + (z >> 5);
-        const uint32_t bit = 1u << (z & 31u);
-        const uint32_t nf = frame + 1u;
-        const uint32_t* tlo = nullptr;
-        const uint32_t* thi = nullptr;
-        U4 b0{0u, 0u, 0u, 0u};
-        if (SP.fuse) {
-            const uint32_t uc = (rd.flags & 1u) ? 1u : SP.wcode ? (uint32_t)SP.wcode[wo] : 0u;
-            const uint8_t* rpad = P.region_pad + rd.rbase;
-            auto code = [&](int xx, int yy, int zz) -> uint32_t {
-                if ((unsigned)xx >= X || (unsigned)yy >= Y || (unsigned)zz >= Z) return 0u;
-                if (uc) return uc;
-                return rpad[((uint64_t)xx * Y + (uint64_t)yy) * rd.Zr + (uint64_t)zz + 2u];
-            };
-            const uint32_t rs = code((int)x, (int)y, (int)z);
-            tlo = P.T.thr + ((size_t)rs * NC + code((int)x - 1, (int)y, (int)z)) * S1;
-            thi = P.T.thr + ((size_t)rs * NC + code((int)x + 1, (int)y, (int)z)) * S1;
-            b0 = d_philox(v, nf, 0u, 0u, k0, k1);
-        }
-        react_voxel_warp<K>(r, rv, v, frame, k0, k1, rd.rate_mult, rd.counts_index, TS, my0, s_diag, w3, ws);
-        __syncwarp();
-        if (lane == 0u) {
-            for (uint32_t s = 0; s < S1; s++)
-                if (my0[s]) {
-                    atomicAdd(P.counts + (size_t)rd.counts_index * S1 + s, (unsigned long long)(long long)my0[s]);
-                    my0[s] = 0;
-                }
-            if (!vox_empty<K>(r)) {
-                st_vox_g<K>(P.dst + (rd.base + v) * K, r);
-                atomicOr(P.odst + wo, bit);
-                if (SP.fuse) {
-                    const uint32_t d = decide_moves<K>(r, v, nf, 0u, tlo, thi, k0, k1, b0.x);
-                    rec_store<K>(SP.rec_out, ri, r, make_uint4(d, b0.y, b0.z, b0.w));
-                    if (d & 0xFFFFu) atomicOr(SP.out.mv_m + wo, bit);
-                    if (d >> 16) atomicOr(SP.out.mv_p + wo, bit);
-                }
-            }
-        }
-        __syncwarp();
-    }
-    __syncthreads();
-    for (int i = tid; i < PD_N; i += 128)
-        if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
-}
-
-// the four warps' SSA scratch, per-thread deltas, diagnostics, then the staged tables (16 S1 +
-// 23 R bytes)
-size_t stream_ssa_smem(uint32_t S1, uint32_t R) {
-    return (size_t)4 * SSA_WARP_SCRATCH * 4 + ((size_t)128 * S1 + PD_N + 3) / 4 * 16 + (size_t)16 * S1 + (size_t)23 * R;
-}
-
 static void launch_pdl(void* fn, int grid, int threads, size_t smem, cudaStream_t s, const StreamParams& SP);
-
-bool stream_ssa_launch(int K, int grid, size_t smem, cudaStream_t s, const StreamParams& SP) {
-    void* fn = K == 16 ? reinterpret_cast<void*>(&sweep_ssa_kernel<16>)
-             : K == 8  ? reinterpret_cast<void*>(&sweep_ssa_kernel<8>)
-                       : nullptr;
-    if (!fn) return false;
-    launch_pdl(fn, grid, 128, smem, s, SP);
-    return true;
-}
 
 // ------------------------------------------------------------------ launchers
 
@@ -721,15 +671,13 @@ int stream_blocks_per_sm(int K, int variant, int pass, size_t smem) {
     return n;
 }
 
-void stream_set_attrs(int K, int variant, size_t smem, size_t ssa_smem) {
+void stream_set_attrs(int K, int variant, size_t smem) {
     for (int pass = 0; pass < 4; pass++) {
         void* fn = kernel_of(K, variant, pass);
         if (!fn) continue;
         CS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         CS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     }
-    void* ssa = K == 16 ? reinterpret_cast<void*>(&sweep_ssa_kernel<16>) : reinterpret_cast<void*>(&sweep_ssa_kernel<8>);
-    CS_CUDA(cudaFuncSetAttribute(ssa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssa_smem));
 }
 
 }  // namespace cellsim

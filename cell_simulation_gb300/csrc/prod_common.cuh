@@ -517,8 +517,8 @@ __device__ __forceinline__ uint64_t byte_run_mask(int a, int b) {
     return hi & ~((1ull << (8 * a)) - 1ull);  // a < 8 here
 }
 
-// Words of the per-warp shared scratch react_voxel_warp uses (4 KB).
-constexpr int SSA_WARP_SCRATCH = 1024;
+// Words of the per-warp shared scratch react_voxel_warp uses (1408 bytes).
+constexpr int SSA_WARP_SCRATCH = 352;
 
 // The SSA of react_voxel_inline run by a whole warp: every lane calls it with
 // the same voxel and gets the same result.  The warp works on the voxel's
@@ -529,25 +529,25 @@ constexpr int SSA_WARP_SCRATCH = 1024;
 // index order, lane 0 forms the running sums in that order (binary32 and, when
 // the selection needs it, binary64) exactly as react_voxel_inline does, and
 // the selected candidate is the first whose running sum exceeds the target (a
-// ballot over the stored sums).  An event's change list is applied one entry
-// per lane.  So every result, and so the lattice, equals react_voxel_inline's.
+// ballot over the stored binary32 sums; lane 0 scans the binary64 ones).  An
+// event's change list is applied one entry per lane, its species deltas added
+// to s_delta (shared) or, when that is null, to the global counts row
+// g_counts.  So every result, and so the lattice, equals react_voxel_inline's.
 template <int K>
 __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint32_t v, uint32_t frame, uint32_t k0,
                                                  uint32_t k1, float mult, uint32_t rep, const ProdTables& T,
-                                                 int32_t* s_delta, uint32_t* s_diag, uint32_t w3, float* ws) {
+                                                 int32_t* s_delta, unsigned long long* g_counts, uint32_t* s_diag,
+                                                 uint32_t w3, float* ws) {
     const uint32_t lane = threadIdx.x & 31u;
     if (T.R == 0) return false;
     if (lane == 0u) atomicAdd(s_diag + PD_SSA_VOXELS, 1u);
-    float* const a_s = ws;                                           // [128] propensities by candidate rank
-    float* const p_s = ws + 128;                                     // [128] their binary32 running sums
-    double* const pd_s = reinterpret_cast<double*>(ws + 256);        // [128] binary64 running sums
-    int32_t* const hist = reinterpret_cast<int32_t*>(ws + 512);      // [256] particles per species
-    uint8_t* const r_s = reinterpret_cast<uint8_t*>(ws + 768);       // [128] reaction of each rank
+    float* const a_s = ws;                                      // [128] propensities by candidate rank
+    float* const p_s = ws + 128;                                // [128] their binary32 running sums
+    uint8_t* const hist = reinterpret_cast<uint8_t*>(ws + 256);  // [256] particles per species
+    uint8_t* const r_s = reinterpret_cast<uint8_t*>(ws + 320);   // [128] reaction of each rank
     const uint32_t S1 = T.S1, R = T.R;
     uint32_t n = vox_n<K>(c);
-    for (uint32_t s = lane; s < S1; s += 32u) hist[s] = 0;
-    __syncwarp();
-    if (lane < n) atomicAdd(hist + vox_get<K>(c, lane), 1);
+    for (uint32_t s = lane; s < S1; s += 32u) hist[s] = s ? (uint8_t)vox_count<K>(c, s) : (uint8_t)0;
     __syncwarp();
     double td = 0.0;
     float tf = 0.0f;
@@ -666,19 +666,19 @@ __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint3
         } else {
             if (lane == 0u) {
                 atomicAdd(s_diag + PD_FP64_SEL, 1u);
+                double a0d = 0.0;
+                for (uint32_t k = 0; k < nc; k++) a0d = __dadd_rn(a0d, (double)a_s[k]);
+                const double target = __dmul_rn((double)u2, a0d);
                 double run = 0.0;
                 for (uint32_t k = 0; k < nc; k++) {
                     run = __dadd_rn(run, (double)a_s[k]);
-                    pd_s[k] = run;
+                    if (target < run) {
+                        idx = (int)k;
+                        break;
+                    }
                 }
             }
-            __syncwarp();
-            const double target = __dmul_rn((double)u2, nc ? pd_s[nc - 1u] : 0.0);
-            for (uint32_t q = 0; q < rounds && idx < 0; q++) {
-                const uint32_t k = q * 32u + lane;
-                const uint32_t b = __ballot_sync(0xffffffffu, k < nc && target < pd_s[k]);
-                if (b) idx = (int)(q * 32u) + __ffs((int)b) - 1;
-            }
+            idx = __shfl_sync(0xffffffffu, idx, 0);
         }
         if (idx < 0) {
             for (int q = (int)rounds - 1; q >= 0 && idx < 0; q--) {
@@ -704,8 +704,9 @@ __device__ __forceinline__ bool react_voxel_warp(Vox<K>& c, uint32_t resv, uint3
             continue;
         }
         if (act) {
-            hist[es] = have + ed;
-            atomicAdd(s_delta + es, ed);
+            hist[es] = (uint8_t)(have + ed);
+            if (s_delta) atomicAdd(s_delta + es, ed);
+            else atomicAdd(g_counts + es, (unsigned long long)(long long)ed);
         }
         __syncwarp();
         n = (uint32_t)total;

@@ -1,20 +1,20 @@
 // stream_kernel.cuh — the sweep-stream form of the production step.
 //
-// One frame is four barrier-free passes over the occupancy bitmaps:
+// One frame is barrier-free passes over the occupancy bitmaps:
 //
 //   pass 0  x-move decisions of every occupied voxel of the source lattice
 //   pass 1  X sweep (new content along x), y-move decisions
 //   pass 2  Y sweep, z-move decisions
 //   pass 3  Z sweep, reactions, store into the destination lattice and its
 //           occupancy bitmap; voxels that became empty get zeros
-//   pass 4  the SSA of the few voxels whose first reaction event may fall
-//           within the frame (pass 3 lists them instead of running it)
 //
 // Pass 3 decides for every occupied voxel whether an event can fire at all
-// (the exact quiet-voxel bound); the rest are parked in their output record
-// and listed, and pass 4 runs their SSA one thread per voxel, stores them and
-// makes their next-frame decisions.  Keeping the SSA out of pass 3 keeps its
-// registers and its warps free of rare, long single-lane calls.
+// (the exact quiet-voxel bound).  The few voxels whose first event may fall
+// within the frame are set aside by the lane that meets them, and once the
+// group's items are done the whole warp runs their SSA together
+// (react_voxel_warp), then stores them and makes their next-frame decisions.
+// So no lane runs a long single-voxel SSA while the others wait, and no launch
+// of its own (and no launch boundary) is spent on them.
 //
 // Pass 0 of frame f + 1 needs only the final contents of frame f, so pass 3
 // also makes the next frame's x-decisions while the contents are in
@@ -94,8 +94,9 @@ struct StreamParams {
     const uint4* rec_in;
     uint4* rec_mid;  // PASS_YZ: the z-decision records its Y sweep writes and its Z sweep reads
     uint4* rec_out;
-    uint32_t* ssa_list;   // output record indices of the voxels listed for pass 4
-    uint32_t* ssa_count;  // their number (zero at the start of the frame)
+    // pass 3: per warp of the launch (block * warps per block + warp), room for a group's items:
+    // the voxels set aside for the warp's SSA beyond its shared buffer (record index, item)
+    uint2* ssa_over;
 };
 
 // Template value of the fused Y and Z sweep (passes 2 and 3 in one launch).
@@ -115,11 +116,9 @@ bool stream_launch(int K, int variant, int pass, int grid, size_t smem, cudaStre
 int stream_blocks_per_sm(int K, int variant, int pass, size_t smem);
 // Dynamic shared memory of one block of NT threads.
 size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words);
-// Sets the kernel attributes (shared-memory size and carveout) of every pass;
-// ssa_smem is the SSA pass's.
-void stream_set_attrs(int K, int variant, size_t smem, size_t ssa_smem);
-// The SSA pass (pass 4): `grid` blocks over the listed voxels.
-bool stream_ssa_launch(int K, int grid, size_t smem, cudaStream_t s, const StreamParams& SP);
-size_t stream_ssa_smem(uint32_t S1, uint32_t R);
+// Sets the kernel attributes (shared-memory size and carveout) of every pass.
+void stream_set_attrs(int K, int variant, size_t smem);
+// Entries of StreamParams::ssa_over per warp of a pass-3 launch.
+constexpr uint32_t STREAM_SSA_OVER_PER_WARP = 1024;
 
 }  // namespace cellsim

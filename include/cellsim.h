@@ -279,7 +279,7 @@ cs_status cs_step_philox_timed(cs_sim* sim, uint32_t n_steps, uint64_t seed, flo
  * kind 2 = sweep stream (the default): barrier-free passes over groups of 32
  * occupancy-bitmap words (TY = 0, TZ = 32, brick_planes = 0).  Every variant
  * computes the same lattice.  cs_tiling_launches: kernel launches per frame
- * once a run is under way (the sweep stream: 4, or 3 where the Y and Z sweeps
+ * once a run is under way (the sweep stream: 3, or 2 where the Y and Z sweeps
  * are one launch; those variants need Z <= 1024 and cs_set_tiling refuses
  * them otherwise).  No reference counterpart (the reference has one fixed
  * dispatch shape per shader). */

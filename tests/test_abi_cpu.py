@@ -33,7 +33,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_variant_tables(lib):
     """The compiled step variants as the autotuner and bench.py see them (no device call): every
-    slot count has four-launch sweep streams and fused ones (three launches per frame); bricks
+    slot count has three-launch sweep streams and fused ones (two launches per frame); bricks
     with bounded pools take two launches, the tile pipeline one."""
     from cell_simulation_gb300 import tiling_kinds, tiling_launches, tiling_variants
 
@@ -41,7 +41,7 @@ def test_variant_tables(lib):
     assert len(v) == len(k) == len(n) > 0
     for K in (8, 16):
         stream = [n[i] for i in range(len(v)) if v[i][0] == K and k[i][0] == 2]
-        assert 3 in stream and 4 in stream
+        assert 2 in stream and 3 in stream
     assert all(n[i] == 1 for i in range(len(v)) if k[i][0] == 0)
     assert all(n[i] in (1, 2) for i in range(len(v)) if k[i][0] == 1)
     with pytest.raises(CellsimError):

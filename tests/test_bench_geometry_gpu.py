@@ -15,13 +15,14 @@ pytestmark = pytest.mark.gpu
 
 def _variants(K):
     """The default step (Y and Z sweeps fused, three blocks per SM), the fused step at four blocks
-    per SM, the four-launch sweep stream and the 16-plane brick pass of slot count K."""
+    per SM, the three-launch sweep stream (Y and Z sweeps apart) and the 16-plane brick pass of
+    slot count K."""
     kinds, launches, var = tiling_kinds(), tiling_launches(), tiling_variants()
     stream = [i for i, (t, k) in enumerate(zip(var, kinds)) if t[0] == K and k[0] == 2]
-    fused = [i for i in stream if launches[i] == 3]
-    four = [i for i in stream if launches[i] == 4]
+    fused = [i for i in stream if launches[i] == 2]
+    apart = [i for i in stream if launches[i] == 3]
     brick = [i for i, (t, k) in enumerate(zip(var, kinds)) if t[0] == K and k == (1, 16)]
-    return {"fused3": fused[0], "fused4": fused[-1], "four_launch": four[-1], "brick16": brick[-1]}
+    return {"fused3": fused[0], "fused4": fused[-1], "unfused": apart[-1], "brick16": brick[-1]}
 
 
 def _oracle_frames(orc, sim, n, seed):
@@ -70,7 +71,7 @@ def test_c2_128_cube_matches_oracle(orc):
         _check(_gpu_frames(configs.c2_single_cell().sim, 6, 2024, ti, chunks=3), want, tag)
 
 
-@pytest.mark.parametrize("variant", ["fused3", "fused4", "four_launch"])
+@pytest.mark.parametrize("variant", ["fused3", "fused4", "unfused"])
 def test_c4_edge_range_matches_oracle(orc, variant):
     """Replicates with the ensemble's extreme and word-boundary edges (32, 33, 63, 64, 95, 96) and
     the ensemble's particle counts, rate multipliers and seeds, batched in one launch per pass."""

@@ -140,7 +140,7 @@ def test_fused_sweep_stream_needs_short_rows(orc):
     sim = mk()
     sim.prepare_for_gpu(RNG_PHILOX, 0)
     launches = tiling_launches()
-    fused = next(i for i in stream_tilings(16) if launches[i] == 3)
+    fused = next(i for i in stream_tilings(16) if launches[i] == 2)
     with pytest.raises(CellsimError, match="at most 32 bitmap words"):
         sim.set_tiling(fused)
     sim.step_philox(3, 31)
@@ -227,11 +227,11 @@ def test_graph_replay_equals_single_launches():
     assert np.array_equal(a.counts(), b.counts())
 
 
-@pytest.mark.parametrize("variant", ["default", "four_launches", "fused_last"])
+@pytest.mark.parametrize("variant", ["default", "unfused", "fused_last"])
 def test_ensemble_batched_equals_plain_and_oracle(orc, variant):
     """Replicates of different sizes in one launch per pass: batched frames equal per-replicate
-    (plain) frames and the oracle, for the default step (fused Y and Z sweeps), a four-launch
-    sweep stream and the fused stream at four blocks per SM."""
+    (plain) frames and the oracle, for the default step (fused Y and Z sweeps), the sweep stream
+    with the Y and Z sweeps apart and the fused stream at four blocks per SM."""
     tmpl = configs.c4_ensemble_template(K=8)
     res = np.array([[9, 9, 9], [12, 12, 12], [7, 7, 7], [16, 16, 16]], np.uint32)
     seeds = np.array([11, 22, 33, 44], np.uint64)
@@ -241,7 +241,7 @@ def test_ensemble_batched_equals_plain_and_oracle(orc, variant):
     ep = Ensemble(tmpl, res, seeds, mult, init)
     if variant != "default":
         launches = tiling_launches()
-        want = 4 if variant == "four_launches" else 3
+        want = 3 if variant == "unfused" else 2
         ti = [i for i in stream_tilings(8) if launches[i] == want][-1]
         eb.set_tiling(ti)
         ep.set_tiling(ti)
@@ -295,7 +295,7 @@ def test_switching_step_kinds_mid_run_matches_oracle(orc):
 
 
 def test_switching_to_and_from_the_sweep_stream_matches_oracle(orc):
-    """Brick, sweep-stream (four launches, and Y and Z sweeps fused) and tile frames in one run:
+    """Brick, sweep-stream (three launches, and Y and Z sweeps fused) and tile frames in one run:
     frames of another kind (and an upload) make the x-decisions the last stream frame left for the
     next frame stale, so the stream recomputes them.  Odd frame counts change the parity the kinds
     hand over; the fused variant keeps its records in buffers of fixed roles."""
@@ -307,8 +307,8 @@ def test_switching_to_and_from_the_sweep_stream_matches_oracle(orc):
     tile = next(i for i, (t, k) in enumerate(zip(tiling_variants(), kinds)) if t[0] == 16 and k[0] == 0)
     brick = next(i for i, (t, k) in enumerate(zip(tiling_variants(), kinds)) if t[0] == 16 and k == (1, 8))
     launches = tiling_launches()
-    stream = [i for i in stream_tilings(16) if launches[i] == 4][-1]
-    fused = next(i for i in stream_tilings(16) if launches[i] == 3)
+    stream = [i for i in stream_tilings(16) if launches[i] == 3][-1]
+    fused = next(i for i in stream_tilings(16) if launches[i] == 2)
     for ti, n in ((stream, 3), (brick, 4), (fused, 5), (tile, 3), (stream, 2), (fused, 3)):
         sim.set_tiling(ti)
         sim.step_philox(n, 777)
