@@ -245,6 +245,9 @@ def describe_variant(i):
     if kind == 1:
         return {"index": i, "kind": "brick", "slots": k, "brick": [bx, ty, tz], "threads": nt}
     if kind == 2:
+        if ty == 1:  # the persistent form: every frame of a step call in one launch
+            return {"index": i, "kind": "stream", "slots": k, "words_per_group": 32, "threads": nt,
+                    "passes_per_frame": 2, "multi_frame": True, "launches_per_call": 1}
         return {"index": i, "kind": "stream", "slots": k, "words_per_group": 32, "threads": nt,
                 "passes_per_frame": tiling_launches()[i]}
     return {"index": i, "kind": "tile", "slots": k, "tile": [ty, tz], "threads": nt}
@@ -253,14 +256,25 @@ def describe_variant(i):
 def launches_per_frame(i):
     """Kernel launches per frame of variant i once a run is under way: the sweep stream's passes
     (two where the Y and Z sweeps are one launch, else three), a brick pass and the pass over its
-    spilled bricks, or one tile-pipeline launch."""
+    spilled bricks, or one tile-pipeline launch.  The persistent sweep stream runs a whole step
+    call in one launch: 1 here, see launches_in_call."""
     from cell_simulation_gb300 import tiling_launches
     return tiling_launches()[i]
+
+
+def launches_in_call(i, frames):
+    """Kernel launches of one step call of `frames` frames with variant i (none for pass 0, which
+    runs only when the x-decisions are stale)."""
+    if describe_variant(i).get("multi_frame"):
+        return 1
+    return frames * launches_per_frame(i)
 
 
 def frame_kernels(desc):
     """The kernels of one frame of a variant, as named in the committed ncu summaries."""
     if desc["kind"] == "stream":
+        if desc.get("multi_frame"):
+            return ["sweep_frames_kernel"]
         if desc["passes_per_frame"] == 2:
             return ["sweep_pass_kernel<1>", "sweep_pass_kernel<5>"]
         return ["sweep_pass_kernel<1>", "sweep_pass_kernel<2>", "sweep_pass_kernel<3>"]
@@ -295,7 +309,8 @@ def ensemble_numbers(device, steps_batched=5000, steps_plain=200, variant=-1):
            "batched_over_plain": rb / rp, "steps_batched": steps_batched, "steps_plain": steps_plain,
            "ms_per_step_batched": ms_b / steps_batched, "ms_per_step_plain": ms_p / steps_plain,
            "roofline_frac_batched": tot * steps_batched / (ms_b / 1e3) * 17 / 1e9 / peak,
-           "launches_per_frame_batched": per_frame, "launches_per_frame_plain": n * per_frame,
+           "launches_per_frame_batched": per_frame,
+           "launches_per_frame_plain": n * (2 if describe_variant(variant).get("multi_frame") else per_frame),
            "variant": describe_variant(variant)}
     ens.close()
     return out
@@ -428,6 +443,7 @@ def main():
     kernels = frame_kernels(desc)
     longest = "sweep_pass_kernel<5>" if "sweep_pass_kernel<5>" in kernels else (
         "sweep_pass_kernel<3>" if "sweep_pass_kernel<3>" in kernels else kernels[0])
+    # the persistent kernel's committed traffic is per frame of its launch
     traffic = profiled_traffic(longest, w.name)
     per_kernel = {k: profiled_traffic(k, w.name) for k in kernels}
     frame_dram = sum(per_kernel.values()) if all(v is not None for v in per_kernel.values()) else None
@@ -479,7 +495,7 @@ def main():
                                        "over the measured frame time, against the measured copy bandwidth"},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": args.steps * launches_per_frame(variant),
+        "gpu_launches": launches_in_call(variant, args.steps),
         "clocks": clk,
         "diagnostics": {"events": int(diag[0]), "rejected_capacity": int(diag[1]), "event_cap": int(diag[2]),
                         "fp64_selections": int(diag[3]), "ssa_voxels": int(diag[6])},

@@ -63,8 +63,10 @@ struct KernelCfg {
     int variant;   // kind 2: launch shape of the passes
 };
 
+// TY = 1 marks the persistent multi-frame form (cs_tiling_describe)
 static KernelCfg stream_cfg(int K, int variant) {
-    return KernelCfg{KIND_STREAM, K, 0, 32, stream_variant_threads(variant), 0, nullptr, nullptr, -1, 0, variant};
+    return KernelCfg{KIND_STREAM, K, stream_variant_frames(variant) ? 1 : 0, 32, stream_variant_threads(variant), 0,
+                     nullptr, nullptr, -1, 0, variant};
 }
 
 template <int K, int TY, int TZ>
@@ -117,6 +119,9 @@ static const std::vector<KernelCfg>& all_cfgs() {
         // sweep stream with the Y and Z sweeps fused into one launch (rows of at most 32 words), at
         // three / four blocks per SM
         stream_cfg(16, 4), stream_cfg(8, 4), stream_cfg(16, 5), stream_cfg(8, 5),
+        // the fused stream as one persistent launch per step call (pass 1 and the fused pass of
+        // every frame as tasks of one counter), at three / four blocks per SM
+        stream_cfg(16, 6), stream_cfg(8, 6), stream_cfg(16, 7), stream_cfg(8, 7),
     };
     return v;
 }
@@ -169,10 +174,16 @@ struct DeviceProd {
     DevBuf<uint32_t> sw[14];
     DevBuf<uint8_t> wcode;  // per bitmap word: uniform region code of its window, or 0 (single lattices)
     DevBuf<uint2> ssa_over;  // pass 3: per-warp lists of the voxels set aside for the warp's SSA
+    // the multi-frame form: per group its four neighbours and the completion values of its last
+    // pass 1 and fused pass; the launch's task and exit counters; the completion base of the next
+    // launch (completion values compare modulo 2^32)
+    DevBuf<uint32_t> nbr, done1, done2, frames_ctr;
+    uint32_t frames_seq = 0;
     std::vector<WordGroup> h_groups;
     bool groups_sorted = false;  // groups dealt heaviest first (sorted once per group build)
     int stream_per_sm[4] = {0, 0, 0, 0};  // resident blocks per SM of the current stream passes
     int stream_occ_cfg = -1;
+    int frames_per_sm = 0, frames_occ_cfg = -1;  // ... of the current multi-frame kernel
     // The x-decisions of frame xdec_frame (parity xdec_cur, configuration xdec_cfg, seed epoch
     // xdec_epoch) are in the per-word arrays and rec[xdec_cur]: made by the last sweep-stream
     // frame's pass 3.  Any other change of the lattice clears xdec_valid.
@@ -653,6 +664,43 @@ static void sort_groups(DeviceProd* d) {
     d->h_groups = std::move(out);
     CS_CUDA(cudaMemcpy(d->groups.p, d->h_groups.data(), d->h_groups.size() * sizeof(WordGroup), cudaMemcpyHostToDevice));
     d->groups_sorted = true;
+    if (fused_fits(d)) {
+        // neighbour links of the multi-frame form, by the sorted positions of the groups: with rows
+        // of at most 32 words a group holds rows y0 .. y0 + 32 / Wz - 1 of plane x, and the
+        // replicate's groups in build order are plane-major
+        const size_t n = d->h_groups.size();
+        std::vector<uint32_t> pos(n), nb(4 * n, 0xFFFFFFFFu);
+        auto build_index = [&](const WordGroup& G) -> size_t {
+            const RepDesc& r = d->h_reps[G.rep];
+            const uint32_t per = 32 / r.Wz, gpp = (r.Y + per - 1) / per;
+            return d->rep_group_off[G.rep] + (size_t)G.x * gpp + G.y0 / per;
+        };
+        for (size_t j = 0; j < n; j++) pos[build_index(d->h_groups[j])] = (uint32_t)j;
+        for (size_t j = 0; j < n; j++) {
+            const WordGroup& G = d->h_groups[j];
+            const RepDesc& r = d->h_reps[G.rep];
+            const uint32_t per = 32 / r.Wz, gpp = (r.Y + per - 1) / per;
+            const size_t bi = build_index(G);
+            if (G.x > 0) nb[4 * j + 0] = pos[bi - gpp];
+            if (G.x + 1 < r.X) nb[4 * j + 1] = pos[bi + gpp];
+            if (G.y0 > 0) nb[4 * j + 2] = pos[bi - 1];
+            if (G.y0 / per + 1 < gpp) nb[4 * j + 3] = pos[bi + 1];
+        }
+        if (d->nbr.n != nb.size()) d->nbr.alloc(nb.size());
+        CS_CUDA(cudaMemcpy(d->nbr.p, nb.data(), nb.size() * 4, cudaMemcpyHostToDevice));
+        if (d->done1.n != n) {
+            // fresh completion values: every group done up to the base 0
+            d->done1.alloc(n);
+            d->done2.alloc(n);
+            CS_CUDA(cudaMemset(d->done1.p, 0, n * 4));
+            CS_CUDA(cudaMemset(d->done2.p, 0, n * 4));
+            d->frames_seq = 0;
+        }
+        if (d->frames_ctr.n == 0) {
+            d->frames_ctr.alloc(2);
+            CS_CUDA(cudaMemset(d->frames_ctr.p, 0, 8));
+        }
+    }
 }
 
 static uint32_t thr_words(const DeviceProd* d) {
@@ -770,13 +818,12 @@ static uint32_t* group_ctr(DeviceProd* d, int g, int p) { return d->counters.p +
 // Pass 1, the first pass of every frame, resets the other parity's work
 // counters (as the brick pass does, so that the kinds can alternate); pass 3
 // (fused variants: pass 2) advances the frame number.
-static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity, int pass) {
+static StreamParams stream_params(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity, int pass) {
     uint32_t goff = 0, ng = d->n_groups;
     if (rep >= 0) {
         goff = d->rep_group_off[rep];
         ng = d->rep_group_off[rep + 1] - goff;
     }
-    if (ng == 0) return;
     uint32_t* w[14];
     for (int i = 0; i < 14; i++) w[i] = d->sw[i].p;
     // per-word arrays of the pass boundaries: {occ, movers down, movers up, work, base}; the
@@ -790,8 +837,6 @@ static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdPa
     uint4* const ry = d->rec[fused ? 1 : parity ^ 1].p;   // y-decisions
     uint4* const rz = d->rec[fused ? 2 : parity].p;       // z-decisions
     uint4* const rnx = d->rec[fused ? 0 : parity ^ 1].p;  // the next frame's x-decisions
-    const size_t smem = cfg_smem(d, cfg);
-    const uint32_t nw = (uint32_t)cfg.NT / 32u;
     StreamParams S{};
     S.P = P;
     S.P.items = nullptr;
@@ -822,6 +867,18 @@ static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdPa
             break;
         default: S.in = z_dec; S.rec_in = rz; S.fuse = 1u; S.out = x_dec; S.rec_out = rnx; break;
     }
+    S.in_occ1 = S.in.occ;
+    S.odst1 = S.P.odst;
+    S.dst1 = S.P.dst;
+    return S;
+}
+
+static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity, int pass) {
+    StreamParams S = stream_params(d, cfg, P, rep, parity, pass);
+    const uint32_t ng = S.n_groups;
+    if (ng == 0) return;
+    const size_t smem = cfg_smem(d, cfg);
+    const uint32_t nw = (uint32_t)cfg.NT / 32u;
     if (d->stream_occ_cfg != d->cfg_index) {
         for (int q = 0; q < 4; q++) d->stream_per_sm[q] = stream_blocks_per_sm(cfg.K, cfg.variant, q, cfg_smem(d, cfg));
         d->stream_occ_cfg = d->cfg_index;
@@ -851,6 +908,61 @@ static void launch_stream_pass0(DeviceProd* d) {
     ProdParams P{};
     fill_params(d, P, d->cur, -1);
     launch_stream_pass(d, cfg, P, -1, d->cur, 0);
+}
+
+// n frames of every replicate in the persistent multi-frame form, from the frame in stepbuf[cur]:
+// one launch per chunk of frames (the tasks of a launch are counted in 32 bits).
+static void launch_stream_frames(DeviceProd* d, uint32_t n) {
+    const KernelCfg& cfg = all_cfgs()[d->cfg_index];
+    const uint32_t ng = d->n_groups;
+    if (n == 0 || ng == 0) return;
+    if (d->nbr.n != 4ull * ng || d->done1.n != ng || d->frames_ctr.n < 2)
+        throw Error(CS_ERR_STATE, "multi-frame sweep state missing (groups not sorted)");
+    const size_t smem = cfg_smem(d, cfg);
+    if (d->frames_occ_cfg != d->cfg_index) {
+        d->frames_per_sm = stream_frames_blocks_per_sm(cfg.K, cfg.variant, smem);
+        d->frames_occ_cfg = d->cfg_index;
+    }
+    const int per_sm = d->frames_per_sm;
+    if (per_sm < 1) throw Error(CS_ERR_CUDA, "multi-frame sweep kernel does not fit on an SM");
+    const int grid = per_sm * d->num_sms;
+    const uint64_t over = (uint64_t)grid * ((uint32_t)cfg.NT / 32u) * STREAM_SSA_OVER_PER_WARP;
+    if (d->ssa_over.n < over) d->ssa_over.alloc(over);
+    ProdParams P0{}, P1{};
+    fill_params(d, P0, 0, -1);
+    fill_params(d, P1, 1, -1);
+    FramesParams FP{};
+    FP.sp[0] = stream_params(d, cfg, P0, -1, 0, 1);
+    FP.sp[0].in_occ1 = P1.osrc;
+    FP.sp[0].odst1 = P1.odst;
+    FP.sp[0].dst1 = P1.dst;
+    FP.sp[1] = stream_params(d, cfg, P0, -1, 0, 2);
+    FP.sp[1].odst1 = P1.odst;
+    FP.sp[1].dst1 = P1.dst;
+    FP.nbr = d->nbr.p;
+    FP.done1 = d->done1.p;
+    FP.done2 = d->done2.p;
+    FP.tasks = d->frames_ctr.p;
+    FP.exits = d->frames_ctr.p + 1;
+    FP.reset = d->counters.p;
+    FP.n_reset = (uint32_t)d->counters.n;
+    FP.n_groups = ng;
+    // tasks per launch: 2 ng per frame, and every warp fetches once past the last one, so the
+    // counter stays below 2^32 with room for the largest grid
+    const uint32_t chunk = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>((0xFFFFFFFFull - (1ull << 20)) / (2ull * ng), 1ull << 30));
+    for (uint32_t k = 0; k < n;) {
+        const uint32_t m = std::min(n - k, chunk);
+        FP.n_frames = m;
+        FP.cur0 = (uint32_t)d->cur;
+        FP.seq = d->frames_seq;
+        if (!stream_frames_launch(cfg.K, cfg.variant, grid, smem, d->stream, FP))
+            throw Error(CS_ERR_INVALID_ARG, "multi-frame sweep kernel not compiled for this K");
+        CS_LAUNCH_CHECK();
+        d->frames_seq += m;
+        d->cur = (int)(((uint32_t)d->cur + m) & 1u);
+        k += m;
+    }
 }
 
 static void launch_stream_frame(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity) {
@@ -1113,6 +1225,13 @@ static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched) {
     d->xdec_valid = false;
     if (kind == KIND_STREAM && !xdec_ok) launch_stream_pass0(d);
     uint32_t k = 0;
+    // the multi-frame form for calls of two or more frames; a single frame gains nothing from it
+    // (no other frame's tasks to overlap) and runs as the captured per-pass launches of the same
+    // shape (the fused passes at the same blocks per SM), which compute the same lattice
+    if (batched && n >= 2 && kind == KIND_STREAM && stream_variant_frames(all_cfgs()[d->cfg_index].variant)) {
+        launch_stream_frames(d, n);
+        k = n;
+    }
     // a single frame of parity p, from its own captured graph (a step call of one frame, as the
     // reference's per-frame step makes, costs one graph launch instead of three kernel launches)
     auto single = [&](int p) {
@@ -1409,7 +1528,10 @@ void prod_tiling_kind(int i, int* kind, int* BX) {
 int prod_tiling_launches(int i) {
     const auto& c = all_cfgs();
     if (i < 0 || i >= (int)c.size()) throw Error(CS_ERR_INVALID_ARG, "tile configuration index out of range");
-    if (c[i].kind == KIND_STREAM) return stream_variant_fused(c[i].variant) ? 2 : 3;
+    if (c[i].kind == KIND_STREAM) {
+        if (stream_variant_frames(c[i].variant)) return 1;  // one launch per step call
+        return stream_variant_fused(c[i].variant) ? 2 : 3;
+    }
     return c[i].spill >= 0 ? 2 : 1;
 }
 int prod_tiling_current(const DeviceProd* d) { return d->cfg_index; }

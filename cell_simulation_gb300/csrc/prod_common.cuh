@@ -40,10 +40,11 @@
 namespace cellsim {
 
 // Diagnostic counters: events fired, events rejected for capacity, voxels that hit the event cap,
-// FP64 selections, bricks spilled to the second pass, bricks lost (never), voxels that ran the SSA.
+// FP64 selections, bricks spilled to the second pass, bricks lost (never), voxels that ran the SSA,
+// dependency waits of the multi-frame sweep kernel that timed out (never).
 enum {
     PD_EVENTS = 0, PD_REJECT_CAP = 1, PD_EVENT_CAP = 2, PD_FP64_SEL = 3, PD_DENSE_BRICKS = 4, PD_LOST_BRICKS = 5,
-    PD_SSA_VOXELS = 6, PD_N = 8
+    PD_SSA_VOXELS = 6, PD_WAIT_TIMEOUTS = 7, PD_N = 8
 };
 
 struct RepDesc {

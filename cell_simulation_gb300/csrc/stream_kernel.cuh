@@ -97,10 +97,40 @@ struct StreamParams {
     // pass 3: per warp of the launch (block * warps per block + warp), room for a group's items:
     // the voxels set aside for the warp's SSA beyond its shared buffer (record index, item)
     uint2* ssa_over;
+    // the persistent multi-frame form: the lattice buffers of frames of parity 1 (those of parity 0
+    // are in.occ, P.odst and P.dst)
+    const uint32_t* in_occ1;
+    uint32_t* odst1;
+    uint8_t* dst1;
 };
 
 // Template value of the fused Y and Z sweep (passes 2 and 3 in one launch).
 constexpr int PASS_YZ = 5;
+
+// The persistent multi-frame form of the fused stream: one launch runs pass 1 and the fused Y and
+// Z sweeps of every word group (of every replicate) for n_frames frames.  Tasks come from one
+// counter in the order frame, pass, group (groups heaviest first), so that a warp that finishes
+// early takes the next pass's or the next frame's groups instead of idling in a launch's tail.  A
+// task first waits until the tasks it reads from, and those that read what it overwrites, are
+// done: pass 1 of a group after the previous frame's fused pass of the group, of the groups with
+// the same rows at x - 1 and x + 1 and of the previous and next group of its plane; the fused pass
+// after this frame's pass 1 of the same five groups.
+struct FramesParams {
+    StreamParams sp[2];    // [0] pass 1, [1] the fused Y and Z sweeps (parity 0's lattice buffers;
+                           // parity 1's in in_occ1, odst1 and dst1)
+    const uint32_t* nbr;   // per group: x - 1, x + 1, previous and next group of the plane, or
+                           // 0xFFFFFFFF
+    uint32_t* done1;       // per group: seq + frame index + 1 of its last finished pass 1
+    uint32_t* done2;       // ... of its last finished fused pass
+    uint32_t* tasks;       // the launch's task counter, zero between launches
+    uint32_t* exits;       // warps of the launch that have finished, zero between launches
+    uint32_t* reset;       // queue counters of the per-pass launches, cleared at the start
+    uint32_t n_reset;
+    uint32_t n_groups;
+    uint32_t n_frames;     // n_frames * 2 * n_groups + the launch's warps < 2^32
+    uint32_t cur0;         // parity of the first frame
+    uint32_t seq;          // completion values of this launch are seq + frame index + 1
+};
 
 // Compiled launch shapes ("variants": threads per block and minimum resident
 // blocks per SM) of the four passes.
@@ -118,6 +148,12 @@ int stream_blocks_per_sm(int K, int variant, int pass, size_t smem);
 size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words);
 // Sets the kernel attributes (shared-memory size and carveout) of every pass.
 void stream_set_attrs(int K, int variant, size_t smem);
+// True when the variant runs in the persistent multi-frame form (stream_frames_launch).
+bool stream_variant_frames(int variant);
+// Resident blocks per SM of the multi-frame kernel of the variant (0: not compiled).
+int stream_frames_blocks_per_sm(int K, int variant, size_t smem);
+// Launches the multi-frame kernel; false when none is compiled for K and the variant.
+bool stream_frames_launch(int K, int variant, int grid, size_t smem, cudaStream_t s, const FramesParams& FP);
 // Entries of StreamParams::ssa_over per warp of a pass-3 launch.
 constexpr uint32_t STREAM_SSA_OVER_PER_WARP = 1024;
 

@@ -211,7 +211,9 @@ cs_status cs_pop_stats(cs_sim* sim, cs_stat_sample* out, uint32_t capacity, uint
  * serial order, [3] reaction rollbacks, [4] voxels that fired.  Production
  * path: [0] reaction events, [1] events rejected for capacity, [2] voxels that
  * hit the event cap, [3] FP64 selections, [4] bricks spilled to the second
- * brick pass, [5] bricks lost (always 0), [6] voxels that ran the SSA. */
+ * brick pass, [5] bricks lost (always 0), [6] voxels that ran the SSA, [7]
+ * waits of the multi-frame sweep kernel that timed out (always 0; nonzero
+ * means its frames were abandoned and the lattice is not valid). */
 cs_status cs_get_diagnostics(cs_sim* sim, uint32_t* diag, uint32_t n);
 cs_status cs_synchronize(cs_sim* sim);
 
@@ -277,12 +279,14 @@ cs_status cs_step_philox_timed(cs_sim* sim, uint32_t n_steps, uint64_t seed, flo
  * x-segment) items; kind 1 = sparse brick pass over brick_planes x TY x TZ
  * bricks, crowded bricks finished by a full-capacity second brick pass;
  * kind 2 = sweep stream (the default): barrier-free passes over groups of 32
- * occupancy-bitmap words (TY = 0, TZ = 32, brick_planes = 0).  Every variant
- * computes the same lattice.  cs_tiling_launches: kernel launches per frame
- * once a run is under way (the sweep stream: 3, or 2 where the Y and Z sweeps
- * are one launch; those variants need Z <= 1024 and cs_set_tiling refuses
- * them otherwise).  No reference counterpart (the reference has one fixed
- * dispatch shape per shader). */
+ * occupancy-bitmap words (TZ = 32, brick_planes = 0; TY = 1 marks the
+ * persistent form that runs every frame of a step call in one launch, TY = 0
+ * the per-pass launches).  Every variant computes the same lattice.
+ * cs_tiling_launches: kernel launches per frame once a run is under way (the
+ * sweep stream: 3, or 2 where the Y and Z sweeps are one launch, or 1 per step
+ * call in the persistent form; the last two need Z <= 1024 and cs_set_tiling
+ * refuses them otherwise).  No reference counterpart (the reference has one
+ * fixed dispatch shape per shader). */
 cs_status cs_tiling_count(int32_t* n);
 cs_status cs_tiling_describe(int32_t index, int32_t* K, int32_t* TY, int32_t* TZ, int32_t* threads);
 cs_status cs_tiling_kind(int32_t index, int32_t* kind, int32_t* brick_planes);

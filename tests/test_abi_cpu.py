@@ -33,15 +33,18 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_variant_tables(lib):
     """The compiled step variants as the autotuner and bench.py see them (no device call): every
-    slot count has three-launch sweep streams and fused ones (two launches per frame); bricks
-    with bounded pools take two launches, the tile pipeline one."""
+    slot count has three-launch sweep streams, fused ones (two launches per frame) and persistent
+    ones (one launch per step call); bricks with bounded pools take two launches, the tile
+    pipeline one."""
     from cell_simulation_gb300 import tiling_kinds, tiling_launches, tiling_variants
 
     v, k, n = tiling_variants(), tiling_kinds(), tiling_launches()
     assert len(v) == len(k) == len(n) > 0
     for K in (8, 16):
         stream = [n[i] for i in range(len(v)) if v[i][0] == K and k[i][0] == 2]
-        assert 2 in stream and 3 in stream
+        assert 1 in stream and 2 in stream and 3 in stream
+        # the persistent multi-frame form is marked by TY = 1
+        assert all((v[i][1] == 1) == (n[i] == 1) for i in range(len(v)) if v[i][0] == K and k[i][0] == 2)
     assert all(n[i] == 1 for i in range(len(v)) if k[i][0] == 0)
     assert all(n[i] in (1, 2) for i in range(len(v)) if k[i][0] == 1)
     with pytest.raises(CellsimError):

@@ -15,14 +15,16 @@ pytestmark = pytest.mark.gpu
 
 def _variants(K):
     """The default step (Y and Z sweeps fused, three blocks per SM), the fused step at four blocks
-    per SM, the three-launch sweep stream (Y and Z sweeps apart) and the 16-plane brick pass of
-    slot count K."""
+    per SM, the three-launch sweep stream (Y and Z sweeps apart), the persistent multi-frame stream
+    at three and four blocks per SM and the 16-plane brick pass of slot count K."""
     kinds, launches, var = tiling_kinds(), tiling_launches(), tiling_variants()
     stream = [i for i, (t, k) in enumerate(zip(var, kinds)) if t[0] == K and k[0] == 2]
     fused = [i for i in stream if launches[i] == 2]
     apart = [i for i in stream if launches[i] == 3]
+    frames = [i for i in stream if launches[i] == 1]
     brick = [i for i, (t, k) in enumerate(zip(var, kinds)) if t[0] == K and k == (1, 16)]
-    return {"fused3": fused[0], "fused4": fused[-1], "unfused": apart[-1], "brick16": brick[-1]}
+    return {"fused3": fused[0], "fused4": fused[-1], "unfused": apart[-1], "frames3": frames[0], "frames4": frames[-1],
+            "brick16": brick[-1]}
 
 
 def _oracle_frames(orc, sim, n, seed):
@@ -54,6 +56,7 @@ def _check(got, want, tag):
     assert bad.size == 0, (tag, bad.size, bad[:8])
     assert np.array_equal(gc, wc), tag
     assert np.array_equal(gd[:4], wd[:4]), (tag, gd, wd)
+    assert gd[7] == 0, (tag, gd)  # no dependency wait of the multi-frame kernel timed out
 
 
 def test_c3_256_cube_matches_oracle(orc):
@@ -71,7 +74,7 @@ def test_c2_128_cube_matches_oracle(orc):
         _check(_gpu_frames(configs.c2_single_cell().sim, 6, 2024, ti, chunks=3), want, tag)
 
 
-@pytest.mark.parametrize("variant", ["fused3", "fused4", "unfused"])
+@pytest.mark.parametrize("variant", ["fused3", "fused4", "unfused", "frames3", "frames4"])
 def test_c4_edge_range_matches_oracle(orc, variant):
     """Replicates with the ensemble's extreme and word-boundary edges (32, 33, 63, 64, 95, 96) and
     the ensemble's particle counts, rate multipliers and seeds, batched in one launch per pass."""

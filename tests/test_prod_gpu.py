@@ -215,23 +215,36 @@ def test_conservation_and_confinement():
         assert np.array_equal(r0, r1), q
 
 
-def test_graph_replay_equals_single_launches():
+@pytest.mark.parametrize("form", ["default", "frames"])
+def test_graph_replay_equals_single_launches(form):
+    """25 frames in one call equal 25 one-frame calls: the default step's two-frame graph against
+    its one-frame graphs, and the persistent multi-frame launch against the per-pass launches its
+    variant takes for one-frame calls; calls of mixed lengths as well."""
     a = multi_region_model(res=(10, 12, 30), K=16)
     b = multi_region_model(res=(10, 12, 30), K=16)
-    a.prepare_for_gpu(RNG_PHILOX, 0)
-    b.prepare_for_gpu(RNG_PHILOX, 0)
+    c = multi_region_model(res=(10, 12, 30), K=16)
+    for sim in (a, b, c):
+        sim.prepare_for_gpu(RNG_PHILOX, 0)
+        if form == "frames":
+            launches = tiling_launches()
+            sim.set_tiling(next(i for i in stream_tilings(16) if launches[i] == 1))
     a.step_philox(25, 3)
     for _ in range(25):
         b.step_philox(1, 3)
-    assert np.array_equal(a.get_lattice()[0], b.get_lattice()[0])
-    assert np.array_equal(a.counts(), b.counts())
+    for n in (1, 2, 1, 3, 1, 4, 1, 5, 7):
+        c.step_philox(n, 3)
+    for other in (b, c):
+        assert np.array_equal(a.get_lattice()[0], other.get_lattice()[0])
+        assert np.array_equal(a.counts(), other.counts())
+    assert a.diagnostics()[7] == 0
 
 
-@pytest.mark.parametrize("variant", ["default", "unfused", "fused_last"])
+@pytest.mark.parametrize("variant", ["default", "unfused", "fused_last", "frames"])
 def test_ensemble_batched_equals_plain_and_oracle(orc, variant):
     """Replicates of different sizes in one launch per pass: batched frames equal per-replicate
     (plain) frames and the oracle, for the default step (fused Y and Z sweeps), the sweep stream
-    with the Y and Z sweeps apart and the fused stream at four blocks per SM."""
+    with the Y and Z sweeps apart, the fused stream at four blocks per SM and the persistent
+    multi-frame stream (batched: every frame of a step call in one launch)."""
     tmpl = configs.c4_ensemble_template(K=8)
     res = np.array([[9, 9, 9], [12, 12, 12], [7, 7, 7], [16, 16, 16]], np.uint32)
     seeds = np.array([11, 22, 33, 44], np.uint64)
@@ -241,7 +254,7 @@ def test_ensemble_batched_equals_plain_and_oracle(orc, variant):
     ep = Ensemble(tmpl, res, seeds, mult, init)
     if variant != "default":
         launches = tiling_launches()
-        want = 3 if variant == "unfused" else 2
+        want = {"unfused": 3, "fused_last": 2, "frames": 1}[variant]
         ti = [i for i in stream_tilings(8) if launches[i] == want][-1]
         eb.set_tiling(ti)
         ep.set_tiling(ti)
@@ -295,12 +308,13 @@ def test_switching_step_kinds_mid_run_matches_oracle(orc):
 
 
 def test_switching_to_and_from_the_sweep_stream_matches_oracle(orc):
-    """Brick, sweep-stream (three launches, and Y and Z sweeps fused) and tile frames in one run:
+    """Brick, sweep-stream (three launches, Y and Z sweeps fused, and the persistent multi-frame
+    form) and tile frames in one run:
     frames of another kind (and an upload) make the x-decisions the last stream frame left for the
     next frame stale, so the stream recomputes them.  Odd frame counts change the parity the kinds
     hand over; the fused variant keeps its records in buffers of fixed roles."""
     mk = lambda: multi_region_model(res=(13, 17, 40), K=16, counts=(90, 70, 50, 40))
-    want_s, want_c, _ = oracle_prod(orc, mk(), 24, seed=777)
+    want_s, want_c, _ = oracle_prod(orc, mk(), 29, seed=777)
     sim = mk()
     sim.prepare_for_gpu(RNG_PHILOX, 0)
     kinds = tiling_kinds()
@@ -309,7 +323,8 @@ def test_switching_to_and_from_the_sweep_stream_matches_oracle(orc):
     launches = tiling_launches()
     stream = [i for i in stream_tilings(16) if launches[i] == 3][-1]
     fused = next(i for i in stream_tilings(16) if launches[i] == 2)
-    for ti, n in ((stream, 3), (brick, 4), (fused, 5), (tile, 3), (stream, 2), (fused, 3)):
+    frames = next(i for i in stream_tilings(16) if launches[i] == 1)
+    for ti, n in ((stream, 3), (brick, 4), (frames, 3), (fused, 5), (tile, 3), (frames, 2), (stream, 2), (fused, 3)):
         sim.set_tiling(ti)
         sim.step_philox(n, 777)
     sim.set_lattice(sim.get_lattice()[0])

@@ -25,6 +25,7 @@ def _tilings():
     k16 = [i for i, t in enumerate(var) if t[0] == 16]
     return {"unfused": [i for i in streams if launches[i] == 3][-1],
             "fused": next(i for i in streams if launches[i] == 2),
+            "frames": next(i for i in streams if launches[i] == 1),
             "brick_sparse": next(i for i in k16 if kinds[i][0] == 1 and launches[i] == 2),
             "brick_dense": next(i for i in k16 if kinds[i][0] == 1 and launches[i] == 1),
             "tile": next(i for i in k16 if kinds[i][0] == 0)}
