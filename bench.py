@@ -443,7 +443,6 @@ def main():
     kernels = frame_kernels(desc)
     longest = "sweep_pass_kernel<5>" if "sweep_pass_kernel<5>" in kernels else (
         "sweep_pass_kernel<3>" if "sweep_pass_kernel<3>" in kernels else kernels[0])
-    # the persistent kernel's committed traffic is per frame of its launch
     traffic = profiled_traffic(longest, w.name)
     per_kernel = {k: profiled_traffic(k, w.name) for k in kernels}
     frame_dram = sum(per_kernel.values()) if all(v is not None for v in per_kernel.values()) else None
@@ -489,6 +488,9 @@ def main():
                      "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes, "kernel": longest,
                      "achieved_over": "frame time (every launch of the frame)",
+                     # the persistent kernel runs every frame of a call in one launch: its bytes are
+                     # per frame of that launch
+                     "traffic_per": "frame" if desc.get("multi_frame") else "launch",
                      "frame_dram_bytes": frame_dram, "frame_dram_bytes_per_kernel": per_kernel,
                      "dram_frac": (frame_dram / frame_s / 1e9 / peak) if frame_dram else None,
                      "dram_frac_note": "the frame's profiled DRAM bytes (every launch, one cold-cache ncu capture) "
@@ -498,7 +500,7 @@ def main():
         "gpu_launches": launches_in_call(variant, args.steps),
         "clocks": clk,
         "diagnostics": {"events": int(diag[0]), "rejected_capacity": int(diag[1]), "event_cap": int(diag[2]),
-                        "fp64_selections": int(diag[3]), "ssa_voxels": int(diag[6])},
+                        "fp64_selections": int(diag[3]), "ssa_voxels": int(diag[6]), "wait_timeouts": int(diag[7])},
     }
     line.update(extras)
     print(json.dumps(line), flush=True)
