@@ -120,7 +120,8 @@ static const std::vector<KernelCfg>& all_cfgs() {
         // three / four blocks per SM
         stream_cfg(16, 4), stream_cfg(8, 4), stream_cfg(16, 5), stream_cfg(8, 5),
         // the fused stream as one persistent launch per step call (pass 1 and the fused pass of
-        // every frame as tasks of one counter), at three / four blocks per SM
+        // every frame as tasks of one counter) at three blocks per SM, a pass's groups taken
+        // heaviest first / in plane order
         stream_cfg(16, 6), stream_cfg(8, 6), stream_cfg(16, 7), stream_cfg(8, 7),
     };
     return v;
@@ -178,6 +179,7 @@ struct DeviceProd {
     // pass 1 and fused pass; the launch's task and exit counters; the completion base of the next
     // launch (completion values compare modulo 2^32)
     DevBuf<uint32_t> nbr, done1, done2, frames_ctr;
+    DevBuf<uint32_t> plane_order;  // the sorted position of each group in build (plane) order
     uint32_t frames_seq = 0;
     std::vector<WordGroup> h_groups;
     bool groups_sorted = false;  // groups dealt heaviest first (sorted once per group build)
@@ -688,6 +690,8 @@ static void sort_groups(DeviceProd* d) {
         }
         if (d->nbr.n != nb.size()) d->nbr.alloc(nb.size());
         CS_CUDA(cudaMemcpy(d->nbr.p, nb.data(), nb.size() * 4, cudaMemcpyHostToDevice));
+        if (d->plane_order.n != n) d->plane_order.alloc(n);
+        CS_CUDA(cudaMemcpy(d->plane_order.p, pos.data(), n * 4, cudaMemcpyHostToDevice));
         if (d->done1.n != n) {
             // fresh completion values: every group done up to the base 0
             d->done1.alloc(n);
@@ -916,7 +920,7 @@ static void launch_stream_frames(DeviceProd* d, uint32_t n) {
     const KernelCfg& cfg = all_cfgs()[d->cfg_index];
     const uint32_t ng = d->n_groups;
     if (n == 0 || ng == 0) return;
-    if (d->nbr.n != 4ull * ng || d->done1.n != ng || d->frames_ctr.n < 2)
+    if (d->nbr.n != 4ull * ng || d->done1.n != ng || d->plane_order.n != ng || d->frames_ctr.n < 2)
         throw Error(CS_ERR_STATE, "multi-frame sweep state missing (groups not sorted)");
     const size_t smem = cfg_smem(d, cfg);
     if (d->frames_occ_cfg != d->cfg_index) {
@@ -940,6 +944,7 @@ static void launch_stream_frames(DeviceProd* d, uint32_t n) {
     FP.sp[1].odst1 = P1.odst;
     FP.sp[1].dst1 = P1.dst;
     FP.nbr = d->nbr.p;
+    FP.order = stream_variant_plane_order(cfg.variant) ? d->plane_order.p : nullptr;
     FP.done1 = d->done1.p;
     FP.done2 = d->done2.p;
     FP.tasks = d->frames_ctr.p;

@@ -684,7 +684,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_frames_kernel(const __grid_con
         const uint32_t t_next = fetch();
         const uint32_t fi = t / per_frame, r = t - fi * per_frame;
         const bool yz = r >= ng;
-        const uint32_t g = yz ? r - ng : r;
+        const uint32_t rank = yz ? r - ng : r;
+        const uint32_t g = FP.order ? __ldg(FP.order + rank) : rank;
         if (yz || fi > 0u) {
             // lanes 0-4 wait for the group and its four neighbours
             const uint32_t* done = yz ? FP.done1 : FP.done2;
@@ -735,12 +736,13 @@ struct Variant {
     int NT, MINB, MINB3;  // threads per block, minimum resident blocks per SM of passes 0-2 and of pass 3
     bool fused;           // passes 2 and 3 as one launch (PASS_YZ at MINB3 blocks per SM)
     bool frames;          // the persistent multi-frame kernel at MINB3 blocks per SM (per-pass launches:
-                          // the fused ones of the same shape)
+                          // the fused ones of the same shape); variant 6 takes a pass's groups
+                          // heaviest first, variant 7 in plane order
 };
 // compiled launch shapes; pass 3 (reactions) needs more registers than the sweeps
 constexpr Variant kVariants[] = {{256, 2, 2, false, false}, {256, 4, 4, false, false}, {256, 4, 3, false, false},
                                  {256, 4, 2, false, false}, {256, 4, 3, true, false},  {256, 4, 4, true, false},
-                                 {256, 4, 3, true, true},   {256, 4, 4, true, true}};
+                                 {256, 4, 3, true, true},   {256, 4, 3, true, true}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 template <int K, int NT, int MINB, int MINB3>
@@ -771,8 +773,8 @@ void* fn_of(int variant, int pass) {
         case 1: return pass_fn<K, 256, 4, 4>(pass);
         case 2: return pass_fn<K, 256, 4, 3>(pass);
         case 3: return pass_fn<K, 256, 4, 2>(pass);
-        case 4: case 6: return pass_fn_fused<K, 256, 4, 3>(pass);
-        case 5: case 7: return pass_fn_fused<K, 256, 4, 4>(pass);
+        case 4: case 6: case 7: return pass_fn_fused<K, 256, 4, 3>(pass);
+        case 5: return pass_fn_fused<K, 256, 4, 4>(pass);
         default: return nullptr;
     }
 }
@@ -780,8 +782,7 @@ void* fn_of(int variant, int pass) {
 template <int K>
 void* frames_fn_of(int variant) {
     switch (variant) {
-        case 6: return reinterpret_cast<void*>(&sweep_frames_kernel<K, 256, 3>);
-        case 7: return reinterpret_cast<void*>(&sweep_frames_kernel<K, 256, 4>);
+        case 6: case 7: return reinterpret_cast<void*>(&sweep_frames_kernel<K, 256, 3>);
         default: return nullptr;
     }
 }
@@ -799,6 +800,7 @@ void* kernel_of(int K, int variant, int pass) {
 int stream_variant_count() { return kNumVariants; }
 bool stream_variant_fused(int variant) { return variant >= 0 && variant < kNumVariants && kVariants[variant].fused; }
 bool stream_variant_frames(int variant) { return variant >= 0 && variant < kNumVariants && kVariants[variant].frames; }
+bool stream_variant_plane_order(int variant) { return variant == 7; }
 int stream_variant_threads(int variant) { return variant >= 0 && variant < kNumVariants ? kVariants[variant].NT : 0; }
 
 // Launch with programmatic stream serialization (see wait_previous_launch).

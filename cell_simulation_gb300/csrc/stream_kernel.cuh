@@ -114,12 +114,15 @@ constexpr int PASS_YZ = 5;
 // task first waits until the tasks it reads from, and those that read what it overwrites, are
 // done: pass 1 of a group after the previous frame's fused pass of the group, of the groups with
 // the same rows at x - 1 and x + 1 and of the previous and next group of its plane; the fused pass
-// after this frame's pass 1 of the same five groups.
+// after this frame's pass 1 of the same five groups.  Within a pass the groups are taken heaviest
+// first, or in plane order (a wavefront in x, for lattices whose occupancy is spread evenly).
 struct FramesParams {
     StreamParams sp[2];    // [0] pass 1, [1] the fused Y and Z sweeps (parity 0's lattice buffers;
                            // parity 1's in in_occ1, odst1 and dst1)
     const uint32_t* nbr;   // per group: x - 1, x + 1, previous and next group of the plane, or
                            // 0xFFFFFFFF
+    const uint32_t* order; // the group of each task rank within a pass (plane order); null: the
+                           // groups' own order (heaviest first)
     uint32_t* done1;       // per group: seq + frame index + 1 of its last finished pass 1
     uint32_t* done2;       // ... of its last finished fused pass
     uint32_t* tasks;       // the launch's task counter, zero between launches
@@ -148,8 +151,10 @@ int stream_blocks_per_sm(int K, int variant, int pass, size_t smem);
 size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words);
 // Sets the kernel attributes (shared-memory size and carveout) of every pass.
 void stream_set_attrs(int K, int variant, size_t smem);
-// True when the variant runs in the persistent multi-frame form (stream_frames_launch).
+// True when the variant runs in the persistent multi-frame form (stream_frames_launch), and when
+// that form takes a pass's groups in plane order (FramesParams::order).
 bool stream_variant_frames(int variant);
+bool stream_variant_plane_order(int variant);
 // Resident blocks per SM of the multi-frame kernel of the variant (0: not compiled).
 int stream_frames_blocks_per_sm(int K, int variant, size_t smem);
 // Launches the multi-frame kernel; false when none is compiled for K and the variant.

@@ -16,14 +16,14 @@ pytestmark = pytest.mark.gpu
 def _variants(K):
     """The default step (Y and Z sweeps fused, three blocks per SM), the fused step at four blocks
     per SM, the three-launch sweep stream (Y and Z sweeps apart), the persistent multi-frame stream
-    at three and four blocks per SM and the 16-plane brick pass of slot count K."""
+    (groups heaviest first, and in plane order) and the 16-plane brick pass of slot count K."""
     kinds, launches, var = tiling_kinds(), tiling_launches(), tiling_variants()
     stream = [i for i, (t, k) in enumerate(zip(var, kinds)) if t[0] == K and k[0] == 2]
     fused = [i for i in stream if launches[i] == 2]
     apart = [i for i in stream if launches[i] == 3]
     frames = [i for i in stream if launches[i] == 1]
     brick = [i for i, (t, k) in enumerate(zip(var, kinds)) if t[0] == K and k == (1, 16)]
-    return {"fused3": fused[0], "fused4": fused[-1], "unfused": apart[-1], "frames3": frames[0], "frames4": frames[-1],
+    return {"fused3": fused[0], "fused4": fused[-1], "unfused": apart[-1], "frames": frames[0], "frames_plane": frames[-1],
             "brick16": brick[-1]}
 
 
@@ -67,6 +67,15 @@ def test_c3_256_cube_matches_oracle(orc):
         _check(_gpu_frames(configs.c3_multi_region().sim, 4, 0xC0FFEE, ti), want, tag)
 
 
+def test_c5_192_cube_matches_oracle(orc):
+    """The stiff 192^3 lattice (Z = 192: six words per row, five rows per group of 30 words; 12
+    species, 24 reactions up to k tau = 1.7): four frames in two step calls."""
+    want = _oracle_frames(orc, configs.c5_stiff().sim, 4, seed=4242)
+    assert want[2][0] > 0
+    for tag, ti in _variants(16).items():
+        _check(_gpu_frames(configs.c5_stiff().sim, 4, 4242, ti), want, tag)
+
+
 def test_c2_128_cube_matches_oracle(orc):
     """The 128^3 single cell (Z = 128: four words per row, eight rows per group): six frames."""
     want = _oracle_frames(orc, configs.c2_single_cell().sim, 6, seed=2024)
@@ -74,7 +83,7 @@ def test_c2_128_cube_matches_oracle(orc):
         _check(_gpu_frames(configs.c2_single_cell().sim, 6, 2024, ti, chunks=3), want, tag)
 
 
-@pytest.mark.parametrize("variant", ["fused3", "fused4", "unfused", "frames3", "frames4"])
+@pytest.mark.parametrize("variant", ["fused3", "fused4", "unfused", "frames", "frames_plane"])
 def test_c4_edge_range_matches_oracle(orc, variant):
     """Replicates with the ensemble's extreme and word-boundary edges (32, 33, 63, 64, 95, 96) and
     the ensemble's particle counts, rate multipliers and seeds, batched in one launch per pass."""
