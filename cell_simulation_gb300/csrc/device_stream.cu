@@ -636,10 +636,10 @@ __device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
-// Polls of a completion value before a task gives up (each poll is an L2 round trip plus a short
-// back-off: about a second in all, against a few microseconds for a real wait); then the task and
-// the warp's remaining tasks are abandoned and PD_WAIT_TIMEOUTS counts it.
-constexpr uint32_t kWaitPolls = 1u << 21;
+// Polls of a completion value before a task gives up (each poll is an L2 round trip plus a back-off
+// of at most 1 us: one to two seconds in all, against microseconds for a real wait); then the task
+// and the warp's remaining tasks are abandoned and PD_WAIT_TIMEOUTS counts it.
+constexpr uint32_t kWaitPolls = 1u << 20;
 
 // The persistent multi-frame form (FramesParams): pass 1 and the fused Y and Z sweeps of every
 // group for every frame of the launch, as tasks of one counter.
@@ -694,13 +694,16 @@ __global__ void __launch_bounds__(NT, MINB) sweep_frames_kernel(const __grid_con
             if (lane < 5) {
                 const uint32_t n = lane == 0 ? g : FP.nbr[4 * (size_t)g + (uint32_t)(lane - 1)];
                 if (n != 0xFFFFFFFFu) {
-                    uint32_t polls = 0u;
+                    // back-off doubling from 32 to 1024 ns, so that warps waiting far ahead (small
+                    // lattices, where most warps hold tasks of later frames) poll L2 rarely
+                    uint32_t polls = 0u, ns = 32u;
                     while ((int32_t)(ld_acquire_gpu(done + n) - want) < 0) {
                         if (++polls > kWaitPolls) {
                             late = true;
                             break;
                         }
-                        __nanosleep(64);
+                        __nanosleep(ns);
+                        ns = min(ns * 2u, 1024u);
                     }
                 }
             }
