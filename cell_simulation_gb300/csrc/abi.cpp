@@ -472,6 +472,14 @@ cs_status cs_synchronize(cs_sim* sim) {
     });
 }
 
+cs_status cs_debug_stall_group(cs_sim* sim, uint32_t group) {
+    return guarded([&] {
+        need(sim, "sim");
+        if (!sim->prod) throw Error(CS_ERR_STATE, "cs_debug_stall_group needs cs_prepare_for_gpu(CS_RNG_PHILOX)");
+        prod_debug_stall_group(sim->prod.get(), group);
+    });
+}
+
 cs_status cs_step_timed(cs_sim* sim, uint32_t n_steps, const uint32_t* itimes, float* ms) {
     return guarded([&] {
         need(sim, "sim");

@@ -181,6 +181,7 @@ struct DeviceProd {
     DevBuf<uint32_t> nbr, done1, done2, frames_ctr;
     DevBuf<uint32_t> plane_order;  // the sorted position of each group in build (plane) order
     uint32_t frames_seq = 0;
+    uint32_t stall_group = 0xFFFFFFFFu;  // cs_debug_stall_group: the next multi-frame launch's stalled group
     std::vector<WordGroup> h_groups;
     bool groups_sorted = false;  // groups dealt heaviest first (sorted once per group build)
     int stream_per_sm[4] = {0, 0, 0, 0};  // resident blocks per SM of the current stream passes
@@ -692,12 +693,13 @@ static void sort_groups(DeviceProd* d) {
         CS_CUDA(cudaMemcpy(d->nbr.p, nb.data(), nb.size() * 4, cudaMemcpyHostToDevice));
         if (d->plane_order.n != n) d->plane_order.alloc(n);
         CS_CUDA(cudaMemcpy(d->plane_order.p, pos.data(), n * 4, cudaMemcpyHostToDevice));
-        if (d->done1.n != n) {
-            // fresh completion values: every group done up to the base 0
-            d->done1.alloc(n);
-            d->done2.alloc(n);
-            CS_CUDA(cudaMemset(d->done1.p, 0, n * 4));
-            CS_CUDA(cudaMemset(d->done2.p, 0, n * 4));
+        if (d->done1.n != n + 1) {
+            // fresh completion values: every group done up to the base 0 (and one more entry that
+            // nothing writes, for cs_debug_stall_group)
+            d->done1.alloc(n + 1);
+            d->done2.alloc(n + 1);
+            CS_CUDA(cudaMemset(d->done1.p, 0, (n + 1) * 4));
+            CS_CUDA(cudaMemset(d->done2.p, 0, (n + 1) * 4));
             d->frames_seq = 0;
         }
         if (d->frames_ctr.n == 0) {
@@ -920,7 +922,7 @@ static void launch_stream_frames(DeviceProd* d, uint32_t n) {
     const KernelCfg& cfg = all_cfgs()[d->cfg_index];
     const uint32_t ng = d->n_groups;
     if (n == 0 || ng == 0) return;
-    if (d->nbr.n != 4ull * ng || d->done1.n != ng || d->plane_order.n != ng || d->frames_ctr.n < 2)
+    if (d->nbr.n != 4ull * ng || d->done1.n != ng + 1u || d->plane_order.n != ng || d->frames_ctr.n < 2)
         throw Error(CS_ERR_STATE, "multi-frame sweep state missing (groups not sorted)");
     const size_t smem = cfg_smem(d, cfg);
     if (d->frames_occ_cfg != d->cfg_index) {
@@ -952,10 +954,20 @@ static void launch_stream_frames(DeviceProd* d, uint32_t n) {
     FP.reset = d->counters.p;
     FP.n_reset = (uint32_t)d->counters.n;
     FP.n_groups = ng;
+    FP.fault = d->counts.p + (size_t)d->n_rep * d->S1;
     // tasks per launch: 2 ng per frame, and every warp fetches once past the last one, so the
     // counter stays below 2^32 with room for the largest grid
     const uint32_t chunk = (uint32_t)std::max<uint64_t>(
         1, std::min<uint64_t>((0xFFFFFFFFull - (1ull << 20)) / (2ull * ng), 1ull << 30));
+    uint32_t stalled[4];
+    const bool stall = d->stall_group < ng;
+    if (stall) {
+        // the group's neighbour links point at the entry that nothing writes, for this call
+        CS_CUDA(cudaStreamSynchronize(d->stream));
+        const uint32_t dummy[4] = {ng, ng, ng, ng};
+        CS_CUDA(cudaMemcpy(stalled, d->nbr.p + 4ull * d->stall_group, 16, cudaMemcpyDeviceToHost));
+        CS_CUDA(cudaMemcpy(d->nbr.p + 4ull * d->stall_group, dummy, 16, cudaMemcpyHostToDevice));
+    }
     for (uint32_t k = 0; k < n;) {
         const uint32_t m = std::min(n - k, chunk);
         FP.n_frames = m;
@@ -968,7 +980,14 @@ static void launch_stream_frames(DeviceProd* d, uint32_t n) {
         d->cur = (int)(((uint32_t)d->cur + m) & 1u);
         k += m;
     }
+    if (stall) {
+        CS_CUDA(cudaStreamSynchronize(d->stream));
+        CS_CUDA(cudaMemcpy(d->nbr.p + 4ull * d->stall_group, stalled, 16, cudaMemcpyHostToDevice));
+        d->stall_group = 0xFFFFFFFFu;
+    }
 }
+
+void prod_debug_stall_group(DeviceProd* d, uint32_t group) { d->stall_group = group; }
 
 static void launch_stream_frame(DeviceProd* d, const KernelCfg& cfg, const ProdParams& P, int rep, int parity) {
     const bool fused = stream_variant_fused(cfg.variant);
@@ -1075,7 +1094,8 @@ static DeviceProd* prod_alloc(const Model& m, int device, const std::vector<RepD
     CS_CUDA(cudaMemcpy(d->reps.p, d->h_reps.data(), d->h_reps.size() * sizeof(RepDesc), cudaMemcpyHostToDevice));
     for (int b = 0; b < 2; b++) d->occ[b].alloc(d->occ_words);
     d->occ_valid = false;
-    d->counts.alloc((size_t)d->n_rep * d->S1);
+    // the counts, then one word: dependency waits of the multi-frame kernel that timed out
+    d->counts.alloc((size_t)d->n_rep * d->S1 + 1);
     d->diag.alloc(PD_N);
     d->counters.alloc((size_t)2 * kCtrPerParity * (1 + d->n_rep));
     d->stepbuf.alloc(2);
@@ -1352,12 +1372,17 @@ void prod_step(DeviceProd* d, uint32_t n_steps, uint64_t seed, int precision, ui
     }
 }
 
+static const char* const kWaitFault =
+    "the multi-frame sweep kernel abandoned frames after a dependency wait timed out; the lattice is not valid";
+
 void prod_get_counts(DeviceProd* d, int64_t* counts) {
     DeviceGuard g(d->device);
     const size_t n = (size_t)d->n_rep * d->S1;
-    if (!d->h_counts) CS_CUDA(cudaMallocHost(&d->h_counts, n * 8));
-    CS_CUDA(cudaMemcpyAsync(d->h_counts, d->counts.p, n * 8, cudaMemcpyDeviceToHost, d->stream));
+    if (!d->h_counts) CS_CUDA(cudaMallocHost(&d->h_counts, (n + 1) * 8));
+    // the counts and the wait-timeout word in one copy
+    CS_CUDA(cudaMemcpyAsync(d->h_counts, d->counts.p, (n + 1) * 8, cudaMemcpyDeviceToHost, d->stream));
     CS_CUDA(cudaStreamSynchronize(d->stream));
+    if (d->h_counts[n]) throw Error(CS_ERR_CUDA, kWaitFault);
     for (size_t i = 0; i < n; i++) counts[i] = (int64_t)d->h_counts[i];
 }
 
@@ -1407,7 +1432,10 @@ void prod_get_diag(DeviceProd* d, uint32_t* diag, uint32_t n) {
 
 void prod_sync(DeviceProd* d) {
     DeviceGuard g(d->device);
+    unsigned long long fault = 0;
+    CS_CUDA(cudaMemcpyAsync(&fault, d->counts.p + (size_t)d->n_rep * d->S1, 8, cudaMemcpyDeviceToHost, d->stream));
     CS_CUDA(cudaStreamSynchronize(d->stream));
+    if (fault) throw Error(CS_ERR_CUDA, kWaitFault);
 }
 
 }  // namespace cellsim

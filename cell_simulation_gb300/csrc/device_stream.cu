@@ -709,7 +709,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_frames_kernel(const __grid_con
             }
             __syncwarp();
             if (__any_sync(0xffffffffu, late)) {
-                if (lane == 0) atomicAdd(P.diag + PD_WAIT_TIMEOUTS, 1u);
+                if (lane == 0) {
+                    atomicAdd(P.diag + PD_WAIT_TIMEOUTS, 1u);
+                    atomicAdd(FP.fault, 1ull);
+                }
                 break;
             }
         }

@@ -157,6 +157,7 @@ void prod_get_lattice(DeviceProd* d, const Model& m, uint32_t* slots, uint32_t* 
 void prod_set_lattice(DeviceProd* d, const Model& m, const uint32_t* slots);
 void prod_get_diag(DeviceProd* d, uint32_t* diag, uint32_t n);
 void prod_sync(DeviceProd* d);
+void prod_debug_stall_group(DeviceProd* d, uint32_t group);
 
 DeviceProd* prod_ensemble_create(const Model& m, uint32_t n, const uint32_t* res, const uint64_t* seeds, const float* mult,
                                  const uint32_t* init_counts, int device);

@@ -128,6 +128,7 @@ struct FramesParams {
     uint32_t* tasks;       // the launch's task counter, zero between launches
     uint32_t* exits;       // warps of the launch that have finished, zero between launches
     uint32_t* reset;       // queue counters of the per-pass launches, cleared at the start
+    unsigned long long* fault;  // counts waits that timed out (the host then reports an error)
     uint32_t n_reset;
     uint32_t n_groups;
     uint32_t n_frames;     // n_frames * 2 * n_groups + the launch's warps < 2^32

@@ -101,6 +101,7 @@ SIGNATURES = {
     "cs_pop_stats": (st, [P, C.POINTER(StatSampleC), C.c_uint32, u32p]),
     "cs_get_diagnostics": (st, [P, u32p, C.c_uint32]),
     "cs_synchronize": (st, [P]),
+    "cs_debug_stall_group": (st, [P, C.c_uint32]),
     "cs_ref_frame_noalloc": (st, [C.POINTER(RefFrameNoAllocArgsC)]),
     "cs_step_timed": (st, [P, C.c_uint32, u32p, f32p]),
     "cs_step_philox_timed": (st, [P, C.c_uint32, C.c_uint64, f32p]),

@@ -350,6 +350,10 @@ class Simulation:
     def synchronize(self) -> None:
         N.check(self._lib.cs_synchronize(self._h))
 
+    def debug_stall_group(self, group: int) -> None:
+        """Test hook (cs_debug_stall_group): the next multi-frame launch's waits for `group` run out."""
+        N.check(self._lib.cs_debug_stall_group(self._h, group))
+
     def _drain_stats(self) -> None:
         buf = (N.StatSampleC * 256)()
         names = None

@@ -213,9 +213,19 @@ cs_status cs_pop_stats(cs_sim* sim, cs_stat_sample* out, uint32_t capacity, uint
  * hit the event cap, [3] FP64 selections, [4] bricks spilled to the second
  * brick pass, [5] bricks lost (always 0), [6] voxels that ran the SSA, [7]
  * waits of the multi-frame sweep kernel that timed out (always 0; nonzero
- * means its frames were abandoned and the lattice is not valid). */
+ * means its frames were abandoned and the lattice is not valid: cs_get_counts
+ * and cs_synchronize then fail with CS_ERR_CUDA). */
 cs_status cs_get_diagnostics(cs_sim* sim, uint32_t* diag, uint32_t n);
+/* Waits for the handle's work.  Fails with CS_ERR_CUDA (as cs_get_counts does)
+ * when the multi-frame sweep kernel abandoned frames after a dependency wait
+ * timed out; the lattice is then not valid (upload a new one). */
 cs_status cs_synchronize(cs_sim* sim);
+/* Test hook of the multi-frame sweep kernel's bounded waits: the next
+ * multi-frame launch makes word group `group` (in the current group order)
+ * also wait on a completion value that nothing writes, so that its waits run
+ * out, the launch abandons its frames and the host reports the error.  No
+ * reference counterpart. */
+cs_status cs_debug_stall_group(cs_sim* sim, uint32_t group);
 
 /* ---------------- allocation-free reference-RNG frame ---------------- */
 /* Arguments of cs_ref_frame_noalloc.  Every pointer is a device pointer on
