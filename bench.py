@@ -3,8 +3,9 @@
 Default workload: the 256^3, 16-slot, 16-species / 30-reaction multi-region
 lattice (the roofline configuration), production path (Philox, FP32
 propensities with FP64 clock), the autotuned step variant (the sweep stream:
-two or three launches per frame).  `value` is voxel-steps/s over the whole
-job with the lattice resident in HBM; the lattice (2 x 256 MiB) is larger
+two or three launches per frame, or one persistent launch per call).  `value`
+is voxel-steps/s over the whole job with the lattice resident in HBM; the
+lattice (2 x 256 MiB) is larger
 than L2, so no flush is needed between timed frames.  Also reported: the
 batched 512-replicate ensemble vs the plain one-launch-group-per-replicate
 path (replicate-steps/s), the reference-RNG CUDA path on the same lattice,
