@@ -715,13 +715,13 @@ static uint32_t thr_words(const DeviceProd* d) {
 }
 
 static size_t cfg_smem(const DeviceProd* d, const KernelCfg& cfg) {
-    if (cfg.kind == KIND_STREAM) return stream_smem(cfg.NT, d->S1, thr_words(d));
+    if (cfg.kind == KIND_STREAM) return stream_pass_smem(cfg.variant, 2, d->S1, thr_words(d));  // the largest pass
     return cfg.smem(d->S1, thr_words(d));
 }
 
 static void set_attrs(const DeviceProd* d, const KernelCfg& cfg) {
     if (cfg.kind == KIND_STREAM) {
-        stream_set_attrs(cfg.K, cfg.variant, cfg_smem(d, cfg));
+        stream_set_attrs(cfg.K, cfg.variant, d->S1, thr_words(d));
         return;
     }
     CS_CUDA(cudaFuncSetAttribute(cfg.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg_smem(d, cfg)));
@@ -883,10 +883,12 @@ static void launch_stream_pass(DeviceProd* d, const KernelCfg& cfg, const ProdPa
     StreamParams S = stream_params(d, cfg, P, rep, parity, pass);
     const uint32_t ng = S.n_groups;
     if (ng == 0) return;
-    const size_t smem = cfg_smem(d, cfg);
+    const size_t smem = stream_pass_smem(cfg.variant, pass, d->S1, thr_words(d));
     const uint32_t nw = (uint32_t)cfg.NT / 32u;
     if (d->stream_occ_cfg != d->cfg_index) {
-        for (int q = 0; q < 4; q++) d->stream_per_sm[q] = stream_blocks_per_sm(cfg.K, cfg.variant, q, cfg_smem(d, cfg));
+        for (int q = 0; q < 4; q++)
+            d->stream_per_sm[q] =
+                stream_blocks_per_sm(cfg.K, cfg.variant, q, stream_pass_smem(cfg.variant, q, d->S1, thr_words(d)));
         d->stream_occ_cfg = d->cfg_index;
     }
     const int per_sm = d->stream_per_sm[pass];
@@ -924,7 +926,7 @@ static void launch_stream_frames(DeviceProd* d, uint32_t n) {
     if (n == 0 || ng == 0) return;
     if (d->nbr.n != 4ull * ng || d->done1.n != ng + 1u || d->plane_order.n != ng || d->frames_ctr.n < 2)
         throw Error(CS_ERR_STATE, "multi-frame sweep state missing (groups not sorted)");
-    const size_t smem = cfg_smem(d, cfg);
+    const size_t smem = stream_pass_smem(cfg.variant, 4, d->S1, thr_words(d));
     if (d->frames_occ_cfg != d->cfg_index) {
         d->frames_per_sm = stream_frames_blocks_per_sm(cfg.K, cfg.variant, smem);
         d->frames_occ_cfg = d->cfg_index;

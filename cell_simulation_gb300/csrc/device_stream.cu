@@ -42,9 +42,17 @@ constexpr int PEND_WORDS = 4 + 8 * PEND;
 // the item list (u16)
 __host__ __device__ constexpr size_t stream_warp_words() { return (size_t)NF * 32 + 96 + LIST / 2 + PEND_WORDS; }
 
-size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words) {
+// Records of a group's Y sweep (its z-decisions) that the fused pass keeps in the warp's shared
+// memory for its Z sweep, instead of a round trip through L2: the first 96 of the group's records
+// at three blocks per SM (C3: 0.1480 -> 0.1462 ms per frame in the multi-frame form, the two-launch
+// form unchanged); none at four blocks per SM, where the smaller shared memory left per block cost
+// the 512-replicate ensemble more (0.352 -> 0.357 ms with 32) than the staging saved; 0 for the
+// other passes.
+__host__ __device__ constexpr int stage_recs(int PASS, int MINB) { return PASS == PASS_YZ && MINB < 4 ? 96 : 0; }
+
+size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words, int recs) {
     (void)S1;
-    return ((size_t)(NT / 32) * stream_warp_words() + PD_N + thr_words) * 4;
+    return ((size_t)(NT / 32) * (stream_warp_words() + (size_t)recs * 8) + PD_N + thr_words) * 4;
 }
 
 // NC: the records were written by an earlier launch (read-only path); else
@@ -100,6 +108,8 @@ struct WarpArea {
     const uint32_t* thr;  // threshold table (shared memory or global)
     uint32_t gw;          // the warp's index in the launch
     int lane;
+    uint4* stage;         // [2 n_stage] the fused pass's staged z-decision records
+    uint32_t n_stage;
 };
 
 // A word written earlier: by an earlier launch (plain load), or (COH) possibly earlier in this
@@ -135,6 +145,33 @@ __device__ __forceinline__ void stream_group(const StreamParams& SP, const WarpA
     const uint32_t* const in_occ = par ? SP.in_occ1 : SP.in.occ;
     uint32_t* const odst = par ? SP.odst1 : P.odst;
     uint8_t* const dst = par ? SP.dst1 : P.dst;
+    // the fused pass's z-decision records: the group's first A.n_stage in shared memory, the rest
+    // in rec_mid (read through L2: this launch wrote them)
+    auto mid_store = [&](uint32_t ri, uint32_t rb, const Vox<K>& c, const uint4& t) {
+        const uint32_t rel = ri - rb;
+        if (rel < A.n_stage) {
+            uint4 a;
+            a.x = (uint32_t)c.w[0];
+            a.y = (uint32_t)(c.w[0] >> 32);
+            a.z = K == 16 ? (uint32_t)c.w[K / 8 - 1] : 0u;
+            a.w = K == 16 ? (uint32_t)(c.w[K / 8 - 1] >> 32) : 0u;
+            A.stage[2 * rel] = a;
+            A.stage[2 * rel + 1] = t;
+        } else {
+            rec_store<K>(SP.rec_mid, ri, c, t);
+        }
+    };
+    auto mid_load = [&](uint32_t ri, uint32_t rb, Vox<K>& c, uint4& t) {
+        const uint32_t rel = ri - rb;
+        if (rel < A.n_stage) {
+            const uint4 a = A.stage[2 * rel];
+            t = A.stage[2 * rel + 1];
+            c.w[0] = (uint64_t)a.x | ((uint64_t)a.y << 32);
+            if constexpr (K == 16) c.w[K / 8 - 1] = (uint64_t)a.z | ((uint64_t)a.w << 32);
+        } else {
+            rec_load<K, false>(SP.rec_mid, ri, c, t);
+        }
+    };
     const WordGroup G = SP.groups[g];
     const RepDesc rd = P.reps[G.rep];
     const int X = (int)rd.X, Y = (int)rd.Y, Z = (int)rd.Z;
@@ -350,7 +387,8 @@ __device__ __forceinline__ void stream_group(const StreamParams& SP, const WarpA
                 uint4 tw = make_uint4(0u, 0u, 0u, 0u);
                 const bool own_in = (occ & bit) != 0u;
                 if (own_in) {
-                    rec_load<K, !COH && !(CH && PP == 3)>(rin, f_bw.x + below(f_bw.y, bit), own, tw);
+                    if constexpr (CH && PP == 3) mid_load(f_bw.x + below(f_bw.y, bit), (uint32_t)G.rbase, own, tw);
+                    else rec_load<K, !COH>(rin, f_bw.x + below(f_bw.y, bit), own, tw);
                     dme = tw.x;
                 }
                 // a neighbour's record is needed when it sends to this voxel or receives from it
@@ -386,12 +424,14 @@ __device__ __forceinline__ void stream_group(const StreamParams& SP, const WarpA
                 }
                 if (need_lo) {
                     uint4 tl;
-                    rec_load<K, !COH && !(CH && PP == 3)>(rin, ilo, lo, tl);
+                    if constexpr (CH && PP == 3) mid_load(ilo, (uint32_t)G.rbase, lo, tl);
+                    else rec_load<K, !COH>(rin, ilo, lo, tl);
                     dlo = tl.x;
                 }
                 if (need_hi) {
                     uint4 th;
-                    rec_load<K, !COH && !(CH && PP == 3)>(rin, ihi, hi, th);
+                    if constexpr (CH && PP == 3) mid_load(ihi, (uint32_t)G.rbase, hi, th);
+                    else rec_load<K, !COH>(rin, ihi, hi, th);
                     dhi = th.x;
                 }
                 const uint32_t vs = PP == 1 ? YZ : PP == 2 ? (uint32_t)Z : 1u;
@@ -415,7 +455,8 @@ __device__ __forceinline__ void stream_group(const StreamParams& SP, const WarpA
                         const uint32_t chi = PP == 1 ? code(uc, x, yy + 1, zz) : code(uc, x, yy, zz + 1);
                         const uint32_t d =
                             decide_moves<K>(r, v, frame, (uint32_t)PP, trow(rs, clo), trow(rs, chi), k0, k1, wd);
-                        rec_store<K>(rout, ri, r, make_uint4(d, wn1, wn2, 0u));
+                        if constexpr (CH && PP == 2) mid_store(ri, (uint32_t)G.rbase, r, make_uint4(d, wn1, wn2, 0u));
+                        else rec_store<K>(rout, ri, r, make_uint4(d, wn1, wn2, 0u));
                         atomicOr(acc + i, bit);
                         if (d & 0xFFFFu) atomicOr(acc + 32 + i, bit);
                         if (d >> 16) atomicOr(acc + 64 + i, bit);
@@ -562,11 +603,13 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     extern __shared__ __align__(16) uint32_t sm[];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const uint32_t S1 = P.T.S1, NC = P.T.NC;
-    uint32_t* f = sm + (size_t)w * stream_warp_words();  // [NF][32]
+    constexpr int STAGE = stage_recs(PASS, MINB);
+    constexpr size_t WSTRIDE = stream_warp_words() + (size_t)STAGE * 8;  // u32 words of a warp's area
+    uint32_t* f = sm + (size_t)w * WSTRIDE;  // [NF][32]
     uint32_t* acc = f + NF * 32;                            // [3][32]: content, movers down, movers up
     uint16_t* list = reinterpret_cast<uint16_t*>(acc + 96);
     uint32_t* pend = acc + 96 + LIST / 2;  // [PEND_WORDS]
-    uint32_t* s_diag = sm + (size_t)NW * stream_warp_words();  // [PD_N]
+    uint32_t* s_diag = sm + (size_t)NW * WSTRIDE;  // [PD_N]
     uint32_t* s_thr = s_diag + PD_N;
     allow_next_launch();
     const uint32_t* thr = P.T.thr;
@@ -585,7 +628,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_pass_kernel(const StreamParams
     }
     __syncthreads();
     const uint32_t TW = gridDim.x * NW;
-    const WarpArea A{f, acc, list, pend, s_diag, thr, blockIdx.x * NW + (uint32_t)w, lane};
+    const WarpArea A{f, acc, list, pend, s_diag, thr, blockIdx.x * NW + (uint32_t)w, lane,
+                     reinterpret_cast<uint4*>(f + stream_warp_words()), (uint32_t)STAGE};
     // groups from the pass's counter (one atomic per group, fetched a group ahead), else round-robin
     auto fetch = [&]() -> uint32_t {
         uint32_t q = 0u;
@@ -652,11 +696,13 @@ __global__ void __launch_bounds__(NT, MINB) sweep_frames_kernel(const __grid_con
     extern __shared__ __align__(16) uint32_t sm[];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const uint32_t S1 = P.T.S1, NC = P.T.NC;
-    uint32_t* f = sm + (size_t)w * stream_warp_words();
+    constexpr int STAGE = stage_recs(PASS_YZ, MINB);
+    constexpr size_t WSTRIDE = stream_warp_words() + (size_t)STAGE * 8;
+    uint32_t* f = sm + (size_t)w * WSTRIDE;
     uint32_t* acc = f + NF * 32;
     uint16_t* list = reinterpret_cast<uint16_t*>(acc + 96);
     uint32_t* pend = acc + 96 + LIST / 2;
-    uint32_t* s_diag = sm + (size_t)NW * stream_warp_words();
+    uint32_t* s_diag = sm + (size_t)NW * WSTRIDE;
     uint32_t* s_thr = s_diag + PD_N;
     allow_next_launch();
     const uint32_t* thr = P.T.thr;
@@ -672,7 +718,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_frames_kernel(const __grid_con
     if (blockIdx.x == 0 && tid == 0)
         for (uint32_t i = 0; i < FP.n_reset; i++) FP.reset[i] = 0u;
     __syncthreads();
-    const WarpArea A{f, acc, list, pend, s_diag, thr, blockIdx.x * NW + (uint32_t)w, lane};
+    const WarpArea A{f, acc, list, pend, s_diag, thr, blockIdx.x * NW + (uint32_t)w, lane,
+                     reinterpret_cast<uint4*>(f + stream_warp_words()), (uint32_t)STAGE};
     const uint32_t ng = FP.n_groups, per_frame = 2u * ng, total = FP.n_frames * per_frame;
     auto fetch = [&]() -> uint32_t {
         uint32_t q = 0u;
@@ -832,6 +879,13 @@ bool stream_launch(int K, int variant, int pass, int grid, size_t smem, cudaStre
     return true;
 }
 
+size_t stream_pass_smem(int variant, int pass, uint32_t S1, uint32_t thr_words) {
+    const Variant& v = kVariants[variant];
+    // the fused pass (launched as pass 2) and the multi-frame kernel (pass 4 here) stage records
+    const bool yz = v.fused && (pass == 2 || pass == 4);
+    return stream_smem(v.NT, S1, thr_words, yz ? stage_recs(PASS_YZ, v.MINB3) : 0);
+}
+
 int stream_blocks_per_sm(int K, int variant, int pass, size_t smem) {
     void* fn = kernel_of(K, variant, pass);
     if (!fn) return 0;
@@ -840,10 +894,11 @@ int stream_blocks_per_sm(int K, int variant, int pass, size_t smem) {
     return n;
 }
 
-void stream_set_attrs(int K, int variant, size_t smem) {
+void stream_set_attrs(int K, int variant, uint32_t S1, uint32_t thr_words) {
     for (int pass = 0; pass < 5; pass++) {
         void* fn = pass < 4 ? kernel_of(K, variant, pass) : frames_kernel_of(K, variant);
         if (!fn) continue;
+        const size_t smem = stream_pass_smem(variant, pass, S1, thr_words);
         CS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         CS_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     }

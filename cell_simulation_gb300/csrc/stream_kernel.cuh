@@ -148,10 +148,12 @@ bool stream_variant_fused(int variant);
 bool stream_launch(int K, int variant, int pass, int grid, size_t smem, cudaStream_t s, const StreamParams& SP);
 // Resident blocks per SM of that kernel with `smem` dynamic shared memory.
 int stream_blocks_per_sm(int K, int variant, int pass, size_t smem);
-// Dynamic shared memory of one block of NT threads.
-size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words);
+// Dynamic shared memory of one block of NT threads whose warps stage `recs` records each.
+size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words, int recs);
+// ... of pass `pass` of a variant (0-3 as stream_launch; 4: the multi-frame kernel).
+size_t stream_pass_smem(int variant, int pass, uint32_t S1, uint32_t thr_words);
 // Sets the kernel attributes (shared-memory size and carveout) of every pass.
-void stream_set_attrs(int K, int variant, size_t smem);
+void stream_set_attrs(int K, int variant, uint32_t S1, uint32_t thr_words);
 // True when the variant runs in the persistent multi-frame form (stream_frames_launch), and when
 // that form takes a pass's groups in plane order (FramesParams::order).
 bool stream_variant_frames(int variant);
