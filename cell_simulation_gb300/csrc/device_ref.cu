@@ -685,13 +685,119 @@ __global__ void ref_sp_serial(RefParams p, RefSparse sp, uint8_t* __restrict__ s
 }
 
 // The reaction pass on one voxel and its bit in act bitmap c ^ 1.
+// The reaction tables of ref_cme_voxel staged in shared memory by the reaction pass.
+struct RefTables {
+    const uint32_t* reactants;  // [R+1][3]
+    const float* rates;         // [R+1]
+    const int32_t* stoich;      // [R+1][S1]
+};
+
+// ref_cme_voxel with the tables in shared memory (T) and the voxel's concentration row copied into
+// the thread's shared-memory row `row` while it is evaluated (every change is written through to
+// the global row): the same operations in the same order, so the same results, with the
+// propensity and selection loops reading shared memory instead of about a hundred dependent
+// global loads per voxel.
+__device__ __forceinline__ void ref_cme_voxel_rows(const RefParams& p, const RefTables& T, uint64_t v,
+                                                   uint8_t* __restrict__ slots, uint32_t* __restrict__ occ,
+                                                   int32_t* __restrict__ conc, uint32_t itime, int32_t* s_delta,
+                                                   int32_t* row) {
+    const uint32_t K = p.K, S1 = p.S1, R = p.R;
+    const uint32_t S = S1 - 1;
+    uint32_t x, y, z;
+    ref_coords(p, (uint32_t)v, x, y, z);
+    int32_t* c = conc + v * S1;
+    for (uint32_t s = 0; s < S1; s++) row[s] = c[s];
+    if (row[0] != 1) {  // stored only when it changes: an unchanged row is not written back
+        row[0] = 1;
+        c[0] = 1;
+    }
+    auto prop_of = [&](uint32_t r) -> float {
+        const uint32_t prod = (uint32_t)row[T.reactants[r * 3]] * (uint32_t)row[T.reactants[r * 3 + 1]] *
+                              (uint32_t)row[T.reactants[r * 3 + 2]];
+        return __fmul_rn(T.rates[r], __int2float_rn((int32_t)prod));
+    };
+    float total = 0.0f;
+    for (uint32_t r = 1; r <= R; r++) total = __fadd_rn(total, prop_of(r));
+    const RefSlots snap = rs_load(slots + v * K, K);
+    RefSlots sl = snap;
+    uint32_t state = d_pcg(itime + x * y + z);
+    float r1 = d_uniform_float(state);
+    float fire_p = __fsub_rn(1.0f, d_expf(__fmul_rn(-total, p.tau)));
+    if (r1 <= fire_p) {
+        atomicAdd(&s_delta[S1], 1);
+        float r2 = d_uniform_float(state + 1u);
+        // selection over cum[i] = cum[i-1] + a_i, normalised for i < R (cme.wgsl:50-52,70-73)
+        uint32_t i = 0;
+        float run = 0.0f;
+        while (i < R) {
+            if (!(r2 > __fdiv_rn(run, total))) break;
+            i++;
+            run = __fadd_rn(run, prop_of(i));
+        }
+        const int32_t* st = T.stoich + (size_t)i * S1;
+        uint32_t j = 0;
+        int32_t new_occ = (int32_t)occ[v];
+        uint64_t ri = v * K;  // reservoirs[idx_lattice], cme.wgsl:80
+        uint32_t resv = (ri < p.V) ? p.reservoir[ri] : 0u;
+        bool rolled = false;
+        for (uint32_t s = 1; s <= S && !rolled; s++) {
+            if (resv == s) continue;
+            int32_t d = st[s];
+            row[s] = (int32_t)((uint32_t)row[s] + (uint32_t)d);
+            if (d) c[s] = row[s];
+            new_occ = (int32_t)((uint32_t)new_occ + (uint32_t)d);
+            if (d) atomicAdd(&s_delta[s], d);
+            int32_t cc = row[s];
+            while (cc > 0) {
+                rs_set(sl, j, s);
+                cc--;
+                j++;
+                if (j >= K) {
+                    sl = snap;
+                    for (uint32_t s2 = 1; s2 <= s; s2++) {
+                        int32_t d2 = st[s2];
+                        row[s2] = (int32_t)((uint32_t)row[s2] - (uint32_t)d2);
+                        if (d2) {
+                            c[s2] = row[s2];
+                            atomicAdd(&s_delta[s2], -d2);
+                        }
+                    }
+                    atomicAdd(&s_delta[S1 + 1], 1);
+                    rolled = true;
+                    break;
+                }
+            }
+        }
+        if (!rolled) {
+            occ[v] = (uint32_t)new_occ;
+            while (j < K) rs_set(sl, j++, 0u);
+        }
+    }
+    // stable move of the non-zero slots to the front
+    RefSlots out{0ull, 0ull};
+    uint32_t jj = 0;
+    for (uint32_t s = 0; s < K; s++) {
+        const uint32_t q = rs_get(sl, s);
+        if (q != 0u) rs_set(out, jj++, q);
+    }
+    if (out.lo != snap.lo || out.hi != snap.hi) rs_store(slots + v * K, K, out);
+}
+
+// rows: the staged tables T and the thread's shared-memory concentration row `row` are used (else,
+// when they do not fit, the global-memory form)
 __device__ __forceinline__ void ref_sp_react(const RefParams& p, const RefSparse& sp, uint32_t v, uint8_t* slots,
-                                             uint32_t* occ, int32_t* conc, uint32_t itime, int32_t* s_delta) {
-    ref_cme_voxel(p, v, slots, occ, conc, itime, s_delta);
+                                             uint32_t* occ, int32_t* conc, uint32_t itime, int32_t* s_delta,
+                                             bool rows, const RefTables& T, int32_t* row) {
     const uint32_t K = p.K, S1 = p.S1;
+    const int32_t* c = conc + (size_t)v * S1;
+    if (rows) {
+        ref_cme_voxel_rows(p, T, v, slots, occ, conc, itime, s_delta, row);
+        c = row;
+    } else {
+        ref_cme_voxel(p, v, slots, occ, conc, itime, s_delta);
+    }
     const RefSlots sl = rs_load(slots + (size_t)v * K, K);
     bool keep = occ[v] != 0u || (sl.lo | sl.hi) != 0ull;
-    const int32_t* c = conc + (size_t)v * S1;
     for (uint32_t s = 1; s < S1 && !keep; s++) keep |= c[s] != 0;
     if (keep) set_bit(act_next(sp), v);
 }
@@ -702,12 +808,24 @@ __device__ __forceinline__ void ref_sp_react(const RefParams& p, const RefSparse
 __global__ void __launch_bounds__(256) ref_sp_cme(RefParams p, RefSparse sp, uint8_t* __restrict__ slots,
                                                   uint32_t* __restrict__ occ, int32_t* __restrict__ conc,
                                                   const uint32_t* __restrict__ itimes, uint32_t step, uint32_t dense,
-                                                  int32_t* stat, uint32_t* diag, uint32_t* contended) {
-    extern __shared__ int32_t s_delta[];  // [S1] + 2 counters
+                                                  int32_t* stat, uint32_t* diag, uint32_t* contended, uint32_t rows) {
+    extern __shared__ int32_t s_delta[];  // [S1] + 2 counters, then (rows) the tables and the rows
     for (uint32_t s = threadIdx.x; s < p.S1 + 2; s += blockDim.x) s_delta[s] = 0;
     if (grid_tid() == 0) {
         *contended = 0u;  // every reader of this frame's flag has run
         sp.cnt[0] = 0u;
+    }
+    RefTables T{};
+    int32_t* row = nullptr;
+    if (rows) {
+        uint32_t* s_re = reinterpret_cast<uint32_t*>(s_delta + p.S1 + 2);
+        float* s_rate = reinterpret_cast<float*>(s_re + 3 * (p.R + 1));
+        int32_t* s_st = reinterpret_cast<int32_t*>(s_rate + (p.R + 1));
+        for (uint32_t i = threadIdx.x; i < 3 * (p.R + 1); i += blockDim.x) s_re[i] = p.reactants[i];
+        for (uint32_t i = threadIdx.x; i < p.R + 1; i += blockDim.x) s_rate[i] = p.rates[i];
+        for (uint32_t i = threadIdx.x; i < (p.R + 1) * p.S1; i += blockDim.x) s_st[i] = p.stoich[i];
+        T = RefTables{s_re, s_rate, s_st};
+        row = s_st + (p.R + 1) * p.S1 + threadIdx.x * p.S1;
     }
     __syncthreads();
     const uint32_t itime = __ldg(itimes + step);
@@ -717,11 +835,11 @@ __global__ void __launch_bounds__(256) ref_sp_cme(RefParams p, RefSparse sp, uin
     }
     if (dense) {
         for (uint32_t v = grid_tid(); v < (uint32_t)p.V; v += grid_threads())
-            ref_sp_react(p, sp, v, slots, occ, conc, itime, s_delta);
+            ref_sp_react(p, sp, v, slots, occ, conc, itime, s_delta, rows != 0u, T, row);
     } else {
         const uint32_t n = __ldcg(sp.cnt + 2);
         for (uint32_t e = grid_tid(); e < n; e += grid_threads())
-            ref_sp_react(p, sp, sp.union_list[e], slots, occ, conc, itime, s_delta);
+            ref_sp_react(p, sp, sp.union_list[e], slots, occ, conc, itime, s_delta, rows != 0u, T, row);
     }
     __syncthreads();
     ref_flush_block(p, s_delta, stat, diag);
@@ -926,7 +1044,11 @@ static void ref_enqueue_frame(DeviceRef* d, uint32_t k) {
     const RefParams& p = d->p;
     const RefSparse sp = ref_sparse(d);
     const int TB = 256;
-    const size_t smem = (p.S1 + 2) * sizeof(int32_t);
+    // the reaction pass stages the tables and one concentration row per thread in shared memory when
+    // they fit in the default 48 KB
+    const size_t smem_rows = ((size_t)p.S1 + 2 + 4 * ((size_t)p.R + 1) + ((size_t)p.R + 1) * p.S1 + (size_t)TB * p.S1) * 4;
+    const uint32_t rows = smem_rows <= 48u * 1024u ? 1u : 0u;
+    const size_t smem = rows ? smem_rows : (p.S1 + 2) * sizeof(int32_t);
     ref_sp_list_act<<<d->grid, TB, 0, d->stream>>>(sp);
     ref_sp_directions<<<d->grid, TB, 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->itimes.p, k, d->diag.p, d->flag.p);
     ref_sp_list_touch<<<d->grid, TB, 0, d->stream>>>(sp);
@@ -934,7 +1056,7 @@ static void ref_enqueue_frame(DeviceRef* d, uint32_t k) {
     ref_sp_serial<<<1, 1024, 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->conc.p, d->diag.p, d->flag.p);
     const uint32_t dense = (d->dense_next || d->dense_always) ? 1u : 0u;
     ref_sp_cme<<<d->grid, TB, smem, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->conc.p, d->itimes.p, k, dense, d->stat.p,
-                                                 d->diag.p, d->flag.p);
+                                                 d->diag.p, d->flag.p, rows);
     CS_LAUNCH_CHECK();
     d->dense_next = false;
     d->par ^= 1u;
