@@ -137,6 +137,35 @@ __device__ int ref_decide(const RefParams& p, uint64_t v, uint32_t x, uint32_t y
     }
 }
 
+// ref_decide with the voxel's region codes loaded once for all its particles (rn: own, x-1, x+1,
+// y-1, y+1, z-1, z+1; entries past the lattice edge are not read) and the probability table at Pt
+// (shared memory when it fits): the same sums and the same draw.
+__device__ __forceinline__ int ref_decide_rn(const RefParams& p, const float* Pt, const uint32_t (&rn)[7], uint32_t x,
+                                             uint32_t y, uint32_t z, uint32_t q, uint32_t i_part, uint32_t itime) {
+    const size_t row = (size_t)rn[0] * p.NR;
+    auto prob = [&](uint32_t b) -> float { return Pt[(row + b) * p.S1 + q]; };
+    float pv[6];
+    pv[0] = (x > 0u) ? prob(rn[1]) : 0.0f;
+    pv[1] = (x < p.X - 1u) ? __fadd_rn(pv[0], prob(rn[2])) : pv[0];
+    pv[2] = (y > 0u) ? __fadd_rn(pv[1], prob(rn[3])) : pv[1];
+    pv[3] = (y < p.Y - 1u) ? __fadd_rn(pv[2], prob(rn[4])) : pv[2];
+    pv[4] = (z > 0u) ? __fadd_rn(pv[3], prob(rn[5])) : pv[3];
+    pv[5] = (z < p.Z - 1u) ? __fadd_rn(pv[4], prob(rn[6])) : pv[4];
+    uint32_t xmody = (y == 0u) ? 0u : (x % y);  // WGSL: e1 % 0 == 0
+    float r = d_uniform_float(d_pcg(itime + xmody + z + i_part));
+    int d = 0;
+    while (d < 6 && r > pv[d]) d++;
+    switch (d) {
+        case 0: return (x == 0u) ? 6 : 0;
+        case 1: return (x == p.X - 1u) ? 6 : 1;
+        case 2: return (y == 0u) ? 6 : 2;
+        case 3: return (y == p.Y - 1u) ? 6 : 3;
+        case 4: return (z == 0u) ? 6 : 4;
+        case 5: return (z == p.Z - 1u) ? 6 : 5;
+        default: return 6;
+    }
+}
+
 __global__ void ref_directions(RefParams p, const uint8_t* __restrict__ src, const uint32_t* __restrict__ occS,
                                const uint32_t* __restrict__ itimes, uint32_t step, uint8_t* __restrict__ dirs,
                                uint32_t* diag, uint32_t* contended) {
@@ -523,13 +552,21 @@ __global__ void __launch_bounds__(256) ref_sp_list_touch(RefSparse sp) {
 __global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse sp, const uint8_t* __restrict__ slots,
                                                          const uint32_t* __restrict__ occ,
                                                          const uint32_t* __restrict__ itimes, uint32_t step,
-                                                         uint32_t* diag, uint32_t* contended) {
+                                                         uint32_t* diag, uint32_t* contended, uint32_t stage_P) {
     const uint32_t itime = __ldg(itimes + step);
     const uint32_t K = p.K;
     const uint32_t n = __ldcg(sp.cnt + 0);
     if (grid_tid() == 0) {
         sp.cnt[1] = 0u;
         sp.cnt[2] = 0u;
+    }
+    // the probability table in shared memory when the launch gave room for it
+    extern __shared__ float s_P[];
+    const float* Pt = p.P;
+    if (stage_P) {
+        for (uint32_t i = threadIdx.x; i < p.NR * p.NR * p.S1; i += blockDim.x) s_P[i] = p.P[i];
+        __syncthreads();
+        Pt = s_P;
     }
     for (uint32_t i = grid_tid(); i < sp.W; i += grid_threads()) act_next(sp)[i] = 0u;
     const uint32_t XY = p.X * p.Y;
@@ -550,12 +587,20 @@ __global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse 
         const RefSlots sl = rs_load(slots + (size_t)v * K, K);
         uint32_t x, y, z;
         ref_coords(p, v, x, y, z);
+        const uint8_t* reg = p.regions;
+        uint32_t rn[7] = {reg[v], 0u, 0u, 0u, 0u, 0u, 0u};
+        if (x > 0u) rn[1] = reg[v - p.YZ];
+        if (x < p.X - 1u) rn[2] = reg[v + p.YZ];
+        if (y > 0u) rn[3] = reg[v - p.Z];
+        if (y < p.Y - 1u) rn[4] = reg[v + p.Z];
+        if (z > 0u) rn[5] = reg[v - 1];
+        if (z < p.Z - 1u) rn[6] = reg[v + 1];
         bool has_dep = false;
         RefSlots dr{0x0707070707070707ull, 0x0707070707070707ull};  // 7: stays
         for (uint32_t s = 0; s < K; s++) {
             const uint32_t q = rs_get(sl, s);
             if (s < o && q != 0u) {
-                const int d = ref_decide(p, v, x, y, z, q, v * K + s, itime);
+                const int d = ref_decide_rn(p, Pt, rn, x, y, z, q, v * K + s, itime);
                 rs_set(dr, s, (uint32_t)d);
                 has_dep |= d < 6;
             }
@@ -1050,7 +1095,10 @@ static void ref_enqueue_frame(DeviceRef* d, uint32_t k) {
     const uint32_t rows = smem_rows <= 48u * 1024u ? 1u : 0u;
     const size_t smem = rows ? smem_rows : (p.S1 + 2) * sizeof(int32_t);
     ref_sp_list_act<<<d->grid, TB, 0, d->stream>>>(sp);
-    ref_sp_directions<<<d->grid, TB, 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->itimes.p, k, d->diag.p, d->flag.p);
+    const size_t smem_P = (size_t)p.NR * p.NR * p.S1 * sizeof(float);
+    const uint32_t stage_P = smem_P <= 16u * 1024u ? 1u : 0u;
+    ref_sp_directions<<<d->grid, TB, stage_P ? smem_P : 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->itimes.p, k,
+                                                                     d->diag.p, d->flag.p, stage_P);
     ref_sp_list_touch<<<d->grid, TB, 0, d->stream>>>(sp);
     ref_sp_gather<<<d->grid, TB, 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->conc.p, d->flag.p);
     ref_sp_serial<<<1, 1024, 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->conc.p, d->diag.p, d->flag.p);
