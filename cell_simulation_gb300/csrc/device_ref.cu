@@ -527,7 +527,16 @@ __device__ __forceinline__ void warp_compact(uint32_t m, uint32_t i, uint32_t* l
 }
 
 // The act list of act bitmap c.
+// Programmatic dependent launch between the passes of a frame: a pass lets the next one launch at
+// once and waits for the previous one to complete (and its memory to be visible) before it touches
+// anything; without a programmatic dependency the wait returns at once.
+__device__ __forceinline__ void ref_pdl_start() {
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+
 __global__ void __launch_bounds__(256) ref_sp_list_act(RefSparse sp) {
+    ref_pdl_start();
     for (uint32_t i0 = grid_tid() & ~31u; i0 < sp.W; i0 += grid_threads()) {
         const uint32_t i = i0 + (threadIdx.x & 31u);
         warp_compact(i < sp.W ? act_cur(sp)[i] : 0u, i, sp.act_list, sp.cnt + 0);
@@ -536,6 +545,7 @@ __global__ void __launch_bounds__(256) ref_sp_list_act(RefSparse sp) {
 
 // The touch list, and the union list of act bitmap c and the touch bitmap.
 __global__ void __launch_bounds__(256) ref_sp_list_touch(RefSparse sp) {
+    ref_pdl_start();
     for (uint32_t i0 = grid_tid() & ~31u; i0 < sp.W; i0 += grid_threads()) {
         const uint32_t i = i0 + (threadIdx.x & 31u);
         const uint32_t t = i < sp.W ? __ldcg(sp.touch_bm + i) : 0u;
@@ -553,6 +563,7 @@ __global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse 
                                                          const uint32_t* __restrict__ occ,
                                                          const uint32_t* __restrict__ itimes, uint32_t step,
                                                          uint32_t* diag, uint32_t* contended, uint32_t stage_P) {
+    ref_pdl_start();
     const uint32_t itime = __ldg(itimes + step);
     const uint32_t K = p.K;
     const uint32_t n = __ldcg(sp.cnt + 0);
@@ -630,6 +641,7 @@ __global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse 
 __global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, uint8_t* __restrict__ slots,
                                                      uint32_t* __restrict__ occ, int32_t* __restrict__ conc,
                                                      const uint32_t* __restrict__ contended) {
+    ref_pdl_start();
     if (*contended) return;
     const uint32_t K = p.K, S1 = p.S1;
     const uint32_t n = __ldcg(sp.cnt + 1);
@@ -689,6 +701,7 @@ __global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, 
 // first thread makes the moves.
 __global__ void ref_sp_serial(RefParams p, RefSparse sp, uint8_t* __restrict__ slots, uint32_t* __restrict__ occ,
                               int32_t* __restrict__ conc, uint32_t* diag, const uint32_t* __restrict__ contended) {
+    ref_pdl_start();
     if (*contended == 0u) return;
     __shared__ uint32_t s_words[1024];
     const uint32_t K = p.K, S1 = p.S1;
@@ -854,6 +867,7 @@ __global__ void __launch_bounds__(256) ref_sp_cme(RefParams p, RefSparse sp, uin
                                                   uint32_t* __restrict__ occ, int32_t* __restrict__ conc,
                                                   const uint32_t* __restrict__ itimes, uint32_t step, uint32_t dense,
                                                   int32_t* stat, uint32_t* diag, uint32_t* contended, uint32_t rows) {
+    ref_pdl_start();
     extern __shared__ int32_t s_delta[];  // [S1] + 2 counters, then (rows) the tables and the rows
     for (uint32_t s = threadIdx.x; s < p.S1 + 2; s += blockDim.x) s_delta[s] = 0;
     if (grid_tid() == 0) {
@@ -1085,6 +1099,22 @@ void ref_get_lattice(DeviceRef* d, uint32_t* slots, uint32_t* occ, int32_t* conc
 }
 
 // Enqueues the sparse passes of one frame reading itimes[k].
+// A launch with programmatic stream serialization (see ref_pdl_start).
+template <typename... KArgs, typename... Args>
+static void ref_launch(void (*kernel)(KArgs...), int grid, int block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    CS_CUDA(cudaLaunchKernelEx(&cfg, kernel, args...));
+}
+
 static void ref_enqueue_frame(DeviceRef* d, uint32_t k) {
     const RefParams& p = d->p;
     const RefSparse sp = ref_sparse(d);
@@ -1094,17 +1124,17 @@ static void ref_enqueue_frame(DeviceRef* d, uint32_t k) {
     const size_t smem_rows = ((size_t)p.S1 + 2 + 4 * ((size_t)p.R + 1) + ((size_t)p.R + 1) * p.S1 + (size_t)TB * p.S1) * 4;
     const uint32_t rows = smem_rows <= 48u * 1024u ? 1u : 0u;
     const size_t smem = rows ? smem_rows : (p.S1 + 2) * sizeof(int32_t);
-    ref_sp_list_act<<<d->grid, TB, 0, d->stream>>>(sp);
+    ref_launch(ref_sp_list_act, d->grid, TB, 0, d->stream, sp);
     const size_t smem_P = (size_t)p.NR * p.NR * p.S1 * sizeof(float);
     const uint32_t stage_P = smem_P <= 16u * 1024u ? 1u : 0u;
-    ref_sp_directions<<<d->grid, TB, stage_P ? smem_P : 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->itimes.p, k,
-                                                                     d->diag.p, d->flag.p, stage_P);
-    ref_sp_list_touch<<<d->grid, TB, 0, d->stream>>>(sp);
-    ref_sp_gather<<<d->grid, TB, 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->conc.p, d->flag.p);
-    ref_sp_serial<<<1, 1024, 0, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->conc.p, d->diag.p, d->flag.p);
+    ref_launch(ref_sp_directions, d->grid, TB, stage_P ? smem_P : 0, d->stream, p, sp, (const uint8_t*)d->slots.p,
+               (const uint32_t*)d->occ.p, (const uint32_t*)d->itimes.p, k, d->diag.p, d->flag.p, stage_P);
+    ref_launch(ref_sp_list_touch, d->grid, TB, 0, d->stream, sp);
+    ref_launch(ref_sp_gather, d->grid, TB, 0, d->stream, p, sp, d->slots.p, d->occ.p, d->conc.p, d->flag.p);
+    ref_launch(ref_sp_serial, 1, 1024, 0, d->stream, p, sp, d->slots.p, d->occ.p, d->conc.p, d->diag.p, d->flag.p);
     const uint32_t dense = (d->dense_next || d->dense_always) ? 1u : 0u;
-    ref_sp_cme<<<d->grid, TB, smem, d->stream>>>(p, sp, d->slots.p, d->occ.p, d->conc.p, d->itimes.p, k, dense, d->stat.p,
-                                                 d->diag.p, d->flag.p, rows);
+    ref_launch(ref_sp_cme, d->grid, TB, smem, d->stream, p, sp, d->slots.p, d->occ.p, d->conc.p,
+               (const uint32_t*)d->itimes.p, k, dense, d->stat.p, d->diag.p, d->flag.p, rows);
     CS_LAUNCH_CHECK();
     d->dense_next = false;
     d->par ^= 1u;
