@@ -6,7 +6,9 @@ propensities with FP64 clock), the autotuned step variant (the sweep stream:
 two or three launches per frame, or one persistent launch per call).  `value`
 is voxel-steps/s over the whole job with the lattice resident in HBM; the
 lattice (2 x 256 MiB) is larger
-than L2, so no flush is needed between timed frames.  Also reported: the
+than L2, so no flush is needed between timed frames.  Five more timed calls
+of the same length follow (`repeats`: their median and spread; the headline
+is the first call alone).  Also reported: the
 batched 512-replicate ensemble vs the plain one-launch-group-per-replicate
 path (replicate-steps/s), the reference-RNG CUDA path on the same lattice,
 an end-to-end number through the C ABI, the frame's roofline (algorithmic
@@ -37,6 +39,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "voxel-steps/s and replicate-steps/s, batched vs plain, 1 GB300, KS-matched"
 UNIT = "voxel-steps/s"
+N_REPEATS = 5  # timed calls after the headline one, for the median and spread
 
 
 def env_rank():
@@ -428,6 +431,13 @@ def main():
     t_region = time.perf_counter()
     ms = sim.step_philox_timed(args.steps, seed)
     dist.barrier()
+    # five more timed calls of the same length, continuing from the lattice the timed call left:
+    # their median and spread beside the single timed call the headline is taken from
+    rep_ms = []
+    for _ in range(N_REPEATS):
+        r = sim.step_philox_timed(args.steps, seed)
+        dist.barrier()
+        rep_ms.append(dist.max(r) / args.steps)
     # keep the GPU busy (untimed frames) until the clock window holds three samples
     t_hold = time.perf_counter()
     while clocks.alive() and clocks.rows_since(t_region) < 3 and time.perf_counter() - t_hold < 5.0:
@@ -453,7 +463,12 @@ def main():
     # up, 4 bytes; the seed is uploaded only when it changes) and one blocking
     # read of the species counts (down), like the reference's per-frame itime
     # write, submit and stats readback
-    n_e2e = min(args.steps, 500)
+    n_e2e = 500  # step calls timed, whatever --steps is: a call lasts about 0.17 ms
+    # untimed warm-up calls of the same loop: one-frame calls of either parity run their own
+    # captured graph, made on its first use
+    for _ in range(args.warmup):
+        sim.step_philox(1, seed)
+        sim.counts()
     t0 = time.perf_counter()
     for _ in range(n_e2e):
         sim.step_philox(1, seed)
@@ -500,6 +515,11 @@ def main():
         "e2e": e2e,
         "gpu_launches": launches_in_call(variant, args.steps),
         "clocks": clk,
+        "repeats": {"calls": N_REPEATS, "frames_per_call": args.steps, "ms_per_step": rep_ms,
+                    "median_ms_per_step": statistics.median(rep_ms),
+                    "median_value": world * V / (statistics.median(rep_ms) / 1e3),
+                    "note": "further timed calls after the one the headline is taken from, each continuing "
+                            "from the lattice the previous call left"},
         "diagnostics": {"events": int(diag[0]), "rejected_capacity": int(diag[1]), "event_cap": int(diag[2]),
                         "fp64_selections": int(diag[3]), "ssa_voxels": int(diag[6]), "wait_timeouts": int(diag[7])},
     }
