@@ -59,32 +59,30 @@ size_t stream_smem(int NT, uint32_t S1, uint32_t thr_words, int recs) {
 // by this launch (the fused Y and Z sweeps), read coherently through L2.
 template <int K, bool NC = true>
 __device__ __forceinline__ void rec_load(const uint4* rec, uint32_t i, Vox<K>& c, uint4& t) {
-    uint4 a;
-    if constexpr (NC) {
-        a = __ldg(rec + 2 * (size_t)i);
-        t = __ldg(rec + 2 * (size_t)i + 1);
-    } else {
-        a = __ldcg(rec + 2 * (size_t)i);
-        t = __ldcg(rec + 2 * (size_t)i + 1);
-    }
-    c.w[0] = (uint64_t)a.x | ((uint64_t)a.y << 32);
-    if constexpr (K == 16) c.w[1] = (uint64_t)a.z | ((uint64_t)a.w << 32);
+    // one 32-byte access per record (record buffers come from cudaMalloc, records are 32 bytes)
+    const uint4* p = rec + 2 * (size_t)i;
+    uint32_t a0, a1, a2, a3;
+    if constexpr (NC)
+        asm volatile("ld.global.nc.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                     : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3), "=r"(t.x), "=r"(t.y), "=r"(t.z), "=r"(t.w)
+                     : "l"(p));
+    else
+        asm volatile("ld.global.cg.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                     : "=r"(a0), "=r"(a1), "=r"(a2), "=r"(a3), "=r"(t.x), "=r"(t.y), "=r"(t.z), "=r"(t.w)
+                     : "l"(p)
+                     : "memory");
+    c.w[0] = (uint64_t)a0 | ((uint64_t)a1 << 32);
+    if constexpr (K == 16) c.w[1] = (uint64_t)a2 | ((uint64_t)a3 << 32);
 }
 
 template <int K>
 __device__ __forceinline__ void rec_store(uint4* rec, uint32_t i, const Vox<K>& c, const uint4& t) {
-    uint4 a;
-    a.x = (uint32_t)c.w[0];
-    a.y = (uint32_t)(c.w[0] >> 32);
-    if constexpr (K == 16) {
-        a.z = (uint32_t)c.w[1];
-        a.w = (uint32_t)(c.w[1] >> 32);
-    } else {
-        a.z = 0u;
-        a.w = 0u;
-    }
-    rec[2 * (size_t)i] = a;
-    rec[2 * (size_t)i + 1] = t;
+    ulonglong4_32a v;
+    v.x = c.w[0];
+    v.y = K == 16 ? c.w[K / 8 - 1] : 0ull;
+    v.z = (uint64_t)t.x | ((uint64_t)t.y << 32);
+    v.w = (uint64_t)t.z | ((uint64_t)t.w << 32);
+    *reinterpret_cast<ulonglong4_32a*>(rec + 2 * (size_t)i) = v;
 }
 
 __device__ __forceinline__ uint32_t below(uint32_t m, uint32_t bit) { return (uint32_t)__popc(m & (bit - 1u)); }
