@@ -40,6 +40,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "voxel-steps/s and replicate-steps/s, batched vs plain, 1 GB300, KS-matched"
 UNIT = "voxel-steps/s"
 N_REPEATS = 5  # timed calls after the headline one, for the median and spread
+# lattices the main leg can run (--workload): the 256^3 multi-region cell is the headline
+WORKLOADS = {"c1": "c1_plain_2d", "c2": "c2_single_cell", "c3": "c3_multi_region", "c5": "c5_stiff"}
 
 
 def env_rank():
@@ -210,12 +212,13 @@ def cpu_reference_rate(workload, nx: int, budget_s: float, threads: int, max_fra
 
 
 CPU_SLAB = 8  # planes of the 256^3 cell in the CPU samples (cpu_baseline and the reference arm)
+CPU_SLABS = {"c1": 64, "c2": 16, "c3": CPU_SLAB, "c5": 8}  # the same, per workload (c1: the whole lattice)
 
 
 def reference_arm(args, rank, world):
     """The reference's algorithm on the host cores: the oracle's restatement of the WGSL shaders
-    (the reference itself needs Vulkan and a Rust toolchain), on the same central slab of the 256^3
-    cell as cpu_baseline.  The slab is cut from the lattice the product library's host model
+    (the reference itself needs Vulkan and a Rust toolchain), on the same central slab of the
+    workload's lattice as cpu_baseline (the 256^3 cell by default).  The slab is cut from the lattice the product library's host model
     builder makes (outside the timed region); the timed loop runs the oracle alone."""
     if rank != 0:
         return
@@ -224,7 +227,9 @@ def reference_arm(args, rank, world):
     from cell_simulation_gb300 import configs
 
     oracle.build()
-    a, state, V, desc = central_slab(configs.c3_multi_region(), CPU_SLAB)
+    w = getattr(configs, WORKLOADS[args.workload])()
+    nx = CPU_SLABS[args.workload]
+    a, state, V, desc = central_slab(w, nx)
     n_total = args.warmup + args.steps
     it = (np.arange(n_total, dtype=np.uint64) * 7919 + 12345).astype(np.uint32)
     oracle.ref_run(*a, state, it[:args.warmup], mode=1, threads=threads)
@@ -236,7 +241,7 @@ def reference_arm(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": f"c3_multi_region_256x256x256_K16 ({CPU_SLAB}-plane central x-slab)",
+            "config": {"workload": f"{w.name} ({nx}-plane central x-slab)",
                        "rng": "reference PCG", "threads": threads},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -249,6 +254,9 @@ def describe_variant(i):
     kind, bx = tiling_kinds()[i]
     if kind == 1:
         return {"index": i, "kind": "brick", "slots": k, "brick": [bx, ty, tz], "threads": nt}
+    if kind == 3:  # one block per replicate, every frame of a step call in one launch
+        return {"index": i, "kind": "resident", "slots": k, "threads": nt, "multi_frame": True,
+                "launches_per_call": 1}
     if kind == 2:
         if ty == 1:  # the persistent form: every frame of a step call in one launch
             return {"index": i, "kind": "stream", "slots": k, "words_per_group": 32, "threads": nt,
@@ -283,6 +291,8 @@ def frame_kernels(desc):
         if desc["passes_per_frame"] == 2:
             return ["sweep_pass_kernel<1>", "sweep_pass_kernel<5>"]
         return ["sweep_pass_kernel<1>", "sweep_pass_kernel<2>", "sweep_pass_kernel<3>"]
+    if desc["kind"] == "resident":
+        return ["resident_frames_kernel"]
     return ["brick_step_kernel"] if desc["kind"] == "brick" else ["prod_step_kernel"]
 
 
@@ -384,6 +394,8 @@ def main():
                                                              "reference-RNG, e2e and CPU legs")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--variant", type=int, default=-1, help="step variant index (default: autotuned)")
+    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS),
+                    help="the lattice of the main leg (default: the 256^3 multi-region cell)")
     ap.add_argument("--ensemble-only", action="store_true",
                     help="only the 512-replicate ensemble leg: --steps batched frames, a tenth as many plain ones "
                          "(for profiling; prints that leg's numbers)")
@@ -410,7 +422,7 @@ def main():
     device = local
     seed = 0xC0FFEE + rank
     t_setup = time.perf_counter()
-    w = configs.c3_multi_region()
+    w = getattr(configs, WORKLOADS[args.workload])()
     sim = w.sim
     info = sim.info()
     V, K, S1 = int(info.n_voxels), info.max_particles_site, info.n_species + 1
@@ -468,6 +480,9 @@ def main():
     ms_max = dist.max(ms)
     value = world * V * args.steps / (ms_max / 1e3)
     frame_s = ms / 1e3 / args.steps
+    lat_mib = V * K / 2**20
+    l2_note = (f"inputs larger than L2 (2 x {lat_mib:.0f} MiB lattice buffers)" if 2 * V * K > 129e6 else
+               f"inputs smaller than L2 (2 x {lat_mib * 1024:.0f} KiB lattice buffers), not flushed")
     peak, peak_kind = measured_peaks()
     alg_bytes = V * (2 * K + 1)
     achieved = alg_bytes / frame_s / 1e9
@@ -490,7 +505,8 @@ def main():
         extras["configs"] = config_legs(device, min(args.cpu_budget, 4.0), threads, world == 1)
     cpu = None
     if not args.no_extras and rank == 0 and world == 1:
-        rate, sample = cpu_reference_rate(configs.c3_multi_region(), CPU_SLAB, args.cpu_budget, threads)
+        rate, sample = cpu_reference_rate(getattr(configs, WORKLOADS[args.workload])(), CPU_SLABS[args.workload],
+                                          args.cpu_budget, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
     dist.close()
     if rank != 0:
@@ -501,7 +517,7 @@ def main():
         "dtype": "u8", "data": "synthetic",
         "config": {"workload": w.name, "voxels": V, "slots_per_voxel": K, "species": S1 - 1,
                    "reactions": int(info.n_reactions), "rng": "philox4x32-10", "precision": "fp32 propensities, fp64 clock",
-                   "l2": "inputs larger than L2 (2 x 256 MiB lattice buffers)", "parallelism": f"replicas x{world}",
+                   "l2": l2_note, "parallelism": f"replicas x{world}",
                    "variant": desc},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,

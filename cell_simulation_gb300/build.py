@@ -17,7 +17,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libcellsim.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["model.cpp", "abi.cpp", "device_ref.cu", "device_prod.cu", "device_stream.cu"]
+SOURCES = ["model.cpp", "abi.cpp", "device_ref.cu", "device_prod.cu", "device_stream.cu", "device_resident.cu"]
 
 
 def _nvcc() -> str:

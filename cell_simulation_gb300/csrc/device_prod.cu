@@ -36,6 +36,7 @@
 #include "brick_kernel.cuh"
 #include "prod_common.cuh"
 #include "prod_kernel.cuh"
+#include "resident_kernel.cuh"
 #include "stream_kernel.cuh"
 #include "views.cuh"
 
@@ -52,7 +53,7 @@ typedef void (*ProdKernelFn)(ProdParams);
 // its own BX planes.  kind 2: the sweep stream, four barrier-free passes over
 // bitmap word groups (stream_kernel.cuh); `variant` indexes its compiled
 // launch shapes.
-enum { KIND_TILE = 0, KIND_BRICK = 1, KIND_STREAM = 2 };
+enum { KIND_TILE = 0, KIND_BRICK = 1, KIND_STREAM = 2, KIND_RESIDENT = 3 };
 
 struct KernelCfg {
     int kind, K, TY, TZ, NT, BX;
@@ -67,6 +68,11 @@ struct KernelCfg {
 static KernelCfg stream_cfg(int K, int variant) {
     return KernelCfg{KIND_STREAM, K, stream_variant_frames(variant) ? 1 : 0, 32, stream_variant_threads(variant), 0,
                      nullptr, nullptr, -1, 0, variant};
+}
+
+// the resident form: one block per replicate, every frame of a step call in one launch
+static KernelCfg resident_cfg(int K) {
+    return KernelCfg{KIND_RESIDENT, K, 0, 0, RESIDENT_THREADS, 0, nullptr, nullptr, -1, 0, 0};
 }
 
 template <int K, int TY, int TZ>
@@ -123,6 +129,8 @@ static const std::vector<KernelCfg>& all_cfgs() {
         // every frame as tasks of one counter) at three blocks per SM, a pass's groups taken
         // heaviest first / in plane order
         stream_cfg(16, 6), stream_cfg(8, 6), stream_cfg(16, 7), stream_cfg(8, 7),
+        // lattices that fit in one block's shared memory: the resident form
+        resident_cfg(16), resident_cfg(8),
     };
     return v;
 }
@@ -503,6 +511,7 @@ static bool fused_fits(const DeviceProd* d) {
 
 static void build_items(DeviceProd* d) {
     const KernelCfg& cfg = all_cfgs()[d->cfg_index];
+    if (cfg.kind == KIND_RESIDENT) return;  // no work lists: one block per replicate
     if (cfg.kind == KIND_STREAM) {
         build_groups(d);
         return;
@@ -714,12 +723,31 @@ static uint32_t thr_words(const DeviceProd* d) {
     return n <= kThrSmemWords ? n : 0u;
 }
 
+static uint64_t max_rep_voxels(const DeviceProd* d) {
+    uint64_t m = 0;
+    for (const RepDesc& r : d->h_reps) m = std::max<uint64_t>(m, (uint64_t)r.X * r.Y * r.Z);
+    return m;
+}
+
+// The resident form needs every replicate in one block's shared memory.
+static bool resident_fits(const DeviceProd* d) {
+    int optin = 0;
+    CS_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, d->device));
+    const uint64_t v = max_rep_voxels(d);
+    return v <= 0xFFFFull && resident_smem((int)d->K, v, thr_words(d)) <= (size_t)optin;  // 16-bit voxel lists
+}
+
 static size_t cfg_smem(const DeviceProd* d, const KernelCfg& cfg) {
+    if (cfg.kind == KIND_RESIDENT) return resident_smem(cfg.K, max_rep_voxels(d), thr_words(d));
     if (cfg.kind == KIND_STREAM) return stream_pass_smem(cfg.variant, 2, d->S1, thr_words(d));  // the largest pass
     return cfg.smem(d->S1, thr_words(d));
 }
 
 static void set_attrs(const DeviceProd* d, const KernelCfg& cfg) {
+    if (cfg.kind == KIND_RESIDENT) {
+        resident_set_attrs(d->device);
+        return;
+    }
     if (cfg.kind == KIND_STREAM) {
         stream_set_attrs(cfg.K, cfg.variant, d->S1, thr_words(d));
         return;
@@ -745,6 +773,8 @@ static void set_cfg(DeviceProd* d, int idx) {
     const KernelCfg& cfg = all_cfgs()[idx];
     if (cfg.kind == KIND_STREAM && stream_variant_fused(cfg.variant) && !fused_fits(d))
         throw Error(CS_ERR_INVALID_ARG, "fused sweep-stream variant needs rows of at most 32 bitmap words (Z <= 1024)");
+    if (cfg.kind == KIND_RESIDENT && !resident_fits(d))
+        throw Error(CS_ERR_INVALID_ARG, "resident variant needs every lattice in one block's shared memory");
     set_attrs(d, cfg);
     if (cfg.spill >= 0) set_attrs(d, all_cfgs()[cfg.spill]);
     // build_items reads cfg_index; when it refuses the new configuration (a lattice too large for
@@ -1235,10 +1265,44 @@ static void run_frames(DeviceProd* d, uint32_t n, uint64_t frame0, bool batched)
     run_frames_nosync(d, n, batched);
 }
 
+// Every frame of a call in one launch of the resident form: one block per replicate (batched) or
+// one launch per replicate; the last frame's lattice lands in the buffer of parity cur ^ (n & 1).
+static void launch_resident(DeviceProd* d, uint32_t n, bool batched) {
+    ResidentParams RP{};
+    fill_params(d, RP.P, d->cur, -1);
+    const int out = d->cur ^ (int)(n & 1u);
+    RP.P.dst = d->slots[out].p;
+    RP.P.reset = d->counters.p;
+    RP.P.n_reset = (uint32_t)d->counters.n;
+    RP.frame0 = (uint32_t)d->next_frame;
+    RP.n_frames = n;
+    RP.stepbuf_out = (uint32_t)out;
+    RP.vmax = (uint32_t)max_rep_voxels(d);
+    RP.thr_words = thr_words(d);
+    const size_t smem = resident_smem((int)d->K, RP.vmax, RP.thr_words);
+    if (batched) {
+        RP.rep0 = 0;
+        resident_launch((int)d->K, RP, (int)d->n_rep, smem, d->stream);
+    } else {
+        for (uint32_t r = 0; r < d->n_rep; r++) {
+            RP.rep0 = r;
+            resident_launch((int)d->K, RP, 1, smem, d->stream);
+        }
+    }
+}
+
 // Enqueues n frames; the frame number must already be in stepbuf[cur] (and
 // its host copy in next_frame).
 static void run_frames_nosync(DeviceProd* d, uint32_t n, bool batched) {
     if (n == 0) return;
+    if (all_cfgs()[d->cfg_index].kind == KIND_RESIDENT) {
+        launch_resident(d, n, batched);
+        d->cur ^= (int)(n & 1u);
+        d->next_frame += n;
+        d->occ_valid = false;  // the resident form keeps no occupancy bitmaps and no x-decisions
+        d->xdec_valid = false;
+        return;
+    }
     // the brick pass and the sweep stream read and maintain the occupancy bitmaps
     const int kind = all_cfgs()[d->cfg_index].kind;
     const bool brick = kind != KIND_TILE;
@@ -1563,6 +1627,7 @@ void prod_tiling_kind(int i, int* kind, int* BX) {
 int prod_tiling_launches(int i) {
     const auto& c = all_cfgs();
     if (i < 0 || i >= (int)c.size()) throw Error(CS_ERR_INVALID_ARG, "tile configuration index out of range");
+    if (c[i].kind == KIND_RESIDENT) return 1;  // one launch per step call
     if (c[i].kind == KIND_STREAM) {
         if (stream_variant_frames(c[i].variant)) return 1;  // one launch per step call
         return stream_variant_fused(c[i].variant) ? 2 : 3;
@@ -1667,6 +1732,7 @@ int prod_autotune(DeviceProd* d, uint32_t frames, uint64_t frame0, bool batched,
     for (int i = 0; i < (int)c.size(); i++) {
         if (c[i].K != (int)d->K) continue;
         if (c[i].kind == KIND_STREAM && stream_variant_fused(c[i].variant) && !fused_fits(d)) continue;
+        if (c[i].kind == KIND_RESIDENT && !resident_fits(d)) continue;
         d->seg_len = 0;
         set_cfg(d, i);
         prod_time_frames(d, 2, frame0, batched);  // warm-up: graph, bitmaps, caches

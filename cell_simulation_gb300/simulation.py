@@ -385,7 +385,9 @@ def tiling_variants() -> list[tuple[int, int, int, int]]:
 def tiling_kinds() -> list[tuple[int, int]]:
     """(kind, brick_planes) of every compiled variant: kind 0 = tile pipeline,
     kind 1 = sparse brick pass (crowded bricks finished by a full-capacity brick
-    pass), kind 2 = sweep stream (the default; brick_planes 0)."""
+    pass), kind 2 = sweep stream (the default; brick_planes 0), kind 3 = resident
+    form (one block per replicate, its lattice in shared memory for every frame
+    of a step call; small lattices only)."""
     lib = N.load()
     n = C.c_int32()
     N.check(lib.cs_tiling_count(C.byref(n)))

@@ -291,11 +291,15 @@ cs_status cs_step_philox_timed(cs_sim* sim, uint32_t n_steps, uint64_t seed, flo
  * kind 2 = sweep stream (the default): barrier-free passes over groups of 32
  * occupancy-bitmap words (TZ = 32, brick_planes = 0; TY = 1 marks the
  * persistent form that runs every frame of a step call in one launch, TY = 0
- * the per-pass launches).  Every variant computes the same lattice.
- * cs_tiling_launches: kernel launches per frame once a run is under way (the
- * sweep stream: 3, or 2 where the Y and Z sweeps are one launch, or 1 per step
- * call in the persistent form; the last two need Z <= 1024 and cs_set_tiling
- * refuses them otherwise).  No reference counterpart (the reference has one
+ * the per-pass launches); kind 3 = resident form: one block of `threads`
+ * per replicate holds its lattice in shared memory for every frame of a step
+ * call (TY = TZ = 0; about 5,300 voxels per replicate at K = 16 and 9,000 at
+ * K = 8 at most: cs_set_tiling refuses larger lattices).  Every variant
+ * computes the same lattice.  cs_tiling_launches: kernel launches per frame
+ * once a run is under way (the sweep stream: 3, or 2 where the Y and Z sweeps
+ * are one launch, or 1 per step call in the persistent form; the last two need
+ * Z <= 1024 and cs_set_tiling refuses them otherwise; the resident form: 1
+ * per step call).  No reference counterpart (the reference has one
  * fixed dispatch shape per shader). */
 cs_status cs_tiling_count(int32_t* n);
 cs_status cs_tiling_describe(int32_t index, int32_t* K, int32_t* TY, int32_t* TZ, int32_t* threads);

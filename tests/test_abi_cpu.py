@@ -35,7 +35,7 @@ def test_variant_tables(lib):
     """The compiled step variants as the autotuner and bench.py see them (no device call): every
     slot count has three-launch sweep streams, fused ones (two launches per frame) and persistent
     ones (one launch per step call); bricks with bounded pools take two launches, the tile
-    pipeline one."""
+    pipeline one, the resident form one per step call."""
     from cell_simulation_gb300 import tiling_kinds, tiling_launches, tiling_variants
 
     v, k, n = tiling_variants(), tiling_kinds(), tiling_launches()
@@ -47,6 +47,9 @@ def test_variant_tables(lib):
         assert all((v[i][1] == 1) == (n[i] == 1) for i in range(len(v)) if v[i][0] == K and k[i][0] == 2)
     assert all(n[i] == 1 for i in range(len(v)) if k[i][0] == 0)
     assert all(n[i] in (1, 2) for i in range(len(v)) if k[i][0] == 1)
+    # the resident form: one launch per step call, for both slot counts
+    assert sorted(v[i][0] for i in range(len(v)) if k[i][0] == 3) == [8, 16]
+    assert all(n[i] == 1 for i in range(len(v)) if k[i][0] == 3)
     with pytest.raises(CellsimError):
         out = C.c_int32()
         native.check(lib.cs_tiling_launches(len(v), C.byref(out)))

@@ -239,12 +239,13 @@ def test_graph_replay_equals_single_launches(form):
     assert a.diagnostics()[7] == 0
 
 
-@pytest.mark.parametrize("variant", ["default", "unfused", "fused_last", "frames"])
+@pytest.mark.parametrize("variant", ["default", "unfused", "fused_last", "frames", "resident"])
 def test_ensemble_batched_equals_plain_and_oracle(orc, variant):
     """Replicates of different sizes in one launch per pass: batched frames equal per-replicate
     (plain) frames and the oracle, for the default step (fused Y and Z sweeps), the sweep stream
-    with the Y and Z sweeps apart, the fused stream at four blocks per SM and the persistent
-    multi-frame stream (batched: every frame of a step call in one launch)."""
+    with the Y and Z sweeps apart, the fused stream at four blocks per SM, the persistent
+    multi-frame stream (batched: every frame of a step call in one launch) and the resident form
+    (one block per replicate, every frame of a call in one launch)."""
     tmpl = configs.c4_ensemble_template(K=8)
     res = np.array([[9, 9, 9], [12, 12, 12], [7, 7, 7], [16, 16, 16]], np.uint32)
     seeds = np.array([11, 22, 33, 44], np.uint64)
@@ -252,7 +253,11 @@ def test_ensemble_batched_equals_plain_and_oracle(orc, variant):
     init = np.array([0, 40, 40, 5], np.uint32)
     eb = Ensemble(tmpl, res, seeds, mult, init)
     ep = Ensemble(tmpl, res, seeds, mult, init)
-    if variant != "default":
+    if variant == "resident":
+        ti = next(i for i, (t, k) in enumerate(zip(tiling_variants(), tiling_kinds())) if t[0] == 8 and k[0] == 3)
+        eb.set_tiling(ti)
+        ep.set_tiling(ti)
+    elif variant != "default":
         launches = tiling_launches()
         want = {"unfused": 3, "fused_last": 2, "frames": 1}[variant]
         ti = [i for i in stream_tilings(8) if launches[i] == want][-1]

@@ -1,7 +1,7 @@
 """Zero-order reactions (no reactants) fire in every voxel, empty ones included: every kind of
 production step (both forms of the sweep stream, a sparse brick pass whose crowded bricks spill, a
-dense brick pass, a tile pipeline) matches the oracle on such a model, and particles appear in
-voxels that were empty."""
+dense brick pass, a tile pipeline, the resident form) matches the oracle on such a model, and
+particles appear in voxels that were empty."""
 import numpy as np
 import pytest
 
@@ -28,7 +28,8 @@ def _tilings():
             "frames": next(i for i in streams if launches[i] == 1),
             "brick_sparse": next(i for i in k16 if kinds[i][0] == 1 and launches[i] == 2),
             "brick_dense": next(i for i in k16 if kinds[i][0] == 1 and launches[i] == 1),
-            "tile": next(i for i in k16 if kinds[i][0] == 0)}
+            "tile": next(i for i in k16 if kinds[i][0] == 0),
+            "resident": next(i for i in k16 if kinds[i][0] == 3)}
 
 
 def test_zero_order_reactions_match_oracle(orc):
