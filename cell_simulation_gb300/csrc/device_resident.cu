@@ -14,16 +14,15 @@ constexpr int NSSA = RESIDENT_SSA_WARPS;
 
 // Byte offsets of a block's shared-memory areas, each 16-byte aligned.
 struct ResidentLayout {
-    size_t cnt;   // [16] list lengths and the count of voxels set aside, then PD_N diagnostic counters
-    size_t thr;   // [thr_words] threshold table
-    size_t ws;    // [NSSA][SSA_WARP_SCRATCH] the SSA scratch of the warps that run the SSA
-    size_t mark;  // [vmax / 32] bitmap: the voxel is on the sweep's work list
-    size_t code;  // [vmax] region code (id + 1) of every voxel
-    size_t dec;   // [vmax] move decisions of the current axis (0 but for listed voxels); in the
-                  // reaction step, the voxels set aside
+    size_t cnt;    // [16] list lengths and counts, then PD_N diagnostic counters
+    size_t thr;    // [thr_words] threshold table
+    size_t ws;     // [NSSA][SSA_WARP_SCRATCH] the SSA scratch of the warps that run the SSA
+    size_t mark0, mark1;  // [vmax / 32] bitmaps: the voxel is on the current / the other work list
+    size_t code;   // [vmax] region code (id + 1) of every voxel
+    size_t dec;    // [vmax] move decisions of the current axis, valid for the voxels on the work
+                   // list (a marked voxel); in the reaction step, the voxels set aside
     size_t list0, list1;  // [vmax] 16-bit voxel lists: the occupied voxels, then the sweep's work list
-    size_t lat;   // [vmax] slot contents
-    size_t res;   // [vmax] the sweep's new contents, by work-list position
+    size_t lat0, lat1;    // [vmax] slot contents: the current state and the one two sweeps back
     size_t total;
 };
 
@@ -36,16 +35,18 @@ __host__ __device__ inline size_t take(size_t& o, size_t bytes) {
 __host__ __device__ inline ResidentLayout resident_layout(int K, uint64_t vmax, uint32_t thr_words) {
     ResidentLayout L;
     size_t o = 0;
+    const size_t mark_words = (size_t)((vmax + 31) / 32);
     L.cnt = take(o, sizeof(uint32_t) * (16 + PD_N));
     L.thr = take(o, sizeof(uint32_t) * thr_words);
     L.ws = take(o, sizeof(float) * (size_t)SSA_WARP_SCRATCH * NSSA);
-    L.mark = take(o, sizeof(uint32_t) * (size_t)((vmax + 31) / 32));
+    L.mark0 = take(o, sizeof(uint32_t) * mark_words);
+    L.mark1 = take(o, sizeof(uint32_t) * mark_words);
     L.code = take(o, (size_t)vmax);
     L.dec = take(o, sizeof(uint32_t) * (size_t)vmax);
     L.list0 = take(o, sizeof(uint16_t) * (size_t)vmax);
     L.list1 = take(o, sizeof(uint16_t) * (size_t)vmax);
-    L.lat = take(o, (size_t)K * vmax);
-    L.res = take(o, (size_t)K * vmax);
+    L.lat0 = take(o, (size_t)K * vmax);
+    L.lat1 = take(o, (size_t)K * vmax);
     L.total = o;
     return L;
 }
@@ -60,26 +61,46 @@ __device__ __forceinline__ void warp_append(bool want, uint32_t v, uint16_t* lis
     if (want) list[pos + (uint32_t)__popc(m & ((1u << lane) - 1u))] = (uint16_t)v;
 }
 
+__device__ __forceinline__ bool test_mark(const uint32_t* mark, uint32_t v) { return (mark[v >> 5] >> (v & 31u)) & 1u; }
+__device__ __forceinline__ bool set_mark(uint32_t* mark, uint32_t v) {  // true when v was not marked yet
+    const uint32_t bit = 1u << (v & 31u);
+    return (atomicOr(&mark[v >> 5], bit) & bit) == 0u;
+}
+
+// A sweep is two block-wide steps.  With the lattice state of this sweep in `cur`, the state two
+// sweeps back in `nx`, the occupied voxels in lists[b] (all marked in mark_cur) and the previous
+// sweep's work list in lists[b ^ 1] (marked in mark_nx):
+//   1. clear the previous work list's voxels in nx and mark_nx; move decisions of the occupied
+//      voxels into dec, appending each receiving neighbour not marked yet (dec 0) to lists[b]:
+//      the work list, every voxel once
+//   2. new contents of the work list's voxels into nx (a neighbour's decision counts when the
+//      neighbour is marked: every other voxel is empty), marking and listing in lists[b ^ 1] those
+//      that end up occupied
+// Voxels off the work list are empty before and after the sweep, and nx held nothing else, so nx
+// is then the whole next state; the roles of the buffers swap.
 template <int K>
 __global__ void __launch_bounds__(NT, 1) resident_frames_kernel(const __grid_constant__ ResidentParams RP) {
     extern __shared__ __align__(16) unsigned char sm[];
     const ProdParams& P = RP.P;
     const ResidentLayout L = resident_layout(K, RP.vmax, RP.thr_words);
-    // cnt[0], cnt[1]: lengths of list0 / list1; cnt[2]: the work list's; cnt[3]: voxels set aside
+    // cnt[0], cnt[1]: lengths of list0 / list1; cnt[2 + a]: receiving voxels appended in sweeps of
+    // parity a; cnt[4 + (f & 1)]: voxels set aside in frame f
     uint32_t* const cnt = reinterpret_cast<uint32_t*>(sm + L.cnt);
     uint32_t* const s_diag = cnt + 16;
-    uint32_t* const mark = reinterpret_cast<uint32_t*>(sm + L.mark);
     uint8_t* const code = sm + L.code;
     uint32_t* const dec = reinterpret_cast<uint32_t*>(sm + L.dec);
     uint16_t* const list0 = reinterpret_cast<uint16_t*>(sm + L.list0);
     uint16_t* const list1 = reinterpret_cast<uint16_t*>(sm + L.list1);
     auto lists = [&](uint32_t k) -> uint16_t* { return k ? list1 : list0; };
-    Vox<K>* const lat = reinterpret_cast<Vox<K>*>(sm + L.lat);
-    Vox<K>* const res = reinterpret_cast<Vox<K>*>(sm + L.res);
+    uint32_t* mark_cur = reinterpret_cast<uint32_t*>(sm + L.mark0);
+    uint32_t* mark_nx = reinterpret_cast<uint32_t*>(sm + L.mark1);
+    Vox<K>* cur = reinterpret_cast<Vox<K>*>(sm + L.lat0);
+    Vox<K>* nx = reinterpret_cast<Vox<K>*>(sm + L.lat1);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t S1 = P.T.S1, NC = P.T.NC;
     const RepDesc rd = P.reps[RP.rep0 + blockIdx.x];
     const uint32_t X = rd.X, Y = rd.Y, Z = rd.Z, YZ = Y * Z, V = X * YZ;  // V <= vmax < 2^16
+    const uint32_t mark_words = (V + 31) / 32;
 
     const uint32_t* thr = P.T.thr;
     if (RP.thr_words) {
@@ -88,7 +109,10 @@ __global__ void __launch_bounds__(NT, 1) resident_frames_kernel(const __grid_con
         thr = s_thr;
     }
     for (uint32_t i = tid; i < 16 + PD_N; i += NT) cnt[i] = 0u;
-    for (uint32_t i = tid; i < (V + 31) / 32; i += NT) mark[i] = 0u;
+    for (uint32_t i = tid; i < mark_words; i += NT) {
+        mark_cur[i] = 0u;
+        mark_nx[i] = 0u;
+    }
     // the other forms' work counters start the next frame at zero whatever parity it has
     if (blockIdx.x == 0 && tid == 0)
         for (uint32_t i = 0; i < P.n_reset; i++) P.reset[i] = 0u;
@@ -97,14 +121,16 @@ __global__ void __launch_bounds__(NT, 1) resident_frames_kernel(const __grid_con
     for (uint32_t v = tid; v < V; v += NT) {  // unrolled: several global loads in flight per thread
         const uint32_t x = v / YZ, y = (v / Z) % Y, z = v % Z;
         code[v] = rpad ? rpad[((uint64_t)x * Y + y) * rd.Zr + z + 2u] : (uint8_t)1u;
-        lat[v] = ld_vox_g<K>(P.src + (rd.base + v) * K);
-        dec[v] = 0u;
+        cur[v] = ld_vox_g<K>(P.src + (rd.base + v) * K);
+        nx[v] = vox_zero<K>();
     }
     __syncthreads();
-    // the occupied voxels (loops that call warp_append run whole warps: base is warp-uniform)
+    // the occupied voxels, marked (loops that call warp_append run whole warps: base is warp-uniform)
     for (uint32_t base = warp * 32u; base < V; base += NT) {
         const uint32_t v = base + lane;
-        warp_append(v < V && !vox_empty<K>(lat[v]), v, lists(0), &cnt[0], lane);
+        const bool occupied = v < V && !vox_empty<K>(cur[v]);
+        if (occupied) set_mark(mark_cur, v);
+        warp_append(occupied, v, list0, &cnt[0], lane);
     }
     __syncthreads();
 
@@ -118,12 +144,10 @@ __global__ void __launch_bounds__(NT, 1) resident_frames_kernel(const __grid_con
     const float* const a2 = P.T.a2 ? P.T.a2 + (size_t)ci * S1 * S1 : nullptr;
     unsigned long long* const counts = P.counts + (size_t)ci * S1;
     auto trow = [&](uint32_t a, uint32_t b) -> const uint32_t* { return thr + (a * NC + b) * S1; };
-    auto set_mark = [&](uint32_t v) -> bool {  // true when v was not marked yet
-        const uint32_t bit = 1u << (v & 31u);
-        return (atomicOr(&mark[v >> 5], bit) & bit) == 0u;
-    };
 
-    uint32_t b = 0;  // lists(b) holds the occupied voxels (and possibly voxels emptied since)
+    uint32_t b = 0;        // lists(b) holds the occupied voxels (and possibly voxels emptied since)
+    uint32_t a = 0;        // parity of the sweeps run so far: cnt[2 + a] counts this sweep's appends
+    uint32_t nw_prev = 0;  // length of the previous sweep's work list, lists(b ^ 1)
     for (uint32_t f = 0; f < RP.n_frames; f++) {
         const uint32_t fr = RP.frame0 + f;
         for (uint32_t sweep = 0; sweep < 3u; sweep++) {
@@ -131,20 +155,27 @@ __global__ void __launch_bounds__(NT, 1) resident_frames_kernel(const __grid_con
             const uint32_t dim = sweep == 0u ? X : sweep == 1u ? Y : Z;
             // an axis of length 1 has no neighbour: every decision is 0 and every content stays
             if (dim == 1u) continue;
-            uint16_t* const wl = lists(b);  // the occupied voxels, then the voxels they send to
+            uint16_t* const wl = lists(b);
+            const uint16_t* const wprev = lists(b ^ 1u);
             const uint32_t na = cnt[b];
-            // 1. mark the occupied voxels, so that a receiving voxel joins the work list once
-            for (uint32_t i = tid; i < na; i += NT) set_mark(wl[i]);
+            uint32_t* const n_app = &cnt[2 + a];
+            // 1.
+            for (uint32_t i = tid; i < nw_prev; i += NT) {
+                const uint32_t u = wprev[i];
+                nx[u] = vox_zero<K>();
+                atomicAnd(&mark_nx[u >> 5], ~(1u << (u & 31u)));
+            }
             if (tid == 0) {
-                cnt[2] = na;
+                cnt[2 + (a ^ 1u)] = 0u;
                 cnt[b ^ 1u] = 0u;
             }
-            __syncthreads();
-            // 2. move decisions of the occupied voxels; their receiving neighbours join the list
             for (uint32_t i = tid; i < na; i += NT) {
                 const uint32_t v = wl[i];
-                const Vox<K> c = lat[v];
-                if (vox_empty<K>(c)) continue;
+                const Vox<K> c = cur[v];
+                if (vox_empty<K>(c)) {
+                    dec[v] = 0u;
+                    continue;
+                }
                 const uint32_t coord = (v / stride) % dim;
                 const uint32_t rs = code[v];
                 const uint32_t rlo = coord > 0u ? code[v - stride] : 0u;
@@ -153,88 +184,107 @@ __global__ void __launch_bounds__(NT, 1) resident_frames_kernel(const __grid_con
                 const uint32_t d =
                     decide_moves<K>(c, v, fr, sweep, trow(rs, rlo), trow(rs, rhi), k0, k1, sweep_word(b0, sweep));
                 dec[v] = d;
-                if ((d & 0xFFFFu) && set_mark(v - stride)) wl[atomicAdd(&cnt[2], 1u)] = (uint16_t)(v - stride);
-                if ((d >> 16) && set_mark(v + stride)) wl[atomicAdd(&cnt[2], 1u)] = (uint16_t)(v + stride);
-            }
-            __syncthreads();
-            // 3. new contents of the work list's voxels (every other voxel is empty and stays so)
-            const uint32_t nw = cnt[2];
-            for (uint32_t i = tid; i < nw; i += NT) {
-                const uint32_t v = wl[i];
-                const uint32_t coord = (v / stride) % dim;
-                const bool has_lo = coord > 0u, has_hi = coord + 1u < dim;
-                const uint32_t dme = dec[v], dlo = has_lo ? dec[v - stride] : 0u, dhi = has_hi ? dec[v + stride] : 0u;
-                if ((dme | (dlo >> 16) | (dhi & 0xFFFFu)) == 0u) {  // nothing leaves or arrives
-                    res[i] = lat[v];
-                    continue;
+                // a receiving voxel not marked yet is empty and on no list: nobody else writes its dec
+                if ((d & 0xFFFFu) && set_mark(mark_cur, v - stride)) {
+                    dec[v - stride] = 0u;
+                    wl[na + atomicAdd(n_app, 1u)] = (uint16_t)(v - stride);
                 }
-                const Vox<K> lo = has_lo ? lat[v - stride] : vox_zero<K>();
-                const Vox<K> hi = has_hi ? lat[v + stride] : vox_zero<K>();
-                res[i] = combine<K>(lat[v], dme, lo, dlo, hi, dhi, v, v - stride, v + stride, fr, sweep);
+                if ((d >> 16) && set_mark(mark_cur, v + stride)) {
+                    dec[v + stride] = 0u;
+                    wl[na + atomicAdd(n_app, 1u)] = (uint16_t)(v + stride);
+                }
             }
             __syncthreads();
-            // 4. store them, clear the decisions and marks, and list the voxels now occupied
+            // 2.
+            const uint32_t nw = na + *n_app;
             for (uint32_t base = warp * 32u; base < nw; base += NT) {
                 const uint32_t i = base + lane;
                 bool occupied = false;
                 uint32_t v = 0u;
                 if (i < nw) {
                     v = wl[i];
-                    const Vox<K> r = res[i];
-                    lat[v] = r;
-                    dec[v] = 0u;
-                    atomicAnd(&mark[v >> 5], ~(1u << (v & 31u)));
+                    const uint32_t coord = (v / stride) % dim;
+                    const bool has_lo = coord > 0u, has_hi = coord + 1u < dim;
+                    const uint32_t dme = dec[v];
+                    const uint32_t dlo = has_lo && test_mark(mark_cur, v - stride) ? dec[v - stride] : 0u;
+                    const uint32_t dhi = has_hi && test_mark(mark_cur, v + stride) ? dec[v + stride] : 0u;
+                    Vox<K> r = cur[v];
+                    if ((dme | (dlo >> 16) | (dhi & 0xFFFFu)) != 0u) {  // something leaves or arrives
+                        const Vox<K> lo = has_lo ? cur[v - stride] : vox_zero<K>();
+                        const Vox<K> hi = has_hi ? cur[v + stride] : vox_zero<K>();
+                        r = combine<K>(r, dme, lo, dlo, hi, dhi, v, v - stride, v + stride, fr, sweep);
+                    }
+                    nx[v] = r;
                     occupied = !vox_empty<K>(r);
+                    if (occupied) set_mark(mark_nx, v);
                 }
                 warp_append(occupied, v, lists(b ^ 1u), &cnt[b ^ 1u], lane);
             }
             __syncthreads();
+            Vox<K>* const t = cur;
+            cur = nx;
+            nx = t;
+            uint32_t* const tm = mark_cur;
+            mark_cur = mark_nx;
+            mark_nx = tm;
             b ^= 1u;
+            a ^= 1u;
+            nw_prev = nw;
         }
         // reactions: the voxels whose first event may fall inside the frame are set aside (their
         // indices in dec), then each runs its SSA on one warp
+        uint32_t* const n_pend = &cnt[4 + (f & 1u)];
         const uint32_t na = all_react ? V : cnt[b];
+        if (tid == 0) {
+            cnt[4 + ((f + 1u) & 1u)] = 0u;
+            cnt[b ^ 1u] = 0u;
+        }
         for (uint32_t i = tid; i < na; i += NT) {
             const uint32_t v = all_react ? i : (uint32_t)lists(b)[i];
-            const Vox<K> c = lat[v];
+            const Vox<K> c = cur[v];
             const uint32_t rv = P.reservoir ? (uint32_t)P.reservoir[rd.base + v] : 0u;
             if (rv != 0u || zero_order || !vox_empty<K>(c)) {
                 const uint32_t w3 = d_philox(v, fr, 0u, 0u, k0, k1).w;
                 const bool calm =
                     rv == 0u && !zero_order && calm_voxel<K>(c, w3, quiet, P.T.QS, one, g23, a2, P.T.tau);
-                if (!calm) dec[atomicAdd(&cnt[3], 1u)] = v;
+                if (!calm) dec[atomicAdd(n_pend, 1u)] = v;
             }
         }
-        if (tid == 0) cnt[b ^ 1u] = 0u;
         __syncthreads();
-        const uint32_t np = cnt[3];
+        const uint32_t np = *n_pend;
         if (warp < (uint32_t)NSSA) {
             float* const ws = reinterpret_cast<float*>(sm + L.ws) + (size_t)warp * SSA_WARP_SCRATCH;
             for (uint32_t q = warp; q < np; q += NSSA) {
                 const uint32_t v = dec[q];
-                Vox<K> r = lat[v];
+                Vox<K> r = cur[v];
                 const uint32_t rv = P.reservoir ? (uint32_t)P.reservoir[rd.base + v] : 0u;
                 const uint32_t w3 = d_philox(v, fr, 0u, 0u, k0, k1).w;
                 react_voxel_warp<K>(r, rv, v, fr, k0, k1, rd.rate_mult, ci, P.T, nullptr, counts, s_diag, w3, ws);
-                if (lane == 0u) lat[v] = r;
+                if (lane == 0u) cur[v] = r;
                 __syncwarp();
             }
         }
-        __syncthreads();
-        for (uint32_t q = tid; q < np; q += NT) dec[q] = 0u;
         if (all_react) {
-            // reactions may have filled empty voxels: list the occupied ones afresh
+            // reactions may fill empty voxels: the lists and marks start afresh from the lattice
+            for (uint32_t i = tid; i < mark_words; i += NT) {
+                mark_cur[i] = 0u;
+                mark_nx[i] = 0u;
+            }
+            for (uint32_t v = tid; v < V; v += NT) nx[v] = vox_zero<K>();
+            nw_prev = 0u;
+            __syncthreads();
             for (uint32_t base = warp * 32u; base < V; base += NT) {
                 const uint32_t v = base + lane;
-                warp_append(v < V && !vox_empty<K>(lat[v]), v, lists(b ^ 1u), &cnt[b ^ 1u], lane);
+                const bool occupied = v < V && !vox_empty<K>(cur[v]);
+                if (occupied) set_mark(mark_cur, v);
+                warp_append(occupied, v, lists(b ^ 1u), &cnt[b ^ 1u], lane);
             }
             b ^= 1u;
         }
-        if (tid == 0) cnt[3] = 0u;
         __syncthreads();
     }
 
-    for (uint32_t v = tid; v < V; v += NT) st_vox_g<K>(P.dst + (rd.base + v) * K, lat[v]);
+    for (uint32_t v = tid; v < V; v += NT) st_vox_g<K>(P.dst + (rd.base + v) * K, cur[v]);
     for (uint32_t i = tid; i < PD_N; i += NT)
         if (s_diag[i]) atomicAdd(P.diag + i, s_diag[i]);
     if (blockIdx.x == 0 && tid == 0) P.stepbuf[RP.stepbuf_out] = RP.frame0 + RP.n_frames;
