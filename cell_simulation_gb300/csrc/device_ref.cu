@@ -535,17 +535,20 @@ __device__ __forceinline__ void ref_pdl_start() {
     asm volatile("griddepcontrol.wait;\n" ::: "memory");
 }
 
-__global__ void __launch_bounds__(256) ref_sp_list_act(RefSparse sp) {
-    ref_pdl_start();
+__device__ __forceinline__ void ref_sp_list_act_body(RefSparse sp) {
     for (uint32_t i0 = grid_tid() & ~31u; i0 < sp.W; i0 += grid_threads()) {
         const uint32_t i = i0 + (threadIdx.x & 31u);
         warp_compact(i < sp.W ? act_cur(sp)[i] : 0u, i, sp.act_list, sp.cnt + 0);
     }
 }
 
-// The touch list, and the union list of act bitmap c and the touch bitmap.
-__global__ void __launch_bounds__(256) ref_sp_list_touch(RefSparse sp) {
+__global__ void __launch_bounds__(256) ref_sp_list_act(RefSparse sp) {
     ref_pdl_start();
+    ref_sp_list_act_body(sp);
+}
+
+// The touch list, and the union list of act bitmap c and the touch bitmap.
+__device__ __forceinline__ void ref_sp_list_touch_body(RefSparse sp) {
     for (uint32_t i0 = grid_tid() & ~31u; i0 < sp.W; i0 += grid_threads()) {
         const uint32_t i = i0 + (threadIdx.x & 31u);
         const uint32_t t = i < sp.W ? __ldcg(sp.touch_bm + i) : 0u;
@@ -555,15 +558,19 @@ __global__ void __launch_bounds__(256) ref_sp_list_touch(RefSparse sp) {
     }
 }
 
+__global__ void __launch_bounds__(256) ref_sp_list_touch(RefSparse sp) {
+    ref_pdl_start();
+    ref_sp_list_touch_body(sp);
+}
+
 // Pass 1: directions of every particle of the act list; departures, arrival
 // counts, touched voxels and the contention test.  Also marks the voxels whose
 // reaction seed itime + x*y + z is 0 this frame, clears act bitmap c ^ 1 (the
 // reaction pass fills it) and the touch and union list counters.
-__global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse sp, const uint8_t* __restrict__ slots,
-                                                         const uint32_t* __restrict__ occ,
-                                                         const uint32_t* __restrict__ itimes, uint32_t step,
+__device__ __forceinline__ void ref_sp_directions_body(RefParams p, RefSparse sp, const uint8_t* slots,
+                                                         const uint32_t* occ,
+                                                         const uint32_t* itimes, uint32_t step,
                                                          uint32_t* diag, uint32_t* contended, uint32_t stage_P) {
-    ref_pdl_start();
     const uint32_t itime = __ldg(itimes + step);
     const uint32_t K = p.K;
     const uint32_t n = __ldcg(sp.cnt + 0);
@@ -637,11 +644,18 @@ __global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse 
     }
 }
 
-// Pass 2 (frames without contention): the gather of every touched voxel, in place.
-__global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, uint8_t* __restrict__ slots,
-                                                     uint32_t* __restrict__ occ, int32_t* __restrict__ conc,
-                                                     const uint32_t* __restrict__ contended) {
+__global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse sp, const uint8_t* __restrict__ slots,
+                                                         const uint32_t* __restrict__ occ,
+                                                         const uint32_t* __restrict__ itimes, uint32_t step,
+                                                         uint32_t* diag, uint32_t* contended, uint32_t stage_P) {
     ref_pdl_start();
+    ref_sp_directions_body(p, sp, slots, occ, itimes, step, diag, contended, stage_P);
+}
+
+// Pass 2 (frames without contention): the gather of every touched voxel, in place.
+__device__ __forceinline__ void ref_sp_gather_body(RefParams p, RefSparse sp, uint8_t* slots,
+                                                     uint32_t* occ, int32_t* conc,
+                                                     const uint32_t* contended) {
     if (*contended) return;
     const uint32_t K = p.K, S1 = p.S1;
     const uint32_t n = __ldcg(sp.cnt + 1);
@@ -694,24 +708,30 @@ __global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, 
     }
 }
 
+__global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, uint8_t* __restrict__ slots,
+                                                     uint32_t* __restrict__ occ, int32_t* __restrict__ conc,
+                                                     const uint32_t* __restrict__ contended) {
+    ref_pdl_start();
+    ref_sp_gather_body(p, sp, slots, occ, conc, contended);
+}
+
 // Pass 3 (contended frames): the serial diffusion of rdme.wgsl:45-88 in place,
 // voxels in linear order.  A departing slot still holds its particle when its
 // voxel's turn comes (arrivals only fill empty slots), and a slot that an
 // arrival filled has direction 7.  One block scans the departure bitmap; its
 // first thread makes the moves.
-__global__ void ref_sp_serial(RefParams p, RefSparse sp, uint8_t* __restrict__ slots, uint32_t* __restrict__ occ,
-                              int32_t* __restrict__ conc, uint32_t* diag, const uint32_t* __restrict__ contended) {
-    ref_pdl_start();
+__device__ __forceinline__ void ref_sp_serial_body(RefParams p, RefSparse sp, uint8_t* slots, uint32_t* occ,
+                              int32_t* conc, uint32_t* diag, const uint32_t* contended) {
     if (*contended == 0u) return;
     __shared__ uint32_t s_words[1024];
     const uint32_t K = p.K, S1 = p.S1;
     uint32_t spills = 0;
-    for (uint32_t w0 = 0; w0 < sp.W; w0 += 1024) {
+    for (uint32_t w0 = 0; w0 < sp.W; w0 += blockDim.x) {
         const uint32_t i = w0 + threadIdx.x;
         s_words[threadIdx.x] = i < sp.W ? sp.dep_bm[i] : 0u;
         __syncthreads();
         if (threadIdx.x == 0) {
-            for (uint32_t k = 0; k < 1024 && w0 + k < sp.W; k++) {
+            for (uint32_t k = 0; k < blockDim.x && w0 + k < sp.W; k++) {
                 for (uint32_t m = s_words[k]; m; m &= m - 1u) {
                     const uint32_t v = (w0 + k) * 32u + (uint32_t)(__ffs((int)m) - 1);
                     for (uint32_t s = 0; s < K; s++) {
@@ -740,6 +760,12 @@ __global__ void ref_sp_serial(RefParams p, RefSparse sp, uint8_t* __restrict__ s
         diag[DIAG_SPILL] += spills;
         diag[DIAG_SLOW_STEPS] += 1u;
     }
+}
+
+__global__ void ref_sp_serial(RefParams p, RefSparse sp, uint8_t* __restrict__ slots, uint32_t* __restrict__ occ,
+                              int32_t* __restrict__ conc, uint32_t* diag, const uint32_t* __restrict__ contended) {
+    ref_pdl_start();
+    ref_sp_serial_body(p, sp, slots, occ, conc, diag, contended);
 }
 
 // The reaction pass on one voxel and its bit in act bitmap c ^ 1.
@@ -863,11 +889,10 @@ __device__ __forceinline__ void ref_sp_react(const RefParams& p, const RefSparse
 // Pass 4: the reaction pass over the union list (every voxel when `dense`),
 // setting act bitmap c ^ 1; clears the contention flag, the touch and
 // departure bitmaps and the act list counter for the next frame.
-__global__ void __launch_bounds__(256) ref_sp_cme(RefParams p, RefSparse sp, uint8_t* __restrict__ slots,
-                                                  uint32_t* __restrict__ occ, int32_t* __restrict__ conc,
-                                                  const uint32_t* __restrict__ itimes, uint32_t step, uint32_t dense,
+__device__ __forceinline__ void ref_sp_cme_body(RefParams p, RefSparse sp, uint8_t* slots,
+                                                  uint32_t* occ, int32_t* conc,
+                                                  const uint32_t* itimes, uint32_t step, uint32_t dense,
                                                   int32_t* stat, uint32_t* diag, uint32_t* contended, uint32_t rows) {
-    ref_pdl_start();
     extern __shared__ int32_t s_delta[];  // [S1] + 2 counters, then (rows) the tables and the rows
     for (uint32_t s = threadIdx.x; s < p.S1 + 2; s += blockDim.x) s_delta[s] = 0;
     if (grid_tid() == 0) {
@@ -902,6 +927,47 @@ __global__ void __launch_bounds__(256) ref_sp_cme(RefParams p, RefSparse sp, uin
     }
     __syncthreads();
     ref_flush_block(p, s_delta, stat, diag);
+}
+
+__global__ void __launch_bounds__(256) ref_sp_cme(RefParams p, RefSparse sp, uint8_t* __restrict__ slots,
+                                                  uint32_t* __restrict__ occ, int32_t* __restrict__ conc,
+                                                  const uint32_t* __restrict__ itimes, uint32_t step, uint32_t dense,
+                                                  int32_t* stat, uint32_t* diag, uint32_t* contended, uint32_t rows) {
+    ref_pdl_start();
+    ref_sp_cme_body(p, sp, slots, occ, conc, itimes, step, dense, stat, diag, contended, rows);
+}
+
+// Threads of the one-block form below.
+constexpr int REF_BLOCK_THREADS = 512;
+// Lattices of at most this many voxels run every frame of a call in the one-block form: one SM does
+// such a frame's work sooner than six launches take to run back to back.
+constexpr uint64_t REF_BLOCK_MAX_VOXELS = 16384;
+
+// Every frame of a step call in one block: the passes' own bodies in the same order, with block
+// barriers where the launches were (the serial pass runs on the same block).  The bodies read
+// nothing that the block writes through the non-coherent path (their pointers carry no
+// __restrict__ here), so each pass sees the previous one's writes after the barrier.
+__global__ void __launch_bounds__(REF_BLOCK_THREADS, 1)
+    ref_sp_frames_block(RefParams p, RefSparse sp, uint8_t* slots, uint32_t* occ, int32_t* conc,
+                        const uint32_t* itimes, uint32_t step0, uint32_t n, uint32_t dense_first,
+                        uint32_t dense_always, int32_t* stat, uint32_t* diag, uint32_t* contended, uint32_t stage_P,
+                        uint32_t rows) {
+    for (uint32_t k = 0; k < n; k++) {
+        ref_sp_list_act_body(sp);
+        __syncthreads();
+        ref_sp_directions_body(p, sp, slots, occ, itimes, step0 + k, diag, contended, stage_P);
+        __syncthreads();
+        ref_sp_list_touch_body(sp);
+        __syncthreads();
+        ref_sp_gather_body(p, sp, slots, occ, conc, contended);
+        __syncthreads();
+        ref_sp_serial_body(p, sp, slots, occ, conc, diag, contended);
+        __syncthreads();
+        const uint32_t dense = ((k == 0u && dense_first) || dense_always) ? 1u : 0u;
+        ref_sp_cme_body(p, sp, slots, occ, conc, itimes, step0 + k, dense, stat, diag, contended, rows);
+        __syncthreads();
+        sp.c ^= 1u;
+    }
 }
 
 // Act bitmap c of a freshly uploaded lattice.
@@ -1115,19 +1181,48 @@ static void ref_launch(void (*kernel)(KArgs...), int grid, int block, size_t sme
     CS_CUDA(cudaLaunchKernelEx(&cfg, kernel, args...));
 }
 
+// Shared memory of the reaction pass in blocks of tb threads: it stages the tables and one
+// concentration row per thread when they fit in the default 48 KB (rows = 1).
+static size_t ref_cme_smem(const RefParams& p, int tb, uint32_t& rows) {
+    const size_t smem_rows =
+        ((size_t)p.S1 + 2 + 4 * ((size_t)p.R + 1) + ((size_t)p.R + 1) * p.S1 + (size_t)tb * p.S1) * 4;
+    rows = smem_rows <= 48u * 1024u ? 1u : 0u;
+    return rows ? smem_rows : (p.S1 + 2) * sizeof(int32_t);
+}
+
+// The directions pass stages the probability table in shared memory when it takes at most 16 KB.
+static size_t ref_dir_smem(const RefParams& p, uint32_t& stage_P) {
+    const size_t smem_P = (size_t)p.NR * p.NR * p.S1 * sizeof(float);
+    stage_P = smem_P <= 16u * 1024u ? 1u : 0u;
+    return stage_P ? smem_P : 0u;
+}
+
+static bool ref_one_block(const DeviceRef* d) { return d->p.V <= REF_BLOCK_MAX_VOXELS; }
+
+// Frames k0 .. k0 + n - 1 of the call (itimes[k]) in one launch of the one-block form.
+static void ref_enqueue_block(DeviceRef* d, uint32_t k0, uint32_t n) {
+    if (n == 0) return;
+    const RefParams& p = d->p;
+    const RefSparse sp = ref_sparse(d);
+    uint32_t rows = 0, stage_P = 0;
+    const size_t smem = std::max(ref_cme_smem(p, REF_BLOCK_THREADS, rows), ref_dir_smem(p, stage_P));
+    ref_sp_frames_block<<<1, REF_BLOCK_THREADS, smem, d->stream>>>(
+        p, sp, d->slots.p, d->occ.p, d->conc.p, (const uint32_t*)d->itimes.p, k0, n, d->dense_next ? 1u : 0u,
+        d->dense_always ? 1u : 0u, d->stat.p, d->diag.p, d->flag.p, stage_P, rows);
+    CS_LAUNCH_CHECK();
+    d->dense_next = false;
+    d->par ^= n & 1u;
+}
+
 static void ref_enqueue_frame(DeviceRef* d, uint32_t k) {
     const RefParams& p = d->p;
     const RefSparse sp = ref_sparse(d);
     const int TB = 256;
-    // the reaction pass stages the tables and one concentration row per thread in shared memory when
-    // they fit in the default 48 KB
-    const size_t smem_rows = ((size_t)p.S1 + 2 + 4 * ((size_t)p.R + 1) + ((size_t)p.R + 1) * p.S1 + (size_t)TB * p.S1) * 4;
-    const uint32_t rows = smem_rows <= 48u * 1024u ? 1u : 0u;
-    const size_t smem = rows ? smem_rows : (p.S1 + 2) * sizeof(int32_t);
+    uint32_t rows = 0, stage_P = 0;
+    const size_t smem = ref_cme_smem(p, TB, rows);
     ref_launch(ref_sp_list_act, d->grid, TB, 0, d->stream, sp);
-    const size_t smem_P = (size_t)p.NR * p.NR * p.S1 * sizeof(float);
-    const uint32_t stage_P = smem_P <= 16u * 1024u ? 1u : 0u;
-    ref_launch(ref_sp_directions, d->grid, TB, stage_P ? smem_P : 0, d->stream, p, sp, (const uint8_t*)d->slots.p,
+    const size_t smem_P = ref_dir_smem(p, stage_P);
+    ref_launch(ref_sp_directions, d->grid, TB, smem_P, d->stream, p, sp, (const uint8_t*)d->slots.p,
                (const uint32_t*)d->occ.p, (const uint32_t*)d->itimes.p, k, d->diag.p, d->flag.p, stage_P);
     ref_launch(ref_sp_list_touch, d->grid, TB, 0, d->stream, sp);
     ref_launch(ref_sp_gather, d->grid, TB, 0, d->stream, p, sp, d->slots.p, d->occ.p, d->conc.p, d->flag.p);
@@ -1141,6 +1236,10 @@ static void ref_enqueue_frame(DeviceRef* d, uint32_t k) {
 }
 
 static void ref_enqueue(DeviceRef* d, uint32_t n) {
+    if (ref_one_block(d)) {
+        ref_enqueue_block(d, 0, n);
+        return;
+    }
     for (uint32_t k = 0; k < n; k++) ref_enqueue_frame(d, k);
 }
 
@@ -1159,15 +1258,19 @@ void ref_step(DeviceRef* d, uint32_t n_steps, const uint32_t* itimes, uint64_t f
     if (!sample_frames.empty() && d->sample_ring.n < sample_frames.size() * p.S1)
         d->sample_ring.alloc(sample_frames.size() * p.S1);
     size_t si = 0;
+    uint32_t k0 = 0;  // first frame not yet enqueued (the one-block form runs the frames between samples)
     for (uint32_t k = 0; k < n_steps; k++) {
         uint64_t f = frame0 + k;
         if (si < sample_frames.size() && sample_frames[si] == f) {
+            if (ref_one_block(d)) ref_enqueue_block(d, k0, k - k0);
+            k0 = k;
             CS_CUDA(cudaMemcpyAsync(d->sample_ring.p + si * p.S1, d->stat.p, p.S1 * sizeof(int32_t),
                                     cudaMemcpyDeviceToDevice, d->stream));
             si++;
         }
-        ref_enqueue_frame(d, k);
+        if (!ref_one_block(d)) ref_enqueue_frame(d, k);
     }
+    if (ref_one_block(d)) ref_enqueue_block(d, k0, n_steps - k0);
     if (!sample_frames.empty()) {
         std::vector<int32_t> h(sample_frames.size() * p.S1);
         CS_CUDA(cudaMemcpyAsync(h.data(), d->sample_ring.p, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, d->stream));
