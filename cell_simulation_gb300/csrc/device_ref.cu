@@ -526,7 +526,6 @@ __device__ __forceinline__ void warp_compact(uint32_t m, uint32_t i, uint32_t* l
     for (; m; m &= m - 1u) list[base++] = i * 32u + (uint32_t)(__ffs((int)m) - 1);
 }
 
-// The act list of act bitmap c.
 // Programmatic dependent launch between the passes of a frame: a pass lets the next one launch at
 // once and waits for the previous one to complete (and its memory to be visible) before it touches
 // anything; without a programmatic dependency the wait returns at once.
@@ -535,6 +534,11 @@ __device__ __forceinline__ void ref_pdl_start() {
     asm volatile("griddepcontrol.wait;\n" ::: "memory");
 }
 
+// Each pass is a device body with grid-stride loops, run by its own launch (a thin kernel that
+// waits for the previous pass first) or, on small lattices, by the one-block form
+// ref_sp_frames_block.
+
+// The act list of act bitmap c.
 __device__ __forceinline__ void ref_sp_list_act_body(RefSparse sp) {
     for (uint32_t i0 = grid_tid() & ~31u; i0 < sp.W; i0 += grid_threads()) {
         const uint32_t i = i0 + (threadIdx.x & 31u);
@@ -568,9 +572,8 @@ __global__ void __launch_bounds__(256) ref_sp_list_touch(RefSparse sp) {
 // reaction seed itime + x*y + z is 0 this frame, clears act bitmap c ^ 1 (the
 // reaction pass fills it) and the touch and union list counters.
 __device__ __forceinline__ void ref_sp_directions_body(RefParams p, RefSparse sp, const uint8_t* slots,
-                                                         const uint32_t* occ,
-                                                         const uint32_t* itimes, uint32_t step,
-                                                         uint32_t* diag, uint32_t* contended, uint32_t stage_P) {
+                                                       const uint32_t* occ, const uint32_t* itimes, uint32_t step,
+                                                       uint32_t* diag, uint32_t* contended, uint32_t stage_P) {
     const uint32_t itime = __ldg(itimes + step);
     const uint32_t K = p.K;
     const uint32_t n = __ldcg(sp.cnt + 0);
@@ -653,9 +656,8 @@ __global__ void __launch_bounds__(256) ref_sp_directions(RefParams p, RefSparse 
 }
 
 // Pass 2 (frames without contention): the gather of every touched voxel, in place.
-__device__ __forceinline__ void ref_sp_gather_body(RefParams p, RefSparse sp, uint8_t* slots,
-                                                     uint32_t* occ, int32_t* conc,
-                                                     const uint32_t* contended) {
+__device__ __forceinline__ void ref_sp_gather_body(RefParams p, RefSparse sp, uint8_t* slots, uint32_t* occ,
+                                                   int32_t* conc, const uint32_t* contended) {
     if (*contended) return;
     const uint32_t K = p.K, S1 = p.S1;
     const uint32_t n = __ldcg(sp.cnt + 1);
@@ -721,7 +723,7 @@ __global__ void __launch_bounds__(256) ref_sp_gather(RefParams p, RefSparse sp, 
 // arrival filled has direction 7.  One block scans the departure bitmap; its
 // first thread makes the moves.
 __device__ __forceinline__ void ref_sp_serial_body(RefParams p, RefSparse sp, uint8_t* slots, uint32_t* occ,
-                              int32_t* conc, uint32_t* diag, const uint32_t* contended) {
+                                                   int32_t* conc, uint32_t* diag, const uint32_t* contended) {
     if (*contended == 0u) return;
     __shared__ uint32_t s_words[1024];
     const uint32_t K = p.K, S1 = p.S1;
@@ -889,10 +891,9 @@ __device__ __forceinline__ void ref_sp_react(const RefParams& p, const RefSparse
 // Pass 4: the reaction pass over the union list (every voxel when `dense`),
 // setting act bitmap c ^ 1; clears the contention flag, the touch and
 // departure bitmaps and the act list counter for the next frame.
-__device__ __forceinline__ void ref_sp_cme_body(RefParams p, RefSparse sp, uint8_t* slots,
-                                                  uint32_t* occ, int32_t* conc,
-                                                  const uint32_t* itimes, uint32_t step, uint32_t dense,
-                                                  int32_t* stat, uint32_t* diag, uint32_t* contended, uint32_t rows) {
+__device__ __forceinline__ void ref_sp_cme_body(RefParams p, RefSparse sp, uint8_t* slots, uint32_t* occ,
+                                                int32_t* conc, const uint32_t* itimes, uint32_t step, uint32_t dense,
+                                                int32_t* stat, uint32_t* diag, uint32_t* contended, uint32_t rows) {
     extern __shared__ int32_t s_delta[];  // [S1] + 2 counters, then (rows) the tables and the rows
     for (uint32_t s = threadIdx.x; s < p.S1 + 2; s += blockDim.x) s_delta[s] = 0;
     if (grid_tid() == 0) {
