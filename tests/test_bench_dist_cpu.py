@@ -68,3 +68,18 @@ def test_profiled_traffic_covers_the_reported_kernels():
     for kernel in ("sweep_pass_kernel<5>", "sweep_pass_kernel<3>", "brick_step_kernel", "prod_step_kernel"):
         t = bench.profiled_traffic(kernel, "c3_multi_region_256x256x256_K16")
         assert t is not None and t > 1e7, kernel
+
+
+def test_reference_arm_follows_the_workload():
+    """`--workload` picks the lattice of the main leg and of the reference arm: the 64 x 64 x 1 case
+    runs on the host cores as a whole lattice (its CPU sample is all 64 planes)."""
+    import json
+
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    res = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "c1", "--steps", "2",
+                          "--warmup", "3"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    line = json.loads(res.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert line["config"]["workload"].startswith("c1_plain_64x64x1_K8 (64-plane")
+    assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
