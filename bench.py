@@ -400,7 +400,7 @@ def main():
                     help="only the 512-replicate ensemble leg: --steps batched frames, a tenth as many plain ones "
                          "(for profiling; prints that leg's numbers)")
     ap.add_argument("--refrng-only", action="store_true",
-                    help="only the reference-RNG CUDA path on the 256^3 cell: --steps frames (for profiling)")
+                    help="only the reference-RNG CUDA path on the --workload lattice: --steps frames (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = env_rank()
@@ -415,7 +415,8 @@ def main():
         print(json.dumps(ensemble_numbers(local, args.steps, max(1, args.steps // 10), args.variant)), flush=True)
         return
     if args.refrng_only:
-        print(json.dumps(reference_rng_leg(configs.c3_multi_region(), local, args.steps, args.warmup)), flush=True)
+        w = getattr(configs, WORKLOADS[args.workload])()
+        print(json.dumps(reference_rng_leg(w, local, args.steps, args.warmup)), flush=True)
         return
 
     dist = Dist(world)
