@@ -218,8 +218,9 @@ CPU_SLABS = {"c1": 64, "c2": 16, "c3": CPU_SLAB, "c5": 8}  # the same, per workl
 def reference_arm(args, rank, world):
     """The reference's algorithm on the host cores: the oracle's restatement of the WGSL shaders
     (the reference itself needs Vulkan and a Rust toolchain), on the same central slab of the
-    workload's lattice as cpu_baseline (the 256^3 cell by default).  The slab is cut from the lattice the product library's host model
-    builder makes (outside the timed region); the timed loop runs the oracle alone."""
+    workload's lattice as cpu_baseline (the 256^3 cell by default).  The slab is cut from the
+    lattice the product library's host model builder makes (outside the timed region); the timed
+    loop runs the oracle alone."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
