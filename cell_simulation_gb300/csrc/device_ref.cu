@@ -942,8 +942,9 @@ __global__ void __launch_bounds__(256) ref_sp_cme(RefParams p, RefSparse sp, uin
 constexpr int REF_BLOCK_THREADS = 512;
 // Lattices of at most this many voxels run every frame of a call in the one-block form: one SM does
 // such a frame's work sooner than six launches take to run back to back.  Measured on cubic
-// lattices, 1 particle in 40 voxels: six launches take 31-36 us a frame at any size from 4,096 to
-// 110,592 voxels, the one block 22.9 us at 4,096 and 69.8 us at 13,824 voxels.
+// lattices with one particle per 16 voxels: six launches take 31-36 us a frame at any size from
+// 4,096 to 110,592 voxels, the one block 22.9 us at 4,096 and 69.8 us at 13,824 voxels (its time
+// follows the particles).
 constexpr uint64_t REF_BLOCK_MAX_VOXELS = 6144;
 
 // Every frame of a step call in one block: the passes' own bodies in the same order, with block
