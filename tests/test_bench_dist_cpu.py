@@ -83,3 +83,22 @@ def test_reference_arm_follows_the_workload():
     assert line["impl"] == "reference"
     assert line["config"]["workload"].startswith("c1_plain_64x64x1_K8 (64-plane")
     assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
+
+
+def test_every_variant_is_described():
+    """bench.py names every compiled variant (tile pipeline, bricks, the sweep stream's forms and
+    the resident form), its frame's kernels and its launches per step call."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from cell_simulation_gb300 import tiling_kinds, tiling_variants
+
+    kinds = tiling_kinds()
+    for i in range(len(tiling_variants())):
+        d = bench.describe_variant(i)
+        assert d["index"] == i and d["kind"] in ("tile", "brick", "stream", "resident")
+        assert bench.frame_kernels(d)
+        if d["kind"] == "resident" or d.get("multi_frame"):
+            assert bench.launches_in_call(i, 20) == 1
+        else:
+            assert bench.launches_in_call(i, 20) == 20 * bench.launches_per_frame(i)
+    assert sum(1 for k in kinds if k[0] == 3) == 2
